@@ -1,0 +1,215 @@
+"""aran_gb300 -- GB300-native FMM behind LibAran's 3D solver interface.
+
+Python mirror of the reference's ``AranSolver3d`` (aran/aransolver3d.h:68-170)
+on top of the C ABI of ``libaran_gpu.so`` (declared in include/aran_gpu.h).
+Everything computes on the GPU; when the CUDA library or a device is missing,
+the calls raise instead of falling back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libaran_gpu.so")
+
+FLAVOUR_NORMAL, FLAVOUR_KKYLIN, FLAVOUR_ROTATE = 0, 1, 2
+FLAVOURS = {"normal": 0, "kkylin": 1, "rotate": 2}
+PRECISIONS = {"fp64": 0, "mixed": 1}
+MEM_HOST, MEM_DEVICE = 0, 1
+STAT_NAMES = ("zero", "p2p", "p2m", "m2m", "m2l", "l2l", "l2p", "p2l", "m2p",
+              "p2p_remote", "m2l_remote")
+STAGE_NAMES = ("total", "sort", "tree", "lists", "p2m", "m2m", "m2l", "l2l", "l2p",
+               "p2p", "h2d", "d2h")
+
+# exported symbols of include/aran_gpu.h
+EXPORTS = (
+    "aran_gpu_solver3d_create", "aran_gpu_solver3d_destroy", "aran_gpu_solver3d_solve",
+    "aran_gpu_solver3d_get_stats", "aran_gpu_solver3d_tree_info",
+    "aran_gpu_solver3d_tree_lists", "aran_gpu_solver3d_expansions",
+    "aran_gpu_solver3d_timings", "aran_gpu_solver3d_launches", "aran_gpu_last_error",
+    "aran_gpu_version",
+)
+
+
+class AranError(RuntimeError):
+    """Raised for every non-zero status of the C ABI."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"aran_gpu error {code}: {msg}")
+        self.code = code
+
+
+class Config3d(C.Structure):
+    _fields_ = [("lb", C.c_double * 3), ("ub", C.c_double * 3), ("maxbox", C.c_int),
+                ("order", C.c_int), ("flavour", C.c_int), ("field", C.c_int),
+                ("precision", C.c_int), ("max_depth", C.c_int)]
+
+
+_lib = None
+
+
+def load(build_if_missing: bool = True):
+    """Load libaran_gpu.so (building it in-tree when absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise OSError(f"{LIB_PATH} is missing; run __graft_entry__.build()")
+        from . import _build
+        _build.build()
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    i64p = C.POINTER(C.c_int64)
+    L.aran_gpu_solver3d_create.argtypes = [C.POINTER(Config3d), C.POINTER(vp)]
+    L.aran_gpu_solver3d_create.restype = C.c_int
+    L.aran_gpu_solver3d_destroy.argtypes = [vp]
+    L.aran_gpu_solver3d_destroy.restype = None
+    L.aran_gpu_solver3d_solve.argtypes = [vp, C.c_int64, vp, vp, vp, vp, C.c_int]
+    L.aran_gpu_solver3d_solve.restype = C.c_int
+    L.aran_gpu_solver3d_get_stats.argtypes = [vp, i64p]
+    L.aran_gpu_solver3d_get_stats.restype = C.c_int
+    L.aran_gpu_solver3d_tree_info.argtypes = [vp, i64p]
+    L.aran_gpu_solver3d_tree_info.restype = C.c_int
+    L.aran_gpu_solver3d_tree_lists.argtypes = [vp] * 8
+    L.aran_gpu_solver3d_tree_lists.restype = C.c_int
+    L.aran_gpu_solver3d_expansions.argtypes = [vp, dp, dp]
+    L.aran_gpu_solver3d_expansions.restype = C.c_int
+    L.aran_gpu_solver3d_timings.argtypes = [vp, dp]
+    L.aran_gpu_solver3d_timings.restype = C.c_int
+    L.aran_gpu_solver3d_launches.argtypes = [vp]
+    L.aran_gpu_solver3d_launches.restype = C.c_int64
+    L.aran_gpu_last_error.restype = C.c_char_p
+    L.aran_gpu_version.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise AranError(rc, load().aran_gpu_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class Solver3d:
+    """GPU counterpart of ``AranSolver3d`` for the Newton potential/field.
+
+    ``lbound``/``ubound``/``maxbox`` are the arguments of
+    ``vsg_prtree3d_new_full``; ``order`` is p of
+    ``aran_development3d_new (0, p)``; ``flavour`` picks the M2M/M2L/L2L
+    family; ``field`` selects newtonfield3 (potential + field) over newtonpot3
+    (potential only); ``precision`` is "fp64" (plain path) or "mixed".
+    """
+
+    def __init__(self, lbound=(0.0, 0.0, 0.0), ubound=(1.0, 1.0, 1.0), *, maxbox=64, order=12,
+                 flavour="rotate", field=True, precision="fp64", max_depth=21):
+        L = load()
+        cfg = Config3d()
+        for k in range(3):
+            cfg.lb[k], cfg.ub[k] = float(lbound[k]), float(ubound[k])
+        cfg.maxbox, cfg.order = int(maxbox), int(order)
+        cfg.flavour = FLAVOURS[flavour] if isinstance(flavour, str) else int(flavour)
+        cfg.field = int(bool(field))
+        cfg.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        cfg.max_depth = int(max_depth)
+        self.cfg = cfg
+        self.order = cfg.order
+        self.field = bool(field)
+        h = C.c_void_p()
+        _check(L.aran_gpu_solver3d_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().aran_gpu_solver3d_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- solve --------------------------------------------------------------
+    def solve(self, xyz, q):
+        """Host arrays in, host arrays out: (potential[n], field[n,3] or None)."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        n = len(q)
+        if xyz.shape != (n, 3):
+            raise ValueError("xyz must be (n, 3)")
+        pot = np.empty(n)
+        fld = np.empty((n, 3)) if self.field else None
+        _check(load().aran_gpu_solver3d_solve(self._h, n, _ptr(xyz), _ptr(q), _ptr(pot),
+                                              _ptr(fld), MEM_HOST))
+        return pot, fld
+
+    def solve_device(self, n, xyz_ptr, q_ptr, pot_ptr, field_ptr=None):
+        """Device pointers (ints, e.g. torch ``data_ptr()``)."""
+        _check(load().aran_gpu_solver3d_solve(self._h, int(n), C.c_void_p(xyz_ptr),
+                                              C.c_void_p(q_ptr),
+                                              C.c_void_p(pot_ptr) if pot_ptr else None,
+                                              C.c_void_p(field_ptr) if field_ptr else None,
+                                              MEM_DEVICE))
+
+    # -- introspection ------------------------------------------------------
+    def get_stats(self) -> dict:
+        st = np.zeros(11, np.int64)
+        _check(load().aran_gpu_solver3d_get_stats(self._h, st.ctypes.data_as(C.POINTER(C.c_int64))))
+        return dict(zip(STAT_NAMES, st.tolist()))
+
+    def tree_info(self) -> dict:
+        info = np.zeros(5, np.int64)
+        _check(load().aran_gpu_solver3d_tree_info(self._h, info.ctypes.data_as(C.POINTER(C.c_int64))))
+        return dict(zip(("nodes", "far", "near", "leaves", "depth"), info.tolist()))
+
+    def tree_lists(self) -> dict:
+        info = self.tree_info()
+        nn, nf, nr = info["nodes"], info["far"], info["near"]
+        ids = np.zeros(nn, np.uint64)
+        beg = np.zeros(nn, np.int32)
+        end = np.zeros(nn, np.int32)
+        leaf = np.zeros(nn, np.uint8)
+        far = np.zeros((nf, 2), np.uint64)
+        near = np.zeros((nr, 2), np.uint64)
+        n = int(self.get_stats()["p2m"])
+        perm = np.zeros(n, np.int32)
+        _check(load().aran_gpu_solver3d_tree_lists(self._h, _ptr(ids), _ptr(beg), _ptr(end),
+                                                   _ptr(leaf), _ptr(far), _ptr(near), _ptr(perm)))
+        return dict(ids=ids, begin=beg, end=end, leaf=leaf, far=far, near=near, perm=perm)
+
+    def expansions(self):
+        nn = self.tree_info()["nodes"]
+        p = self.order
+        nm, nl = p * (p + 1) // 2, (p + 1) * (p + 2) // 2
+        mult = np.zeros((nn, nm), np.complex128)
+        loc = np.zeros((nn, nl), np.complex128)
+        _check(load().aran_gpu_solver3d_expansions(
+            self._h, mult.ctypes.data_as(C.POINTER(C.c_double)),
+            loc.ctypes.data_as(C.POINTER(C.c_double))))
+        return mult, loc
+
+    def timings(self) -> dict:
+        ms = np.zeros(16)
+        _check(load().aran_gpu_solver3d_timings(self._h, ms.ctypes.data_as(C.POINTER(C.c_double))))
+        return dict(zip(STAGE_NAMES, ms[:len(STAGE_NAMES)].tolist()))
+
+    def launches(self) -> int:
+        return int(load().aran_gpu_solver3d_launches(self._h))
+
+
+def version() -> str:
+    return load().aran_gpu_version().decode()

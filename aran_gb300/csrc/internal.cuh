@@ -1,0 +1,159 @@
+// internal.cuh -- device buffers, solver state and kernel entry points shared
+// by the translation units of libaran_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/aran_gpu.h"
+#include "fmm_math.cuh"
+
+namespace aran {
+
+void set_error(const std::string &msg);
+
+struct CudaError {
+  cudaError_t code;
+  std::string where;
+};
+
+#define ACHECK(call)                                                          \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess)                                                    \
+      throw ::aran::CudaError{e_, std::string(#call) + " @ " + __FILE__ + ":" + \
+                                      std::to_string(__LINE__)};              \
+  } while (0)
+
+// Grow-only device buffer.
+template <typename T>
+struct DBuf {
+  T *ptr = nullptr;
+  size_t cap = 0;
+  void reserve(size_t n) {
+    if (n <= cap) return;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    size_t c = n + n / 4 + 64;
+    ACHECK(cudaMalloc(&ptr, c * sizeof(T)));
+    cap = c;
+  }
+  // grow keeping the first `keep` elements
+  void grow_keep(size_t n, size_t keep, cudaStream_t st) {
+    if (n <= cap) return;
+    T *old = ptr;
+    size_t c = n + n / 2 + 64;
+    T *np = nullptr;
+    ACHECK(cudaMalloc(&np, c * sizeof(T)));
+    if (old && keep) ACHECK(cudaMemcpyAsync(np, old, keep * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    if (old) {
+      ACHECK(cudaStreamSynchronize(st));
+      cudaFree(old);
+    }
+    ptr = np;
+    cap = c;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+};
+
+template <typename T> struct real4 { T x, y, z, q; };
+
+// Node arrays, level-major (all nodes of depth d are contiguous).
+struct DevTree {
+  int64_t n = 0;
+  int nnodes = 0;
+  int nlevels = 0;
+  int nleaves = 0;                    // non-empty leaves
+  std::vector<int> level_off;        // size nlevels+1 (host)
+  std::vector<int> level_internal;   // internal nodes per level (host)
+  DBuf<uint64_t> key;                 // morton prefix at the node depth
+  DBuf<int> ijk;                      // 3 per node
+  DBuf<uint8_t> depth;
+  DBuf<int> begin, end, child, parent;
+  DBuf<double> center;                // 3 per node
+  DBuf<int> col;                      // 27 per node
+  DBuf<int> ncol;
+  DBuf<int> lf_begin, lf_end;         // leaf-ordinal range below the node
+  DBuf<int> far_off, far_src;         // CSR over nodes
+  DBuf<uint16_t> far_dir;             // offset code (dx+3)+7(dy+3)+49(dz+3)
+  DBuf<int> leaf_node;                // leaf ordinal -> node
+  DBuf<int> near_off, near_rng;       // CSR over leaves of [lf_a, lf_b) ranges (2 ints)
+  DBuf<int> m2l_targets;              // nodes with non-empty far lists
+  int n_m2l_targets = 0;
+  int64_t n_far = 0;
+  int64_t n_near_rng = 0;
+};
+
+// Per-order operator tables (device).  Direction tables: 343 M2L offsets,
+// 8 M2M octants, 8 L2L octants.
+template <typename T>
+struct OpTables {
+  int p = -1;
+  int stride_m2l = 0, stride_m2m = 0, stride_l2l = 0;
+  DBuf<T> rec;      // 2*tri(p+1)
+  DBuf<T> p2mf;     // p
+  DBuf<T> vt;       // tri(p+1)*p   (M2L vertical, sign folded)
+  DBuf<T> vm;       // tri(p)*p     (M2M vertical, 2^-l folded)
+  DBuf<T> vl;       // tri(p+1)*(p+1) (L2L vertical, 2^-l folded)
+  DBuf<T> gz, gm;   // gradient coefficients
+  DBuf<T> dir_m2l, dir_m2m, dir_l2l;
+  DBuf<uint8_t> lm; // (l,m) of coefficient index, 2*tri(p+1)
+};
+
+struct Stage {
+  enum { TOTAL, SORT, TREE, LISTS, P2M, M2M, M2L, L2L, L2P, P2P, H2D, D2H, NSTAGE };
+};
+
+}  // namespace aran
+
+struct AranGpuSolver3d {
+  AranGpuConfig3d cfg;
+  int device = 0;
+  cudaStream_t s0 = nullptr, s1 = nullptr;
+  cudaEvent_t ev[2 * aran::Stage::NSTAGE] = {};
+  cudaEvent_t ev_p2p_done = nullptr, ev_lists_done = nullptr;
+  double scale_e = 1.;   // 2^E >= root extent
+  aran::OpTables<double> t64;
+  aran::OpTables<float> t32;
+  aran::DevTree tree;
+  // particles (sorted)
+  aran::DBuf<uint64_t> keys_in, keys_out;
+  aran::DBuf<int> idx_in, perm;
+  aran::DBuf<uint8_t> cub_tmp;
+  aran::DBuf<double> sx, sy, sz, sq;     // sorted FP64 positions/charges
+  aran::DBuf<aran::real4<double>> rel64;
+  aran::DBuf<aran::real4<float>> rel32;
+  aran::DBuf<double> acc_pot, acc_fld;   // sorted accumulators (FP64)
+  aran::DBuf<double> io_xyz, io_q, io_pot, io_fld;  // staging for host calls
+  aran::DBuf<double> mult64, loc64;
+  aran::DBuf<float> mult32, loc32;
+  aran::DBuf<int> scan_tmp;
+  aran::DBuf<unsigned long long> stats_dev;
+  int64_t stats[11] = {};
+  double ms[16] = {};
+  int64_t launches = 0;
+  bool have_tree = false;
+};
+
+namespace aran {
+
+// tree.cu
+void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double *d_q);
+void build_lists(AranGpuSolver3d *s);
+// tables.cu
+void build_tables(AranGpuSolver3d *s);
+// passes.cu
+void run_passes(AranGpuSolver3d *s);
+void compute_stats(AranGpuSolver3d *s);
+void copy_expansions(AranGpuSolver3d *s, double *mult, double *local);
+
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+}  // namespace aran

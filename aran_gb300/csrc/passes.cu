@@ -1,0 +1,821 @@
+// passes.cu -- the FMM passes on the device.
+//
+// LibAran runs them as callbacks from tree traversals (aran/aransolver3d.c):
+//   clear_func :399-410   -> one memset of all expansions
+//   up_func :412-450      -> k_p2m (leaves) + k_m2m_rotate (level by level)
+//   far_func :333-354     -> k_m2l_rotate (every directed far pair)
+//   near_func :254-324    -> k_p2p (every leaf against its near ranges)
+//   down_func :452-490    -> k_l2l_rotate (level by level) + k_l2p
+// The operators are the "point and shoot" rotation flavour of
+// aran/aransphericalseriesd-rotate.c (rotate to the z axis, translate along
+// z, rotate back), with even/odd real rotation blocks and the z-phases
+// applied separately; expansions are stored scaled per level (see
+// fmm_math.cuh).  Every kernel is templated on the arithmetic type: double
+// for the plain FP64 path, float for the mixed path (whose P2P/L2P results
+// are accumulated in FP64).
+#include "internal.cuh"
+
+namespace aran {
+
+int dir_offset(int p, int kind, int what);
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T inv_scale(int depth, double scale_e) {
+  // 1/h_d = 2^d / 2^E (exact power of two)
+  return (T)(ldexp(1.0, depth) / scale_e);
+}
+
+// ---------------------------------------------------------------------------
+// P2M: aran/arandevelopment3d.c:169-216, one warp per non-empty leaf.
+// Mhat_l^m = sum_i q_i 4pi/(2l+1) conj(S_l^m(xhat_i)), S = r^l Y_l^m by the
+// trig-free recurrence of fmm_math.cuh.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_p2m(int nleaves, const int *__restrict__ leaf_node, const int *__restrict__ begin,
+                      const int *__restrict__ end, const uint8_t *__restrict__ depth,
+                      const real4<T> *__restrict__ rel, int p, const T *__restrict__ rec_g,
+                      const T *__restrict__ p2mf_g, double scale_e, cplx<T> *__restrict__ mult) {
+  extern __shared__ unsigned char smem_raw[];
+  const int nm = tri(p);
+  T *rec = reinterpret_cast<T *>(smem_raw);
+  T *p2mf = rec + 2 * tri(p + 1);
+  cplx<T> *outs = reinterpret_cast<cplx<T> *>(p2mf + p + 1 + ((p + 1) & 1));
+  for (int i = threadIdx.x; i < 2 * tri(p + 1); i += blockDim.x) rec[i] = rec_g[i];
+  for (int i = threadIdx.x; i <= p; i += blockDim.x) p2mf[i] = p2mf_g[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int L = blockIdx.x * (blockDim.x >> 5) + w;
+  if (L >= nleaves) return;
+  cplx<T> *out = outs + w * nm;
+  for (int c = lane; c < nm; c += 32) out[c] = cmake<T>(0, 0);
+  __syncwarp();
+  const int node = leaf_node[L];
+  const int b = begin[node], e = end[node];
+  const T ih = inv_scale<T>(depth[node], scale_e);
+  for (int base = b; base < e; base += 32) {
+    int i = base + lane;
+    T x = 0, y = 0, z = 0, q = 0;
+    if (i < e) {
+      real4<T> r = rel[i];
+      x = r.x * ih;
+      y = r.y * ih;
+      z = r.z * ih;
+      q = r.q;
+    }
+    T r2 = x * x + y * y + z * z;
+    cplx<T> diag = cmake<T>(rec[0], 0);
+    for (int m = 0; m < p; ++m) {
+      if (m > 0) {
+        T a = rec[2 * tri(m, m)];
+        diag = cmake<T>(a * (x * diag.re - y * diag.im), a * (x * diag.im + y * diag.re));
+      }
+      cplx<T> s1 = diag, s2 = cmake<T>(0, 0);
+      for (int l = m; l < p; ++l) {
+        cplx<T> S;
+        if (l == m) S = diag;
+        else {
+          T c0 = rec[2 * tri(l, m)], c1 = rec[2 * tri(l, m) + 1];
+          S = cmake<T>(c0 * z * s1.re - c1 * r2 * s2.re, c0 * z * s1.im - c1 * r2 * s2.im);
+          s2 = s1;
+          s1 = S;
+        }
+        T f = q * p2mf[l];
+        T re = warp_sum<T>(f * S.re);
+        T im = warp_sum<T>(-f * S.im);
+        if (lane == 0) {
+          out[tri(l, m)].re += re;
+          out[tri(l, m)].im += im;
+        }
+      }
+    }
+  }
+  __syncwarp();
+  for (int c = lane; c < nm; c += 32) mult[(size_t)node * nm + c] = out[c];
+}
+
+// ---------------------------------------------------------------------------
+// warp-cooperative pieces of the rotation operators
+// ---------------------------------------------------------------------------
+
+// src[c] = in[c] * e^{i m phi} for degrees < L (layout tri)
+template <typename T>
+__device__ __forceinline__ void load_phased(const cplx<T> *__restrict__ in, int ncoef,
+                                            const uint8_t *lm, const T *ph, cplx<T> *src, int lane) {
+  for (int c = lane; c < ncoef; c += 32) {
+    cplx<T> v = in[c];
+    int m = lm[2 * c + 1];
+    T cr = ph[2 * m], ci = ph[2 * m + 1];
+    src[c] = cmake<T>(v.re * cr - v.im * ci, v.re * ci + v.im * cr);
+  }
+}
+
+// out(l,m') = (sum_m E[l][m'][m] Re in(l,m), sum_m O[l][m'][m] Im in(l,m))
+template <typename T>
+__device__ __forceinline__ cplx<T> rot_one(const T *__restrict__ E, const T *__restrict__ O,
+                                           const cplx<T> *in, int l, int mp) {
+  const T *er = E + sq_off(l) + mp * (l + 1);
+  const T *orow = O + sq_off(l) + mp * (l + 1);
+  const cplx<T> *src = in + tri(l);
+  T re = 0, im = 0;
+  for (int m = 0; m <= l; ++m) {
+    cplx<T> s = src[m];
+    re += er[m] * s.re;
+    im += orow[m] * s.im;
+  }
+  return cmake<T>(re, im);
+}
+
+struct DirOffsets {
+  int ef, of, ei, oi, ph, rp, stride;
+};
+
+// ---------------------------------------------------------------------------
+// M2M rotate: aran/aransphericalseriesd-rotate.c:219-263 applied to the
+// multipole (aran_development3d_m2m_rotate, arandevelopment3d.c:402-409).
+// One warp per internal node of the level, summing its non-empty children.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_m2m_rotate(int cnt, int off, const int *__restrict__ child,
+                             const int *__restrict__ begin, const int *__restrict__ end, int p,
+                             const T *__restrict__ dirs, DirOffsets D, const T *__restrict__ vm,
+                             const uint8_t *__restrict__ lm_g, cplx<T> *__restrict__ mult) {
+  extern __shared__ unsigned char smem_raw[];
+  const int nm = tri(p);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  uint8_t *lm = smem_raw;
+  cplx<T> *bufs = reinterpret_cast<cplx<T> *>(smem_raw + ((2 * tri(p + 1) + 15) & ~15));
+  for (int i = threadIdx.x; i < 2 * tri(p + 1); i += blockDim.x) lm[i] = lm_g[i];
+  __syncthreads();
+  const int P = off + blockIdx.x * wpb + w;
+  if (P >= off + cnt) return;
+  const int c0 = child[P];
+  if (c0 < 0) return;
+  cplx<T> *src = bufs + (size_t)w * 2 * nm;
+  cplx<T> *rot = src + nm;
+  cplx<T> acc[(kMaxOrder * (kMaxOrder + 1) / 2 + 31) / 32];
+  const int K = (nm + 31) / 32;
+#pragma unroll
+  for (int k = 0; k < (kMaxOrder * (kMaxOrder + 1) / 2 + 31) / 32; ++k) acc[k] = cmake<T>(0, 0);
+  for (int o = 0; o < 8; ++o) {
+    int ch = c0 + o;
+    if (end[ch] == begin[ch]) continue;
+    const T *tab = dirs + (size_t)o * D.stride;
+    load_phased(mult + (size_t)ch * nm, nm, lm, tab + D.ph, src, lane);
+    __syncwarp();
+    for (int c = lane; c < nm; c += 32) rot[c] = rot_one(tab + D.ef, tab + D.of, src, lm[2 * c], lm[2 * c + 1]);
+    __syncwarp();
+    // vertical M2M (aran/aransphericalseriesd-translate.c:445-505)
+    const T *rp = tab + D.rp;
+    for (int c = lane; c < nm; c += 32) {
+      int l = lm[2 * c], m = lm[2 * c + 1];
+      const T *vrow = vm + (size_t)c * p;
+      T re = 0, im = 0;
+      for (int n = m; n <= l; ++n) {
+        T f = vrow[n] * rp[l - n];
+        cplx<T> r = rot[tri(n, m)];
+        re += f * r.re;
+        im += f * r.im;
+      }
+      src[c] = cmake<T>(re, im);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < (kMaxOrder * (kMaxOrder + 1) / 2 + 31) / 32; ++k) {
+      int c = lane + 32 * k;
+      if (k < K && c < nm) {
+        int l = lm[2 * c], mp = lm[2 * c + 1];
+        cplx<T> v = rot_one(tab + D.ei, tab + D.oi, src, l, mp);
+        T cr = tab[D.ph + 2 * mp], ci = -tab[D.ph + 2 * mp + 1];
+        acc[k].re += v.re * cr - v.im * ci;
+        acc[k].im += v.re * ci + v.im * cr;
+      }
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int k = 0; k < (kMaxOrder * (kMaxOrder + 1) / 2 + 31) / 32; ++k) {
+    int c = lane + 32 * k;
+    if (k < K && c < nm) mult[(size_t)P * nm + c] = acc[k];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// M2L rotate: aran_spherical_seriesd_to_local_rotate
+// (aran/aransphericalseriesd-rotate.c:165-207) with the vertical M2L of
+// aran/aransphericalseriesd-translate.c:609-676.  One warp per target node,
+// looping over its far list; the target local stays in registers.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_m2l_rotate(int cnt, int off, const int *__restrict__ far_off,
+                             const int *__restrict__ far_src, const uint16_t *__restrict__ far_dir,
+                             const uint8_t *__restrict__ depth, int p, const T *__restrict__ dirs,
+                             DirOffsets D, const T *__restrict__ vt, const uint8_t *__restrict__ lm_g,
+                             double scale_e, const cplx<T> *__restrict__ mult,
+                             cplx<T> *__restrict__ loc) {
+  extern __shared__ unsigned char smem_raw[];
+  const int nm = tri(p), nl = tri(p + 1);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  uint8_t *lm = smem_raw;
+  size_t lmb = (2 * nl + 15) & ~15;
+  T *vts = reinterpret_cast<T *>(smem_raw + lmb);
+  size_t vtb = ((size_t)nl * p * sizeof(T) + 15) & ~15;
+  cplx<T> *bufs = reinterpret_cast<cplx<T> *>(smem_raw + lmb + vtb);
+  for (int i = threadIdx.x; i < 2 * nl; i += blockDim.x) lm[i] = lm_g[i];
+  for (int i = threadIdx.x; i < nl * p; i += blockDim.x) vts[i] = vt[i];
+  __syncthreads();
+  const int t = off + blockIdx.x * wpb + w;
+  if (t >= off + cnt) return;
+  const int j0 = far_off[t], j1 = far_off[t + 1];
+  if (j0 == j1) return;
+  cplx<T> *src = bufs + (size_t)w * (nm + nm + nl);
+  cplx<T> *rot = src + nm;
+  cplx<T> *tr = rot + nm;
+  constexpr int KMAX = ((kMaxOrder + 1) * (kMaxOrder + 2) / 2 + 31) / 32;
+  cplx<T> acc[KMAX];
+#pragma unroll
+  for (int k = 0; k < KMAX; ++k) acc[k] = cmake<T>(0, 0);
+  const int K = (nl + 31) / 32;
+  for (int j = j0; j < j1; ++j) {
+    const int s = far_src[j];
+    const T *tab = dirs + (size_t)far_dir[j] * D.stride;
+    load_phased(mult + (size_t)s * nm, nm, lm, tab + D.ph, src, lane);
+    __syncwarp();
+    for (int c = lane; c < nm; c += 32) rot[c] = rot_one(tab + D.ef, tab + D.of, src, lm[2 * c], lm[2 * c + 1]);
+    __syncwarp();
+    const T *rp = tab + D.rp;
+    for (int c = lane; c < nl; c += 32) {
+      int l = lm[2 * c], m = lm[2 * c + 1];
+      const T *vrow = vts + c * p;
+      T re = 0, im = 0;
+      for (int n = m; n < p; ++n) {
+        T f = vrow[n] * rp[l + n + 1];
+        cplx<T> r = rot[tri(n, m)];
+        re += f * r.re;
+        im += f * r.im;
+      }
+      tr[c] = cmake<T>(re, im);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k) {
+      int c = lane + 32 * k;
+      if (k < K && c < nl) {
+        int l = lm[2 * c], mp = lm[2 * c + 1];
+        cplx<T> v = rot_one(tab + D.ei, tab + D.oi, tr, l, mp);
+        T cr = tab[D.ph + 2 * mp], ci = -tab[D.ph + 2 * mp + 1];
+        acc[k].re += v.re * cr - v.im * ci;
+        acc[k].im += v.re * ci + v.im * cr;
+      }
+    }
+    __syncwarp();
+  }
+  const T ih = inv_scale<T>(depth[t], scale_e);
+#pragma unroll
+  for (int k = 0; k < KMAX; ++k) {
+    int c = lane + 32 * k;
+    if (k < K && c < nl) loc[(size_t)t * nl + c] = cmake<T>(acc[k].re * ih, acc[k].im * ih);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// L2L rotate: aran_development3d_l2l_rotate (arandevelopment3d.c:444-451),
+// vertical part aran/aransphericalseriesd-translate.c:301-364.  One warp per
+// non-empty node of the level, adding its parent's translated local.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_l2l_rotate(int cnt, int off, const int *__restrict__ parent,
+                             const int *__restrict__ child, const int *__restrict__ begin,
+                             const int *__restrict__ end, int p, const T *__restrict__ dirs,
+                             DirOffsets D, const T *__restrict__ vl, const uint8_t *__restrict__ lm_g,
+                             cplx<T> *__restrict__ loc) {
+  extern __shared__ unsigned char smem_raw[];
+  const int nl = tri(p + 1);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  uint8_t *lm = smem_raw;
+  cplx<T> *bufs = reinterpret_cast<cplx<T> *>(smem_raw + ((2 * nl + 15) & ~15));
+  for (int i = threadIdx.x; i < 2 * nl; i += blockDim.x) lm[i] = lm_g[i];
+  __syncthreads();
+  const int C = off + blockIdx.x * wpb + w;
+  if (C >= off + cnt) return;
+  if (end[C] == begin[C]) return;
+  const int P = parent[C];
+  const int o = C - child[P];
+  const T *tab = dirs + (size_t)o * D.stride;
+  cplx<T> *src = bufs + (size_t)w * 2 * nl;
+  cplx<T> *rot = src + nl;
+  load_phased(loc + (size_t)P * nl, nl, lm, tab + D.ph, src, lane);
+  __syncwarp();
+  for (int c = lane; c < nl; c += 32) rot[c] = rot_one(tab + D.ef, tab + D.of, src, lm[2 * c], lm[2 * c + 1]);
+  __syncwarp();
+  const T *rp = tab + D.rp;
+  for (int c = lane; c < nl; c += 32) {
+    int l = lm[2 * c], m = lm[2 * c + 1];
+    const T *vrow = vl + (size_t)c * (p + 1);
+    T re = 0, im = 0;
+    for (int n = l; n <= p; ++n) {
+      T f = vrow[n] * rp[n - l];
+      cplx<T> r = rot[tri(n, m)];
+      re += f * r.re;
+      im += f * r.im;
+    }
+    src[c] = cmake<T>(re, im);
+  }
+  __syncwarp();
+  for (int c = lane; c < nl; c += 32) {
+    int l = lm[2 * c], mp = lm[2 * c + 1];
+    cplx<T> v = rot_one(tab + D.ei, tab + D.oi, src, l, mp);
+    T cr = tab[D.ph + 2 * mp], ci = -tab[D.ph + 2 * mp + 1];
+    cplx<T> cur = loc[(size_t)C * nl + c];
+    cur.re += v.re * cr - v.im * ci;
+    cur.im += v.re * ci + v.im * cr;
+    loc[(size_t)C * nl + c] = cur;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// L2P with gradient: aran_development3d_local_gradient_evaluate
+// (arandevelopment3d.c:542-552, aransphericalseriesd.c:419-546) and the
+// local evaluation of arandevelopment3d.c:485-494.  One block per leaf, one
+// thread per particle.  The gradient uses the derivative identities of the
+// regular solid harmonics (fmm_math.cuh gen_grad_coefs): d/dz and
+// d/dx - i d/dy of a degree-p local are degree-(p-1) locals built once per
+// leaf, so a particle only evaluates S_l^m(xhat) once.
+// ---------------------------------------------------------------------------
+template <typename T, bool FIELD>
+__global__ void k_l2p(int nleaves, const int *__restrict__ leaf_node, const int *__restrict__ begin,
+                      const int *__restrict__ end, const uint8_t *__restrict__ depth,
+                      const real4<T> *__restrict__ rel, int p, const T *__restrict__ rec_g,
+                      const T *__restrict__ gz_g, const T *__restrict__ gm_g, double scale_e,
+                      const cplx<T> *__restrict__ loc, double *__restrict__ acc_pot,
+                      double *__restrict__ acc_fld) {
+  extern __shared__ unsigned char smem_raw[];
+  const int nl = tri(p + 1), nm = tri(p);
+  T *rec = reinterpret_cast<T *>(smem_raw);
+  cplx<T> *Lc = reinterpret_cast<cplx<T> *>(rec + ((2 * nl + 1) & ~1));
+  cplx<T> *A = Lc + nl;
+  cplx<T> *B = A + nm;
+  const int L = blockIdx.x;
+  const int node = leaf_node[L];
+  for (int i = threadIdx.x; i < 2 * nl; i += blockDim.x) rec[i] = rec_g[i];
+  for (int c = threadIdx.x; c < nl; c += blockDim.x) Lc[c] = loc[(size_t)node * nl + c];
+  __syncthreads();
+  if (FIELD) {
+    for (int c = threadIdx.x; c < nm; c += blockDim.x) {
+      // c = tri(l', m): A = L(l'+1, m) * gz
+      int lp = 0;
+      while (tri(lp + 1) <= c) ++lp;
+      int m = c - tri(lp);
+      cplx<T> v = Lc[tri(lp + 1, m)];
+      T g = gz_g[c];
+      A[c] = cmake<T>(v.re * g, v.im * g);
+    }
+    for (int c = threadIdx.x; c < p * p; c += blockDim.x) {
+      int lp = 0;
+      while ((lp + 1) * (lp + 1) <= c) ++lp;
+      int mp = c - lp * lp - lp;
+      int m = mp + 1;
+      cplx<T> v;
+      if (m >= 0) v = Lc[tri(lp + 1, m)];
+      else {
+        cplx<T> u = Lc[tri(lp + 1, -m)];
+        v = ((-m) & 1) ? cmake<T>(-u.re, u.im) : cmake<T>(u.re, -u.im);
+      }
+      T g = gm_g[c];
+      B[c] = cmake<T>(v.re * g, v.im * g);
+    }
+  }
+  __syncthreads();
+  const int b = begin[node], e = end[node];
+  const T ih = inv_scale<T>(depth[node], scale_e);
+  for (int i = b + threadIdx.x; i < e; i += blockDim.x) {
+    real4<T> r = rel[i];
+    T x = r.x * ih, y = r.y * ih, z = r.z * ih;
+    T r2 = x * x + y * y + z * z;
+    T phi = 0, dz = 0, gre = 0, gim = 0;
+    cplx<T> diag = cmake<T>(rec[0], 0);
+    for (int m = 0; m <= p; ++m) {
+      if (m > 0) {
+        T a = rec[2 * tri(m, m)];
+        diag = cmake<T>(a * (x * diag.re - y * diag.im), a * (x * diag.im + y * diag.re));
+      }
+      cplx<T> s1 = diag, s2 = cmake<T>(0, 0);
+      const T wm = m == 0 ? (T)1 : (T)2;
+      const T sg = (m & 1) ? (T)-1 : (T)1;
+      for (int l = m; l <= p; ++l) {
+        cplx<T> S;
+        if (l == m) S = diag;
+        else {
+          T c0 = rec[2 * tri(l, m)], c1 = rec[2 * tri(l, m) + 1];
+          S = cmake<T>(c0 * z * s1.re - c1 * r2 * s2.re, c0 * z * s1.im - c1 * r2 * s2.im);
+          s2 = s1;
+          s1 = S;
+        }
+        cplx<T> Lv = Lc[tri(l, m)];
+        phi += wm * (Lv.re * S.re - Lv.im * S.im);
+        if (FIELD && l < p) {
+          cplx<T> a = A[tri(l, m)];
+          dz += wm * (a.re * S.re - a.im * S.im);
+          cplx<T> bp = B[l * l + l + m];
+          gre += bp.re * S.re - bp.im * S.im;
+          gim += bp.re * S.im + bp.im * S.re;
+          if (m > 0) {
+            // S^{-m} = (-1)^m conj(S^m)
+            cplx<T> bn = B[l * l + l - m];
+            T sre = sg * S.re, sim = -sg * S.im;
+            gre += bn.re * sre - bn.im * sim;
+            gim += bn.re * sim + bn.im * sre;
+          }
+        }
+      }
+    }
+    acc_pot[i] += (double)phi;
+    if (FIELD) {
+      acc_fld[3 * (size_t)i] += (double)(gre * ih);
+      acc_fld[3 * (size_t)i + 1] += (double)(-gim * ih);
+      acc_fld[3 * (size_t)i + 2] += (double)(dz * ih);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// P2P: the near_func of aran/aransolver3d.c:254-324 with the Newton kernels
+// of tests/newtonpot3.c:61-78 (potential) and tests/newtonfield3.c:91-119
+// (field, |r| > 1e-5 guard).  One block per target leaf; every target sums
+// its near ranges directly (both sides of a pair are computed by their own
+// targets instead of the reference's symmetric update).  threads-per-target
+// adapts to the leaf size.  MIXED: FP32 positions relative to the leaf
+// centres, shifted per source leaf, per-source-leaf FP32 partial sums added
+// into FP64 accumulators.
+// ---------------------------------------------------------------------------
+template <typename T, bool FIELD, bool MIXED>
+__global__ void __launch_bounds__(128) k_p2p(
+    int nleaves, const int *__restrict__ leaf_node, const int *__restrict__ begin,
+    const int *__restrict__ end, const double *__restrict__ center, const int *__restrict__ near_off,
+    const int *__restrict__ near_rng, const double *__restrict__ sx, const double *__restrict__ sy,
+    const double *__restrict__ sz, const double *__restrict__ sq, const real4<float> *__restrict__ rel32,
+    double *__restrict__ acc_pot, double *__restrict__ acc_fld) {
+  const int L = blockIdx.x;
+  const int node = leaf_node[L];
+  const int b = begin[node], e = end[node];
+  const int nt = e - b;
+  const int tpt = nt <= 32 ? 4 : (nt <= 64 ? 2 : 1);
+  const int gsz = blockDim.x / tpt;
+  const int sub = threadIdx.x % tpt;
+  const int r0 = near_off[L], r1 = near_off[L + 1];
+  const double cx = center[3 * node], cy = center[3 * node + 1], cz = center[3 * node + 2];
+  for (int tb = 0; tb < nt; tb += gsz) {
+    const int ti = tb + threadIdx.x / tpt;
+    const bool active = ti < nt;
+    const int t = b + (active ? ti : 0);
+    double pot = 0, fx = 0, fy = 0, fz = 0;
+    T tx, ty, tz;
+    if (MIXED) {
+      real4<float> r = rel32[t];
+      tx = r.x; ty = r.y; tz = r.z;
+    } else {
+      tx = sx[t]; ty = sy[t]; tz = sz[t];
+    }
+    for (int rr = r0; rr < r1; ++rr) {
+      const int la = near_rng[2 * rr], lb = near_rng[2 * rr + 1];
+      for (int lf = la; lf < lb; ++lf) {
+        const int sn = leaf_node[lf];
+        const int sb = begin[sn], se = end[sn];
+        if (MIXED) {
+          // target relative to the source leaf centre
+          float ox = tx - (float)(center[3 * sn] - cx);
+          float oy = ty - (float)(center[3 * sn + 1] - cy);
+          float oz = tz - (float)(center[3 * sn + 2] - cz);
+          float p0 = 0.f, f0 = 0.f, f1 = 0.f, f2 = 0.f;
+          for (int j = sb + sub; j < se; j += tpt) {
+            real4<float> sj = rel32[j];
+            float dx = ox - sj.x, dy = oy - sj.y, dz = oz - sj.z;
+            float r2 = dx * dx + dy * dy + dz * dz;
+            bool ok = FIELD ? (r2 > 1e-10f) : (r2 > 0.f);
+            float inv = ok ? rsqrtf(r2) : 0.f;
+            float qi = sj.q * inv;
+            p0 += qi;
+            if (FIELD) {
+              float q3 = qi * inv * inv;
+              f0 -= q3 * dx;
+              f1 -= q3 * dy;
+              f2 -= q3 * dz;
+            }
+          }
+          pot += (double)p0;
+          if (FIELD) { fx += (double)f0; fy += (double)f1; fz += (double)f2; }
+        } else {
+          for (int j = sb + sub; j < se; j += tpt) {
+            double dx = (double)tx - sx[j], dy = (double)ty - sy[j], dz = (double)tz - sz[j];
+            double r2 = dx * dx + dy * dy + dz * dz;
+            bool ok = FIELD ? (r2 > 1e-10) : (j != t);
+            double inv = ok ? rsqrt(r2) : 0.;
+            double qi = sq[j] * inv;
+            pot += qi;
+            if (FIELD) {
+              double q3 = qi * inv * inv;
+              fx -= q3 * dx;
+              fy -= q3 * dy;
+              fz -= q3 * dz;
+            }
+          }
+        }
+      }
+    }
+    // reduce over the tpt threads of this target (consecutive lanes)
+    for (int o = 1; o < tpt; o <<= 1) {
+      pot += __shfl_xor_sync(kFull, pot, o);
+      if (FIELD) {
+        fx += __shfl_xor_sync(kFull, fx, o);
+        fy += __shfl_xor_sync(kFull, fy, o);
+        fz += __shfl_xor_sync(kFull, fz, o);
+      }
+    }
+    if (active && sub == 0) {
+      acc_pot[t] = pot;
+      if (FIELD) {
+        acc_fld[3 * (size_t)t] = fx;
+        acc_fld[3 * (size_t)t + 1] = fy;
+        acc_fld[3 * (size_t)t + 2] = fz;
+      }
+    }
+  }
+}
+
+__global__ void k_scatter(int64_t n, const int *__restrict__ perm, const double *__restrict__ acc_pot,
+                          const double *__restrict__ acc_fld, double *__restrict__ pot,
+                          double *__restrict__ fld) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int o = perm[i];
+  if (pot) pot[o] = acc_pot[i];
+  if (fld) {
+    fld[3 * (int64_t)o] = acc_fld[3 * i];
+    fld[3 * (int64_t)o + 1] = acc_fld[3 * i + 1];
+    fld[3 * (int64_t)o + 2] = acc_fld[3 * i + 2];
+  }
+}
+
+// counters of aran_solver3d_get_stats from the lists
+__global__ void k_stats(int nn, int nleaves, const int *__restrict__ begin, const int *__restrict__ end,
+                        const int *__restrict__ parent, const int *__restrict__ leaf_node,
+                        const int *__restrict__ near_off, const int *__restrict__ near_rng,
+                        unsigned long long *__restrict__ st) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long m2m = 0, p2p2 = 0;
+  if (i < nn && end[i] > begin[i] && parent[i] >= 0) m2m = 1;
+  if (i < nleaves) {
+    int node = leaf_node[i];
+    long long nt = end[node] - begin[node];
+    for (int r = near_off[i]; r < near_off[i + 1]; ++r)
+      for (int lf = near_rng[2 * r]; lf < near_rng[2 * r + 1]; ++lf) {
+        int sn = leaf_node[lf];
+        long long ns = end[sn] - begin[sn];
+        if (sn == node) p2p2 += (unsigned long long)(nt * (nt + 1));  // 2 * n(n+1)/2
+        else p2p2 += (unsigned long long)(nt * ns);                  // counted from both sides
+      }
+  }
+  if (m2m) atomicAdd(&st[0], m2m);
+  if (p2p2) atomicAdd(&st[1], p2p2);
+}
+
+template <typename T>
+DirOffsets offsets(int p, int kind) {
+  DirOffsets d;
+  d.ef = dir_offset(p, kind, 0);
+  d.of = dir_offset(p, kind, 1);
+  d.ei = dir_offset(p, kind, 2);
+  d.oi = dir_offset(p, kind, 3);
+  d.ph = dir_offset(p, kind, 4);
+  d.rp = dir_offset(p, kind, 5);
+  d.stride = dir_offset(p, kind, 6);
+  return d;
+}
+
+template <typename T>
+void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &locb,
+                  const real4<T> *rel) {
+  cudaStream_t st = s->s0;
+  DevTree &t = s->tree;
+  const int p = s->cfg.order;
+  const int nm = tri(p), nl = tri(p + 1);
+  const bool field = s->cfg.field != 0;
+  multb.reserve((size_t)t.nnodes * nm * 2);
+  locb.reserve((size_t)t.nnodes * nl * 2);
+  cplx<T> *mult = reinterpret_cast<cplx<T> *>(multb.ptr);
+  cplx<T> *loc = reinterpret_cast<cplx<T> *>(locb.ptr);
+  s->acc_pot.reserve(t.n);
+  s->acc_fld.reserve(3 * t.n);
+
+  // near field on the second stream, as soon as the lists exist
+  ACHECK(cudaStreamWaitEvent(s->s1, s->ev[2 * Stage::LISTS + 1], 0));
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::P2P], s->s1));
+  {
+    const bool mixed = s->cfg.precision == ARAN_PRECISION_MIXED;
+#define P2P_ARGS                                                                         \
+  t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr, t.center.ptr, t.near_off.ptr,       \
+      t.near_rng.ptr, s->sx.ptr, s->sy.ptr, s->sz.ptr, s->sq.ptr, s->rel32.ptr, s->acc_pot.ptr, \
+      s->acc_fld.ptr
+    if (mixed) {
+      if (field) k_p2p<float, true, true><<<t.nleaves, 128, 0, s->s1>>>(P2P_ARGS);
+      else k_p2p<float, false, true><<<t.nleaves, 128, 0, s->s1>>>(P2P_ARGS);
+    } else {
+      if (field) k_p2p<double, true, false><<<t.nleaves, 128, 0, s->s1>>>(P2P_ARGS);
+      else k_p2p<double, false, false><<<t.nleaves, 128, 0, s->s1>>>(P2P_ARGS);
+    }
+#undef P2P_ARGS
+    ACHECK(cudaGetLastError());
+    s->launches++;
+  }
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::P2P + 1], s->s1));
+
+  // clear (aran/aransolver3d.c:399-410)
+  ACHECK(cudaMemsetAsync(multb.ptr, 0, (size_t)t.nnodes * nm * 2 * sizeof(T), st));
+  ACHECK(cudaMemsetAsync(locb.ptr, 0, (size_t)t.nnodes * nl * 2 * sizeof(T), st));
+  s->launches += 2;
+
+  // P2M
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::P2M], st));
+  {
+    const int WPB = 4;
+    size_t sm = (2 * nl + p + 2) * sizeof(T) + (size_t)WPB * nm * sizeof(cplx<T>) + 64;
+    k_p2m<T><<<ceil_div(t.nleaves, WPB), WPB * 32, sm, st>>>(
+        t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr, t.depth.ptr, rel, p, tb.rec.ptr,
+        tb.p2mf.ptr, s->scale_e, mult);
+    ACHECK(cudaGetLastError());
+    s->launches++;
+  }
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::P2M + 1], st));
+  // M2M, deepest level first
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::M2M], st));
+  {
+    DirOffsets D = offsets<T>(p, 1);
+    const int WPB = 4;
+    size_t sm = ((2 * nl + 15) & ~15) + (size_t)WPB * 2 * nm * sizeof(cplx<T>) + 64;
+    for (int d = t.nlevels - 2; d >= 0; --d) {
+      if (t.level_internal[d] == 0) continue;
+      int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
+      k_m2m_rotate<T><<<ceil_div(cnt, WPB), WPB * 32, sm, st>>>(
+          cnt, off, t.child.ptr, t.begin.ptr, t.end.ptr, p, tb.dir_m2m.ptr, D, tb.vm.ptr,
+          tb.lm.ptr, mult);
+      ACHECK(cudaGetLastError());
+      s->launches++;
+    }
+  }
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::M2M + 1], st));
+  // M2L over every node of depth >= 2
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L], st));
+  if (t.nlevels > 2) {
+    DirOffsets D = offsets<T>(p, 0);
+    const int WPB = 4;
+    int off = t.level_off[2], cnt = t.nnodes - off;
+    size_t sm = ((2 * nl + 15) & ~15) + (((size_t)nl * p * sizeof(T) + 15) & ~15) +
+                (size_t)WPB * (2 * nm + nl) * sizeof(cplx<T>) + 64;
+    if (sm > 48 * 1024)
+      ACHECK(cudaFuncSetAttribute(k_m2l_rotate<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_m2l_rotate<T><<<ceil_div(cnt, WPB), WPB * 32, sm, st>>>(
+        cnt, off, t.far_off.ptr, t.far_src.ptr, t.far_dir.ptr, t.depth.ptr, p, tb.dir_m2l.ptr, D,
+        tb.vt.ptr, tb.lm.ptr, s->scale_e, mult, loc);
+    ACHECK(cudaGetLastError());
+    s->launches++;
+  }
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L + 1], st));
+  // L2L, from depth 3 (depth 0-1 locals are zero: no far pairs above depth 2)
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::L2L], st));
+  {
+    DirOffsets D = offsets<T>(p, 2);
+    const int WPB = 4;
+    size_t sm = ((2 * nl + 15) & ~15) + (size_t)WPB * 2 * nl * sizeof(cplx<T>) + 64;
+    for (int d = 3; d < t.nlevels; ++d) {
+      int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
+      k_l2l_rotate<T><<<ceil_div(cnt, WPB), WPB * 32, sm, st>>>(
+          cnt, off, t.parent.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, p, tb.dir_l2l.ptr, D,
+          tb.vl.ptr, tb.lm.ptr, loc);
+      ACHECK(cudaGetLastError());
+      s->launches++;
+    }
+  }
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::L2L + 1], st));
+  // L2P after the near field has written the accumulators
+  ACHECK(cudaStreamWaitEvent(st, s->ev[2 * Stage::P2P + 1], 0));
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::L2P], st));
+  {
+    size_t sm = ((2 * nl + 1) & ~1) * sizeof(T) + (size_t)(nl + nm + p * p) * sizeof(cplx<T>) + 64;
+    if (field)
+      k_l2p<T, true><<<t.nleaves, 64, sm, st>>>(t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
+                                                 t.depth.ptr, rel, p, tb.rec.ptr, tb.gz.ptr,
+                                                 tb.gm.ptr, s->scale_e, loc, s->acc_pot.ptr,
+                                                 s->acc_fld.ptr);
+    else
+      k_l2p<T, false><<<t.nleaves, 64, sm, st>>>(t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
+                                                  t.depth.ptr, rel, p, tb.rec.ptr, tb.gz.ptr,
+                                                  tb.gm.ptr, s->scale_e, loc, s->acc_pot.ptr,
+                                                  s->acc_fld.ptr);
+    ACHECK(cudaGetLastError());
+    s->launches++;
+  }
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::L2P + 1], st));
+}
+
+}  // namespace
+
+void run_passes(AranGpuSolver3d *s) {
+  if (s->cfg.precision == ARAN_PRECISION_MIXED)
+    run_passes_t<float>(s, s->t32, s->mult32, s->loc32, s->rel32.ptr);
+  else
+    run_passes_t<double>(s, s->t64, s->mult64, s->loc64, s->rel64.ptr);
+}
+
+void scatter_outputs(AranGpuSolver3d *s, double *pot, double *fld) {
+  const int TB = 256;
+  k_scatter<<<ceil_div(s->tree.n, TB), TB, 0, s->s0>>>(s->tree.n, s->perm.ptr, s->acc_pot.ptr,
+                                                        s->cfg.field ? s->acc_fld.ptr : nullptr,
+                                                        pot, s->cfg.field ? fld : nullptr);
+  ACHECK(cudaGetLastError());
+  s->launches++;
+}
+
+void compute_stats(AranGpuSolver3d *s) {
+  DevTree &t = s->tree;
+  s->stats_dev.reserve(2);
+  ACHECK(cudaMemsetAsync(s->stats_dev.ptr, 0, 2 * sizeof(unsigned long long), s->s0));
+  int nmax = t.nnodes > t.nleaves ? t.nnodes : t.nleaves;
+  k_stats<<<ceil_div(nmax, 256), 256, 0, s->s0>>>(t.nnodes, t.nleaves, t.begin.ptr, t.end.ptr,
+                                                  t.parent.ptr, t.leaf_node.ptr, t.near_off.ptr,
+                                                  t.near_rng.ptr, s->stats_dev.ptr);
+  ACHECK(cudaGetLastError());
+  unsigned long long h[2];
+  ACHECK(cudaMemcpyAsync(h, s->stats_dev.ptr, sizeof(h), cudaMemcpyDeviceToHost, s->s0));
+  ACHECK(cudaStreamSynchronize(s->s0));
+  int64_t *st = s->stats;
+  for (int i = 0; i < 11; ++i) st[i] = 0;
+  st[0] = t.nnodes;          // zero
+  st[1] = (int64_t)(h[1] / 2);  // p2p
+  st[2] = t.n;               // p2m
+  st[3] = (int64_t)h[0];     // m2m
+  st[4] = t.n_far;           // m2l
+  st[5] = (int64_t)h[0];     // l2l
+  st[6] = t.n;               // l2p
+}
+
+namespace {
+template <typename T>
+__global__ void k_unscale(int nn, int p, const uint8_t *__restrict__ depth, double scale_e,
+                          const cplx<T> *__restrict__ mult, const cplx<T> *__restrict__ loc,
+                          double *__restrict__ om, double *__restrict__ ol) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  int nm = tri(p), nl = tri(p + 1);
+  double h = scale_e / ldexp(1.0, depth[i]);
+  for (int l = 0; l <= p; ++l) {
+    double hm = pow(h, l), hl = 1.0 / hm;
+    for (int m = 0; m <= l; ++m) {
+      if (l < p && om) {
+        cplx<T> v = mult[(size_t)i * nm + tri(l, m)];
+        om[2 * ((size_t)i * nm + tri(l, m))] = (double)v.re * hm;
+        om[2 * ((size_t)i * nm + tri(l, m)) + 1] = (double)v.im * hm;
+      }
+      if (ol) {
+        cplx<T> v = loc[(size_t)i * nl + tri(l, m)];
+        ol[2 * ((size_t)i * nl + tri(l, m))] = (double)v.re * hl;
+        ol[2 * ((size_t)i * nl + tri(l, m)) + 1] = (double)v.im * hl;
+      }
+    }
+  }
+}
+}  // namespace
+
+void copy_expansions(AranGpuSolver3d *s, double *mult, double *local) {
+  DevTree &t = s->tree;
+  int p = s->cfg.order;
+  size_t nm = tri(p), nl = tri(p + 1);
+  DBuf<double> om, ol;
+  om.reserve(t.nnodes * nm * 2);
+  ol.reserve(t.nnodes * nl * 2);
+  if (s->cfg.precision == ARAN_PRECISION_MIXED)
+    k_unscale<float><<<ceil_div(t.nnodes, 128), 128, 0, s->s0>>>(
+        t.nnodes, p, t.depth.ptr, s->scale_e, reinterpret_cast<cplx<float> *>(s->mult32.ptr),
+        reinterpret_cast<cplx<float> *>(s->loc32.ptr), om.ptr, ol.ptr);
+  else
+    k_unscale<double><<<ceil_div(t.nnodes, 128), 128, 0, s->s0>>>(
+        t.nnodes, p, t.depth.ptr, s->scale_e, reinterpret_cast<cplx<double> *>(s->mult64.ptr),
+        reinterpret_cast<cplx<double> *>(s->loc64.ptr), om.ptr, ol.ptr);
+  ACHECK(cudaGetLastError());
+  if (mult) ACHECK(cudaMemcpyAsync(mult, om.ptr, t.nnodes * nm * 2 * sizeof(double), cudaMemcpyDeviceToHost, s->s0));
+  if (local) ACHECK(cudaMemcpyAsync(local, ol.ptr, t.nnodes * nl * 2 * sizeof(double), cudaMemcpyDeviceToHost, s->s0));
+  ACHECK(cudaStreamSynchronize(s->s0));
+  om.release();
+  ol.release();
+}
+
+}  // namespace aran

@@ -1,0 +1,306 @@
+// solver.cu -- C ABI of libaran_gpu.so and the solve orchestration.
+//
+// aran_gpu_solver3d_solve replaces aran_solver3d_solve
+// (aran/aransolver3d.c:1135-1202) plus the per-point insertion that precedes
+// it: every stage runs on the device, the host only sequences launches.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "internal.cuh"
+
+namespace aran {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+void scatter_outputs(AranGpuSolver3d *s, double *pot, double *fld);
+
+namespace {
+
+int fail(int code, const std::string &msg) {
+  set_error(msg);
+  return code;
+}
+
+int from_cuda(const CudaError &e) {
+  std::string m = std::string("CUDA error ") + cudaGetErrorName(e.code) + ": " +
+                  cudaGetErrorString(e.code) + " in " + e.where;
+  set_error(m);
+  if (e.code == cudaErrorMemoryAllocation) return ARAN_ERR_OOM;
+  if (e.code == cudaErrorNoDevice || e.code == cudaErrorInsufficientDriver) return ARAN_ERR_NO_DEVICE;
+  return ARAN_ERR_CUDA;
+}
+
+int check_config(const AranGpuConfig3d *c) {
+  if (!c) return fail(ARAN_ERR_INVALID, "config is NULL");
+  for (int a = 0; a < 3; ++a)
+    if (!(c->ub[a] > c->lb[a]) || !std::isfinite(c->lb[a]) || !std::isfinite(c->ub[a]))
+      return fail(ARAN_ERR_INVALID, "bounding box must satisfy lb < ub (finite)");
+  if (c->maxbox < 1) return fail(ARAN_ERR_INVALID, "maxbox must be >= 1");
+  if (c->order < 1 || c->order > kMaxOrder)
+    return fail(ARAN_ERR_INVALID, "order must be in [1, " + std::to_string(kMaxOrder) + "]");
+  if (c->flavour != ARAN_FLAVOUR_ROTATE)
+    return fail(ARAN_ERR_UNSUPPORTED, "only the rotate flavour is available in this build");
+  if (c->precision != ARAN_PRECISION_FP64 && c->precision != ARAN_PRECISION_MIXED)
+    return fail(ARAN_ERR_INVALID, "unknown precision");
+  if (c->max_depth < 0 || c->max_depth > kKeyBits)
+    return fail(ARAN_ERR_INVALID, "max_depth must be in [0, 21]");
+  return ARAN_OK;
+}
+
+}  // namespace
+}  // namespace aran
+
+using namespace aran;
+
+extern "C" {
+
+const char *aran_gpu_last_error(void) { return g_last_error.c_str(); }
+
+const char *aran_gpu_version(void) { return "aran-gb300 0.1 (sm_103a)"; }
+
+int aran_gpu_solver3d_create(const AranGpuConfig3d *cfg, AranGpuSolver3d **out) {
+  if (!out) return fail(ARAN_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int rc = check_config(cfg);
+  if (rc) return rc;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(ARAN_ERR_NO_DEVICE, std::string("no CUDA device available: ") + cudaGetErrorString(e));
+  AranGpuSolver3d *s = new AranGpuSolver3d();
+  s->cfg = *cfg;
+  try {
+    ACHECK(cudaGetDevice(&s->device));
+    ACHECK(cudaStreamCreateWithFlags(&s->s0, cudaStreamNonBlocking));
+    ACHECK(cudaStreamCreateWithFlags(&s->s1, cudaStreamNonBlocking));
+    for (auto &ev : s->ev) ACHECK(cudaEventCreate(&ev));
+    double ext = 0;
+    for (int a = 0; a < 3; ++a) ext = std::fmax(ext, cfg->ub[a] - cfg->lb[a]);
+    s->scale_e = std::ldexp(1.0, (int)std::ceil(std::log2(ext)));
+    if (s->scale_e < ext) s->scale_e *= 2;
+    build_tables(s);
+  } catch (const CudaError &ce) {
+    int r = from_cuda(ce);
+    aran_gpu_solver3d_destroy(s);
+    return r;
+  }
+  *out = s;
+  return ARAN_OK;
+}
+
+void aran_gpu_solver3d_destroy(AranGpuSolver3d *s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  if (s->s0) cudaStreamSynchronize(s->s0);
+  if (s->s1) cudaStreamSynchronize(s->s1);
+  DevTree &t = s->tree;
+  t.key.release(); t.ijk.release(); t.depth.release(); t.begin.release(); t.end.release();
+  t.child.release(); t.parent.release(); t.center.release(); t.col.release(); t.ncol.release();
+  t.lf_begin.release(); t.lf_end.release(); t.far_off.release(); t.far_src.release();
+  t.far_dir.release(); t.leaf_node.release(); t.near_off.release(); t.near_rng.release();
+  t.m2l_targets.release();
+  for (auto *tb : {&s->t64}) {
+    tb->rec.release(); tb->p2mf.release(); tb->vt.release(); tb->vm.release(); tb->vl.release();
+    tb->gz.release(); tb->gm.release(); tb->dir_m2l.release(); tb->dir_m2m.release();
+    tb->dir_l2l.release(); tb->lm.release();
+  }
+  {
+    auto *tb = &s->t32;
+    tb->rec.release(); tb->p2mf.release(); tb->vt.release(); tb->vm.release(); tb->vl.release();
+    tb->gz.release(); tb->gm.release(); tb->dir_m2l.release(); tb->dir_m2m.release();
+    tb->dir_l2l.release(); tb->lm.release();
+  }
+  s->keys_in.release(); s->keys_out.release(); s->idx_in.release(); s->perm.release();
+  s->cub_tmp.release(); s->sx.release(); s->sy.release(); s->sz.release(); s->sq.release();
+  s->rel64.release(); s->rel32.release(); s->acc_pot.release(); s->acc_fld.release();
+  s->io_xyz.release(); s->io_q.release(); s->io_pot.release(); s->io_fld.release();
+  s->mult64.release(); s->loc64.release(); s->mult32.release(); s->loc32.release();
+  s->scan_tmp.release(); s->stats_dev.release();
+  for (auto &ev : s->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (s->s0) cudaStreamDestroy(s->s0);
+  if (s->s1) cudaStreamDestroy(s->s1);
+  delete s;
+}
+
+int aran_gpu_solver3d_solve(AranGpuSolver3d *s, int64_t n, const double *xyz, const double *q,
+                            double *pot, double *field, int mem) {
+  if (!s) return fail(ARAN_ERR_INVALID, "solver is NULL");
+  if (n < 1) return fail(ARAN_ERR_INVALID, "n must be >= 1");
+  if (n > (int64_t)1 << 30) return fail(ARAN_ERR_INVALID, "n exceeds 2^30 particles");
+  if (!xyz || !q) return fail(ARAN_ERR_INVALID, "xyz and q must not be NULL");
+  if (mem != ARAN_MEM_HOST && mem != ARAN_MEM_DEVICE) return fail(ARAN_ERR_INVALID, "bad mem kind");
+  if (field && !s->cfg.field) return fail(ARAN_ERR_INVALID, "field requested from a potential-only solver");
+  try {
+    ACHECK(cudaSetDevice(s->device));
+    s->launches = 0;
+    cudaStream_t st = s->s0;
+    const double *dx = xyz, *dq = q;
+    double *dpot = pot, *dfld = field;
+    ACHECK(cudaEventRecord(s->ev[2 * Stage::TOTAL], st));
+    ACHECK(cudaEventRecord(s->ev[2 * Stage::H2D], st));
+    if (mem == ARAN_MEM_HOST) {
+      s->io_xyz.reserve(3 * n);
+      s->io_q.reserve(n);
+      ACHECK(cudaMemcpyAsync(s->io_xyz.ptr, xyz, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+      ACHECK(cudaMemcpyAsync(s->io_q.ptr, q, n * sizeof(double), cudaMemcpyHostToDevice, st));
+      dx = s->io_xyz.ptr;
+      dq = s->io_q.ptr;
+      if (pot) { s->io_pot.reserve(n); dpot = s->io_pot.ptr; }
+      if (field) { s->io_fld.reserve(3 * n); dfld = s->io_fld.ptr; }
+    }
+    ACHECK(cudaEventRecord(s->ev[2 * Stage::H2D + 1], st));
+    ACHECK(cudaEventRecord(s->ev[2 * Stage::SORT], st));
+    build_tree(s, n, dx, dq);
+    ACHECK(cudaEventRecord(s->ev[2 * Stage::TREE], st));  // tree start == sort end
+    build_lists(s);
+    run_passes(s);
+    scatter_outputs(s, dpot, dfld);
+    ACHECK(cudaEventRecord(s->ev[2 * Stage::D2H], st));
+    if (mem == ARAN_MEM_HOST) {
+      if (pot) ACHECK(cudaMemcpyAsync(pot, dpot, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+      if (field) ACHECK(cudaMemcpyAsync(field, dfld, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    ACHECK(cudaEventRecord(s->ev[2 * Stage::D2H + 1], st));
+    ACHECK(cudaEventRecord(s->ev[2 * Stage::TOTAL + 1], st));
+    ACHECK(cudaStreamSynchronize(st));
+    ACHECK(cudaStreamSynchronize(s->s1));
+    ACHECK(cudaGetLastError());
+    s->have_tree = true;
+    // stage times
+    auto el = [&](int a0, int a1) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, s->ev[a0], s->ev[a1]);
+      return (double)ms;
+    };
+    s->ms[0] = el(2 * Stage::TOTAL, 2 * Stage::TOTAL + 1);
+    s->ms[1] = el(2 * Stage::SORT, 2 * Stage::SORT + 1);
+    s->ms[2] = el(2 * Stage::SORT + 1, 2 * Stage::TREE + 1);
+    s->ms[3] = el(2 * Stage::TREE + 1, 2 * Stage::LISTS + 1);
+    s->ms[4] = el(2 * Stage::P2M, 2 * Stage::P2M + 1);
+    s->ms[5] = el(2 * Stage::M2M, 2 * Stage::M2M + 1);
+    s->ms[6] = el(2 * Stage::M2L, 2 * Stage::M2L + 1);
+    s->ms[7] = el(2 * Stage::L2L, 2 * Stage::L2L + 1);
+    s->ms[8] = el(2 * Stage::L2P, 2 * Stage::L2P + 1);
+    s->ms[9] = el(2 * Stage::P2P, 2 * Stage::P2P + 1);
+    s->ms[10] = el(2 * Stage::H2D, 2 * Stage::H2D + 1);
+    s->ms[11] = el(2 * Stage::D2H, 2 * Stage::D2H + 1);
+  } catch (const CudaError &ce) {
+    return from_cuda(ce);
+  }
+  return ARAN_OK;
+}
+
+int aran_gpu_solver3d_get_stats(AranGpuSolver3d *s, int64_t stats[11]) {
+  if (!s || !stats) return fail(ARAN_ERR_INVALID, "NULL argument");
+  if (!s->have_tree) return fail(ARAN_ERR_INVALID, "no solve has run yet");
+  try {
+    compute_stats(s);
+  } catch (const CudaError &ce) {
+    return from_cuda(ce);
+  }
+  for (int i = 0; i < 11; ++i) stats[i] = s->stats[i];
+  return ARAN_OK;
+}
+
+int aran_gpu_solver3d_tree_info(AranGpuSolver3d *s, int64_t info[5]) {
+  if (!s || !info) return fail(ARAN_ERR_INVALID, "NULL argument");
+  if (!s->have_tree) return fail(ARAN_ERR_INVALID, "no solve has run yet");
+  DevTree &t = s->tree;
+  info[0] = t.nnodes;
+  info[1] = t.n_far;
+  // directed near leaf entries: expand the ranges
+  int64_t nn = 0;
+  try {
+    std::vector<int> off(t.nleaves + 1), rng(2 * t.n_near_rng);
+    ACHECK(cudaMemcpy(off.data(), t.near_off.ptr, off.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    if (t.n_near_rng)
+      ACHECK(cudaMemcpy(rng.data(), t.near_rng.ptr, rng.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int64_t r = 0; r < t.n_near_rng; ++r) nn += rng[2 * r + 1] - rng[2 * r];
+  } catch (const CudaError &ce) {
+    return from_cuda(ce);
+  }
+  info[2] = nn;
+  info[3] = t.nleaves;
+  info[4] = t.nlevels - 1;
+  return ARAN_OK;
+}
+
+int aran_gpu_solver3d_tree_lists(AranGpuSolver3d *s, uint64_t *node_ids, int32_t *node_begin,
+                                 int32_t *node_end, uint8_t *node_leaf, uint64_t *far_pairs,
+                                 uint64_t *near_pairs, int32_t *perm) {
+  if (!s) return fail(ARAN_ERR_INVALID, "solver is NULL");
+  if (!s->have_tree) return fail(ARAN_ERR_INVALID, "no solve has run yet");
+  DevTree &t = s->tree;
+  try {
+    int nn = t.nnodes;
+    std::vector<uint64_t> key(nn);
+    std::vector<uint8_t> dep(nn);
+    std::vector<int> child(nn), beg(nn), en(nn);
+    ACHECK(cudaMemcpy(key.data(), t.key.ptr, nn * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(dep.data(), t.depth.ptr, nn, cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(child.data(), t.child.ptr, nn * sizeof(int), cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(beg.data(), t.begin.ptr, nn * sizeof(int), cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(en.data(), t.end.ptr, nn * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<uint64_t> id(nn);
+    for (int i = 0; i < nn; ++i) id[i] = (1ull << (3 * dep[i])) | key[i];
+    for (int i = 0; i < nn; ++i) {
+      if (node_ids) node_ids[i] = id[i];
+      if (node_begin) node_begin[i] = beg[i];
+      if (node_end) node_end[i] = en[i];
+      if (node_leaf) node_leaf[i] = child[i] < 0 ? 1 : 0;
+    }
+    if (far_pairs) {
+      std::vector<int> off(nn + 1), src(t.n_far);
+      ACHECK(cudaMemcpy(off.data(), t.far_off.ptr, (nn + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+      if (t.n_far) ACHECK(cudaMemcpy(src.data(), t.far_src.ptr, t.n_far * sizeof(int), cudaMemcpyDeviceToHost));
+      for (int i = 0; i < nn; ++i)
+        for (int j = off[i]; j < off[i + 1]; ++j) {
+          far_pairs[2 * (size_t)j] = id[i];
+          far_pairs[2 * (size_t)j + 1] = id[src[j]];
+        }
+    }
+    if (near_pairs) {
+      std::vector<int> off(t.nleaves + 1), rng(2 * t.n_near_rng + 2), ln(t.nleaves);
+      ACHECK(cudaMemcpy(off.data(), t.near_off.ptr, (t.nleaves + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+      if (t.n_near_rng) ACHECK(cudaMemcpy(rng.data(), t.near_rng.ptr, 2 * t.n_near_rng * sizeof(int), cudaMemcpyDeviceToHost));
+      ACHECK(cudaMemcpy(ln.data(), t.leaf_node.ptr, t.nleaves * sizeof(int), cudaMemcpyDeviceToHost));
+      size_t w = 0;
+      for (int L = 0; L < t.nleaves; ++L)
+        for (int r = off[L]; r < off[L + 1]; ++r)
+          for (int lf = rng[2 * r]; lf < rng[2 * r + 1]; ++lf) {
+            near_pairs[2 * w] = id[ln[L]];
+            near_pairs[2 * w + 1] = id[ln[lf]];
+            ++w;
+          }
+    }
+    if (perm) ACHECK(cudaMemcpy(perm, s->perm.ptr, t.n * sizeof(int), cudaMemcpyDeviceToHost));
+  } catch (const CudaError &ce) {
+    return from_cuda(ce);
+  }
+  return ARAN_OK;
+}
+
+int aran_gpu_solver3d_expansions(AranGpuSolver3d *s, double *mult, double *local) {
+  if (!s) return fail(ARAN_ERR_INVALID, "solver is NULL");
+  if (!s->have_tree) return fail(ARAN_ERR_INVALID, "no solve has run yet");
+  try {
+    copy_expansions(s, mult, local);
+  } catch (const CudaError &ce) {
+    return from_cuda(ce);
+  }
+  return ARAN_OK;
+}
+
+int aran_gpu_solver3d_timings(AranGpuSolver3d *s, double ms[16]) {
+  if (!s || !ms) return fail(ARAN_ERR_INVALID, "NULL argument");
+  for (int i = 0; i < 16; ++i) ms[i] = s->ms[i];
+  return ARAN_OK;
+}
+
+int64_t aran_gpu_solver3d_launches(AranGpuSolver3d *s) { return s ? s->launches : -1; }
+
+}  // extern "C"

@@ -1,0 +1,494 @@
+// tree.cu -- device octree and interaction lists.
+//
+// Replaces libvsg's VsgPRTree3d insertion (vsg_prtree3d_insert_point, called
+// from aran/aransolver3d.c:972-978) and its near/far traversal
+// (vsg_prtree3d_near_far_traversal_full, aran/aransolver3d.c:1189-1190) by a
+// Morton-sorted, level-synchronous build:
+//   1. 63-bit keys from the 21-bit quantised coordinates, radix sort;
+//   2. level by level, a node with more than maxbox points (and depth below
+//      the limit) gets its 8 octants, whose point ranges are found by binary
+//      search in the sorted keys;
+//   3. colleagues (adjacent same-depth non-empty nodes, <= 27) level by level;
+//   4. far lists: non-empty children of the parent's internal colleagues that
+//      are not adjacent (the M2L sources of aran/aransolver3d.c:333-354);
+//   5. near lists per non-empty leaf L, as ranges of leaf ordinals (leaves
+//      are numbered in Morton order, so all leaves below a node are one
+//      range): every colleague of L (a leaf, or an internal node standing for
+//      all leaves below it), plus the leaf colleagues of every ancestor of L
+//      (a coarser leaf adjacent to an ancestor is near everything below it).
+#include <cub/cub.cuh>
+
+#include "internal.cuh"
+
+namespace aran {
+
+namespace {
+
+__global__ void k_keys(int64_t n, const double *__restrict__ xyz, double lbx, double lby,
+                       double lbz, double scx, double scy, double scz,
+                       uint64_t *__restrict__ keys, int *__restrict__ idx) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t qx = (uint64_t)quantise(xyz[3 * i], lbx, scx);
+  uint64_t qy = (uint64_t)quantise(xyz[3 * i + 1], lby, scy);
+  uint64_t qz = (uint64_t)quantise(xyz[3 * i + 2], lbz, scz);
+  keys[i] = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
+  idx[i] = (int)i;
+}
+
+__global__ void k_gather(int64_t n, const int *__restrict__ perm, const double *__restrict__ xyz,
+                         const double *__restrict__ q, double *__restrict__ sx,
+                         double *__restrict__ sy, double *__restrict__ sz,
+                         double *__restrict__ sq) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int o = perm[i];
+  sx[i] = xyz[3 * (int64_t)o];
+  sy[i] = xyz[3 * (int64_t)o + 1];
+  sz[i] = xyz[3 * (int64_t)o + 2];
+  sq[i] = q[o];
+}
+
+struct NodeArrays {
+  uint64_t *key;
+  int *ijk;
+  uint8_t *depth;
+  int *begin, *end, *child, *parent;
+  double *center;
+};
+
+__global__ void k_root(NodeArrays na, int64_t n, double lbx, double lby, double lbz, double ubx,
+                       double uby, double ubz) {
+  na.key[0] = 0;
+  na.ijk[0] = na.ijk[1] = na.ijk[2] = 0;
+  na.depth[0] = 0;
+  na.begin[0] = 0;
+  na.end[0] = (int)n;
+  na.child[0] = -1;
+  na.parent[0] = -1;
+  na.center[0] = node_center_axis(lbx, ubx, 0, 0);
+  na.center[1] = node_center_axis(lby, uby, 0, 0);
+  na.center[2] = node_center_axis(lbz, ubz, 0, 0);
+}
+
+__global__ void k_flag_internal(int cnt, int off, const int *__restrict__ begin,
+                                const int *__restrict__ end, int maxbox, int d, int maxd,
+                                int *__restrict__ flags) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  int c = end[off + i] - begin[off + i];
+  flags[i] = (c > maxbox && d < maxd) ? 1 : 0;
+}
+
+__device__ __forceinline__ int digit_at(const uint64_t *k, int j, int shift) {
+  return (int)((k[j] >> shift) & 7ull);
+}
+
+__global__ void k_make_children(int cnt, int off, int child_off, const int *__restrict__ flags,
+                                const int *__restrict__ pos, const uint64_t *__restrict__ skeys,
+                                int d, NodeArrays na, double lbx, double lby, double lbz,
+                                double ubx, double uby, double ubz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  int node = off + i;
+  if (!flags[i]) {
+    na.child[node] = -1;
+    return;
+  }
+  int base = child_off + 8 * pos[i];
+  na.child[node] = base;
+  int b = na.begin[node], e = na.end[node];
+  int shift = 3 * (kKeyBits - d - 1);
+  uint64_t pk = na.key[node];
+  int pi = na.ijk[3 * node], pj = na.ijk[3 * node + 1], pk3 = na.ijk[3 * node + 2];
+  int start = b;
+  for (int c = 0; c < 8; ++c) {
+    // first index in [start, e) whose digit is > c
+    int lo = start, hi = e;
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      if (digit_at(skeys, mid, shift) <= c) lo = mid + 1; else hi = mid;
+    }
+    int cn = base + c;
+    na.key[cn] = (pk << 3) | (uint64_t)c;
+    int ci = (pi << 1) | (c & 1), cj = (pj << 1) | ((c >> 1) & 1), ck = (pk3 << 1) | ((c >> 2) & 1);
+    na.ijk[3 * cn] = ci;
+    na.ijk[3 * cn + 1] = cj;
+    na.ijk[3 * cn + 2] = ck;
+    na.depth[cn] = (uint8_t)(d + 1);
+    na.begin[cn] = start;
+    na.end[cn] = lo;
+    na.child[cn] = -1;
+    na.parent[cn] = node;
+    na.center[3 * cn] = node_center_axis(lbx, ubx, d + 1, ci);
+    na.center[3 * cn + 1] = node_center_axis(lby, uby, d + 1, cj);
+    na.center[3 * cn + 2] = node_center_axis(lbz, ubz, d + 1, ck);
+    start = lo;
+  }
+}
+
+__device__ __forceinline__ bool adjacent(const int *ijk, int a, int b) {
+  int dx = ijk[3 * a] - ijk[3 * b], dy = ijk[3 * a + 1] - ijk[3 * b + 1],
+      dz = ijk[3 * a + 2] - ijk[3 * b + 2];
+  return dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1;
+}
+
+__device__ __forceinline__ int ncount(const int *begin, const int *end, int a) {
+  return end[a] - begin[a];
+}
+
+__global__ void k_colleagues(int cnt, int off, const int *__restrict__ begin,
+                             const int *__restrict__ end, const int *__restrict__ child,
+                             const int *__restrict__ parent, const int *__restrict__ ijk,
+                             int *__restrict__ col, int *__restrict__ ncol) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  int c = off + i;
+  int k = 0;
+  if (ncount(begin, end, c) > 0) {
+    int p = parent[c];
+    if (p < 0) {
+      col[27 * c] = c;
+      k = 1;
+    } else {
+      int np = ncol[p];
+      for (int j = 0; j < np; ++j) {
+        int q = col[27 * p + j];
+        int c0 = child[q];
+        if (c0 < 0) continue;
+        for (int o = 0; o < 8; ++o) {
+          int s = c0 + o;
+          if (ncount(begin, end, s) > 0 && adjacent(ijk, c, s) && k < 27) col[27 * c + k++] = s;
+        }
+      }
+    }
+  }
+  ncol[c] = k;
+}
+
+// M2L sources of node t (same depth, not adjacent, children of the parent's
+// internal colleagues).  mode 0 counts, mode 1 writes.
+__global__ void k_far(int cnt, int off, const int *__restrict__ begin, const int *__restrict__ end,
+                      const int *__restrict__ child, const int *__restrict__ parent,
+                      const int *__restrict__ ijk, const int *__restrict__ col,
+                      const int *__restrict__ ncol, int *__restrict__ far_cnt,
+                      const int *__restrict__ far_off, int *__restrict__ far_src,
+                      uint16_t *__restrict__ far_dir, int mode) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  int t = off + i;
+  int k = 0;
+  int w = mode ? far_off[t] : 0;
+  if (ncount(begin, end, t) > 0) {
+    int p = parent[t];
+    if (p >= 0) {
+      int np = ncol[p];
+      for (int j = 0; j < np; ++j) {
+        int q = col[27 * p + j];
+        int c0 = child[q];
+        if (c0 < 0) continue;
+        for (int o = 0; o < 8; ++o) {
+          int s = c0 + o;
+          if (ncount(begin, end, s) == 0 || adjacent(ijk, t, s)) continue;
+          if (mode) {
+            int dx = ijk[3 * t] - ijk[3 * s], dy = ijk[3 * t + 1] - ijk[3 * s + 1],
+                dz = ijk[3 * t + 2] - ijk[3 * s + 2];
+            far_src[w + k] = s;
+            far_dir[w + k] = (uint16_t)((dx + 3) + 7 * (dy + 3) + 49 * (dz + 3));
+          }
+          ++k;
+        }
+      }
+    }
+  }
+  if (!mode) far_cnt[t] = k;
+}
+
+__global__ void k_mark_leaf_starts(int nn, const int *__restrict__ begin, const int *__restrict__ end,
+                                   const int *__restrict__ child, int *__restrict__ flags) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  if (child[i] < 0 && end[i] > begin[i]) flags[begin[i]] = 1;
+}
+
+__global__ void k_leaf_ranges(int nn, const int *__restrict__ begin, const int *__restrict__ end,
+                              const int *__restrict__ child, const int *__restrict__ incl,
+                              int *__restrict__ lf_begin, int *__restrict__ lf_end,
+                              int *__restrict__ leaf_node) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  int b = begin[i], e = end[i];
+  if (e > b) {
+    lf_begin[i] = incl[b] - 1;
+    lf_end[i] = incl[e - 1];
+    if (child[i] < 0) leaf_node[incl[b] - 1] = i;
+  } else {
+    lf_begin[i] = 0;
+    lf_end[i] = 0;
+  }
+}
+
+// near ranges of leaf ordinal L; mode 0 counts, mode 1 writes
+__global__ void k_near(int nleaves, const int *__restrict__ leaf_node, const int *__restrict__ begin,
+                       const int *__restrict__ end, const int *__restrict__ child,
+                       const int *__restrict__ parent, const int *__restrict__ col,
+                       const int *__restrict__ ncol, const int *__restrict__ lf_begin,
+                       const int *__restrict__ lf_end, int *__restrict__ near_cnt,
+                       const int *__restrict__ near_off, int *__restrict__ near_rng, int mode) {
+  int L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nleaves) return;
+  int node = leaf_node[L];
+  int k = 0;
+  int w = mode ? near_off[L] : 0;
+  int nc = ncol[node];
+  for (int j = 0; j < nc; ++j) {
+    int q = col[27 * node + j];
+    if (mode) {
+      near_rng[2 * (w + k)] = lf_begin[q];
+      near_rng[2 * (w + k) + 1] = lf_end[q];
+    }
+    ++k;
+  }
+  for (int a = parent[node]; a >= 0; a = parent[a]) {
+    int na = ncol[a];
+    for (int j = 0; j < na; ++j) {
+      int q = col[27 * a + j];
+      if (child[q] >= 0 || end[q] == begin[q]) continue;
+      if (mode) {
+        near_rng[2 * (w + k)] = lf_begin[q];
+        near_rng[2 * (w + k) + 1] = lf_end[q];
+      }
+      ++k;
+    }
+  }
+  if (!mode) near_cnt[L] = k;
+}
+
+// relative (leaf-centred) particle coordinates for the kernels
+template <typename T>
+__global__ void k_relative(int64_t n, const int *__restrict__ incl, const int *__restrict__ leaf_node,
+                           const double *__restrict__ center, const double *__restrict__ sx,
+                           const double *__restrict__ sy, const double *__restrict__ sz,
+                           const double *__restrict__ sq, real4<T> *__restrict__ rel) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int node = leaf_node[incl[i] - 1];
+  real4<T> r;
+  r.x = (T)(sx[i] - center[3 * node]);
+  r.y = (T)(sy[i] - center[3 * node + 1]);
+  r.z = (T)(sz[i] - center[3 * node + 2]);
+  r.q = (T)sq[i];
+  rel[i] = r;
+}
+
+template <typename T>
+void exclusive_scan(AranGpuSolver3d *s, const T *in, T *out, int n, cudaStream_t st) {
+  size_t bytes = 0;
+  ACHECK(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, n, st));
+  s->cub_tmp.reserve(bytes);
+  ACHECK(cub::DeviceScan::ExclusiveSum(s->cub_tmp.ptr, bytes, in, out, n, st));
+  s->launches += 2;
+}
+
+template <typename T>
+void inclusive_scan(AranGpuSolver3d *s, const T *in, T *out, int64_t n, cudaStream_t st) {
+  size_t bytes = 0;
+  ACHECK(cub::DeviceScan::InclusiveSum(nullptr, bytes, in, out, n, st));
+  s->cub_tmp.reserve(bytes);
+  ACHECK(cub::DeviceScan::InclusiveSum(s->cub_tmp.ptr, bytes, in, out, n, st));
+  s->launches += 2;
+}
+
+NodeArrays arrays(DevTree &t) {
+  NodeArrays na;
+  na.key = t.key.ptr;
+  na.ijk = t.ijk.ptr;
+  na.depth = t.depth.ptr;
+  na.begin = t.begin.ptr;
+  na.end = t.end.ptr;
+  na.child = t.child.ptr;
+  na.parent = t.parent.ptr;
+  na.center = t.center.ptr;
+  return na;
+}
+
+void grow_nodes(DevTree &t, size_t need, size_t keep, cudaStream_t st) {
+  t.key.grow_keep(need, keep, st);
+  t.ijk.grow_keep(3 * need, 3 * keep, st);
+  t.depth.grow_keep(need, keep, st);
+  t.begin.grow_keep(need, keep, st);
+  t.end.grow_keep(need, keep, st);
+  t.child.grow_keep(need, keep, st);
+  t.parent.grow_keep(need, keep, st);
+  t.center.grow_keep(3 * need, 3 * keep, st);
+}
+
+}  // namespace
+
+void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double *d_q) {
+  cudaStream_t st = s->s0;
+  const AranGpuConfig3d &c = s->cfg;
+  DevTree &t = s->tree;
+  t.n = n;
+  const int TB = 256;
+  double sc[3];
+  for (int a = 0; a < 3; ++a) sc[a] = (double)(1 << kKeyBits) / (c.ub[a] - c.lb[a]);
+
+  s->keys_in.reserve(n);
+  s->keys_out.reserve(n);
+  s->idx_in.reserve(n);
+  s->perm.reserve(n);
+  k_keys<<<ceil_div(n, TB), TB, 0, st>>>(n, d_xyz, c.lb[0], c.lb[1], c.lb[2], sc[0], sc[1], sc[2],
+                                          s->keys_in.ptr, s->idx_in.ptr);
+  s->launches++;
+  size_t bytes = 0;
+  ACHECK(cub::DeviceRadixSort::SortPairs(nullptr, bytes, s->keys_in.ptr, s->keys_out.ptr,
+                                         s->idx_in.ptr, s->perm.ptr, (int)n, 0, 3 * kKeyBits, st));
+  s->cub_tmp.reserve(bytes);
+  ACHECK(cub::DeviceRadixSort::SortPairs(s->cub_tmp.ptr, bytes, s->keys_in.ptr, s->keys_out.ptr,
+                                         s->idx_in.ptr, s->perm.ptr, (int)n, 0, 3 * kKeyBits, st));
+  s->launches += 4;
+  s->sx.reserve(n);
+  s->sy.reserve(n);
+  s->sz.reserve(n);
+  s->sq.reserve(n);
+  k_gather<<<ceil_div(n, TB), TB, 0, st>>>(n, s->perm.ptr, d_xyz, d_q, s->sx.ptr, s->sy.ptr,
+                                            s->sz.ptr, s->sq.ptr);
+  s->launches++;
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::SORT + 1], st));
+
+  // level-synchronous subdivision
+  int maxd = c.max_depth > 0 ? c.max_depth : kKeyBits;
+  if (maxd > kKeyBits) maxd = kKeyBits;
+  size_t est = (size_t)(8 * (n / (c.maxbox + 1) + 1) * 2 + 64);
+  grow_nodes(t, est, 0, st);
+  t.level_off.assign(1, 0);
+  t.level_internal.clear();
+  NodeArrays na = arrays(t);
+  k_root<<<1, 1, 0, st>>>(na, n, c.lb[0], c.lb[1], c.lb[2], c.ub[0], c.ub[1], c.ub[2]);
+  s->launches++;
+  int off = 0, cnt = 1;
+  DBuf<int> &flags = s->scan_tmp;
+  int d = 0;
+  int hostbuf[2];
+  while (cnt > 0) {
+    t.level_off.push_back(off + cnt);
+    flags.reserve(2 * (size_t)cnt + 2);
+    int *pos = flags.ptr + cnt;
+    k_flag_internal<<<ceil_div(cnt, TB), TB, 0, st>>>(cnt, off, t.begin.ptr, t.end.ptr, c.maxbox,
+                                                       d, maxd, flags.ptr);
+    s->launches++;
+    exclusive_scan(s, flags.ptr, pos, cnt, st);
+    ACHECK(cudaMemcpyAsync(&hostbuf[0], pos + cnt - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ACHECK(cudaMemcpyAsync(&hostbuf[1], flags.ptr + cnt - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ACHECK(cudaStreamSynchronize(st));
+    int ninternal = hostbuf[0] + hostbuf[1];
+    t.level_internal.push_back(ninternal);
+    int child_off = off + cnt;
+    size_t need = (size_t)child_off + 8 * (size_t)ninternal;
+    if (need > t.key.cap) {
+      grow_nodes(t, need, child_off, st);
+      na = arrays(t);
+    }
+    k_make_children<<<ceil_div(cnt, TB), TB, 0, st>>>(cnt, off, child_off, flags.ptr, pos,
+                                                       s->keys_out.ptr, d, na, c.lb[0], c.lb[1],
+                                                       c.lb[2], c.ub[0], c.ub[1], c.ub[2]);
+    s->launches++;
+    off = child_off;
+    cnt = 8 * ninternal;
+    ++d;
+  }
+  t.nnodes = off;
+  t.nlevels = d;
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::TREE + 1], st));
+}
+
+void build_lists(AranGpuSolver3d *s) {
+  cudaStream_t st = s->s0;
+  DevTree &t = s->tree;
+  const int TB = 256;
+  int nn = t.nnodes;
+  int64_t n = t.n;
+  t.col.reserve(27 * (size_t)nn);
+  t.ncol.reserve(nn);
+  for (int d = 0; d < t.nlevels; ++d) {
+    int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
+    k_colleagues<<<ceil_div(cnt, TB), TB, 0, st>>>(cnt, off, t.begin.ptr, t.end.ptr, t.child.ptr,
+                                                    t.parent.ptr, t.ijk.ptr, t.col.ptr, t.ncol.ptr);
+    s->launches++;
+  }
+  // far lists over all nodes
+  t.far_off.reserve(nn + 1);
+  DBuf<int> &cntbuf = s->scan_tmp;
+  cntbuf.reserve((size_t)nn + 1 + (size_t)n + 1);
+  k_far<<<ceil_div(nn, TB), TB, 0, st>>>(nn, 0, t.begin.ptr, t.end.ptr, t.child.ptr, t.parent.ptr,
+                                          t.ijk.ptr, t.col.ptr, t.ncol.ptr, cntbuf.ptr, nullptr,
+                                          nullptr, nullptr, 0);
+  s->launches++;
+  ACHECK(cudaMemsetAsync(cntbuf.ptr + nn, 0, sizeof(int), st));
+  exclusive_scan(s, cntbuf.ptr, t.far_off.ptr, nn + 1, st);
+  int nfar = 0;
+  ACHECK(cudaMemcpyAsync(&nfar, t.far_off.ptr + nn, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaStreamSynchronize(st));
+  t.n_far = nfar;
+  t.far_src.reserve(nfar + 1);
+  t.far_dir.reserve(nfar + 1);
+  k_far<<<ceil_div(nn, TB), TB, 0, st>>>(nn, 0, t.begin.ptr, t.end.ptr, t.child.ptr, t.parent.ptr,
+                                          t.ijk.ptr, t.col.ptr, t.ncol.ptr, nullptr, t.far_off.ptr,
+                                          t.far_src.ptr, t.far_dir.ptr, 1);
+  s->launches++;
+
+  // leaves in Morton order
+  DBuf<int> &lflags = s->idx_in;  // reuse (n ints)
+  int *incl = s->keys_in.ptr ? reinterpret_cast<int *>(s->keys_in.ptr) : nullptr;  // n ints fit in n u64
+  ACHECK(cudaMemsetAsync(lflags.ptr, 0, n * sizeof(int), st));
+  k_mark_leaf_starts<<<ceil_div(nn, TB), TB, 0, st>>>(nn, t.begin.ptr, t.end.ptr, t.child.ptr,
+                                                       lflags.ptr);
+  s->launches++;
+  inclusive_scan(s, lflags.ptr, incl, n, st);
+  int nleaves = 0;
+  ACHECK(cudaMemcpyAsync(&nleaves, incl + n - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaStreamSynchronize(st));
+  t.nleaves = nleaves;
+  t.lf_begin.reserve(nn);
+  t.lf_end.reserve(nn);
+  t.leaf_node.reserve(nleaves + 1);
+  k_leaf_ranges<<<ceil_div(nn, TB), TB, 0, st>>>(nn, t.begin.ptr, t.end.ptr, t.child.ptr, incl,
+                                                  t.lf_begin.ptr, t.lf_end.ptr, t.leaf_node.ptr);
+  s->launches++;
+  // relative coordinates
+  if (s->cfg.precision == ARAN_PRECISION_MIXED) {
+    s->rel32.reserve(n);
+    k_relative<float><<<ceil_div(n, TB), TB, 0, st>>>(n, incl, t.leaf_node.ptr, t.center.ptr,
+                                                       s->sx.ptr, s->sy.ptr, s->sz.ptr, s->sq.ptr,
+                                                       s->rel32.ptr);
+  } else {
+    s->rel64.reserve(n);
+    k_relative<double><<<ceil_div(n, TB), TB, 0, st>>>(n, incl, t.leaf_node.ptr, t.center.ptr,
+                                                        s->sx.ptr, s->sy.ptr, s->sz.ptr, s->sq.ptr,
+                                                        s->rel64.ptr);
+  }
+  s->launches++;
+  // near ranges per leaf
+  t.near_off.reserve(nleaves + 1);
+  k_near<<<ceil_div(nleaves, TB), TB, 0, st>>>(nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
+                                                t.child.ptr, t.parent.ptr, t.col.ptr, t.ncol.ptr,
+                                                t.lf_begin.ptr, t.lf_end.ptr, cntbuf.ptr, nullptr,
+                                                nullptr, 0);
+  s->launches++;
+  ACHECK(cudaMemsetAsync(cntbuf.ptr + nleaves, 0, sizeof(int), st));
+  exclusive_scan(s, cntbuf.ptr, t.near_off.ptr, nleaves + 1, st);
+  int nrng = 0;
+  ACHECK(cudaMemcpyAsync(&nrng, t.near_off.ptr + nleaves, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaStreamSynchronize(st));
+  t.n_near_rng = nrng;
+  t.near_rng.reserve(2 * (size_t)nrng + 2);
+  k_near<<<ceil_div(nleaves, TB), TB, 0, st>>>(nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
+                                                t.child.ptr, t.parent.ptr, t.col.ptr, t.ncol.ptr,
+                                                t.lf_begin.ptr, t.lf_end.ptr, nullptr,
+                                                t.near_off.ptr, t.near_rng.ptr, 1);
+  s->launches++;
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::LISTS + 1], st));
+}
+
+}  // namespace aran

@@ -1,0 +1,123 @@
+/*
+ * aran_gpu.h -- C ABI of the GB300 FMM library (libaran_gpu.so).
+ *
+ * The library replaces the hot path behind LibAran's aran_solver3d_solve()
+ * (aran/aransolver3d.c:1135-1202): tree construction (libvsg's PR-octree in
+ * the reference), the clear/up/near-far/down passes and the operator
+ * callbacks aran_development3d_{p2m,m2m*,m2l*,l2l*,local_gradient_evaluate}
+ * (aran/arandevelopment3d.c:169-552) together with the user P2P kernels of
+ * tests/newtonpot3.c:61-78 and tests/newtonfield3.c:91-119.  Everything runs
+ * on one GPU; there is no CPU fallback: a call that cannot run on the GPU
+ * returns an error code and leaves the outputs untouched.
+ *
+ * Plain pointers and sizes only.  Particle positions are AoS xyz triples
+ * (the VsgVector3d at offset 0 of the reference's point structs), charges
+ * and outputs are FP64.
+ */
+#ifndef ARAN_GPU_H
+#define ARAN_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define ARAN_OK 0
+#define ARAN_ERR_INVALID (-1)      /* bad argument / configuration */
+#define ARAN_ERR_CUDA (-2)         /* CUDA runtime failure */
+#define ARAN_ERR_NO_DEVICE (-3)    /* no usable GPU: the library never falls back to the CPU */
+#define ARAN_ERR_OOM (-4)          /* device memory exhausted */
+#define ARAN_ERR_TIMEOUT (-5)      /* a bounded device-side wait gave up */
+#define ARAN_ERR_UNSUPPORTED (-6)
+
+/* M2M/M2L/L2L flavours: aran_development3d_{m2l,m2l_kkylin,m2l_rotate}
+ * (aran/arandevelopment3d.c:306-313,362-369,423-430) */
+#define ARAN_FLAVOUR_NORMAL 0
+#define ARAN_FLAVOUR_KKYLIN 1
+#define ARAN_FLAVOUR_ROTATE 2
+
+/* arithmetic of the solve */
+#define ARAN_PRECISION_FP64 0      /* every pass in FP64 (the plain path) */
+#define ARAN_PRECISION_MIXED 1     /* FP32 bulk, FP64 tables/centres/final sums */
+
+/* pointer location for solve calls */
+#define ARAN_MEM_HOST 0
+#define ARAN_MEM_DEVICE 1
+
+typedef struct
+{
+  double lb[3];        /* tree bounding box (vsg_prtree3d_new_full lbound) */
+  double ub[3];        /* (ubound) */
+  int maxbox;          /* leaf capacity: vsg_prtree3d_new_full 'maxbox' */
+  int order;           /* p of aran_development3d_new (0, p) */
+  int flavour;         /* ARAN_FLAVOUR_* */
+  int field;           /* 0: potential only (newtonpot3); 1: potential + field (newtonfield3) */
+  int precision;       /* ARAN_PRECISION_* */
+  int max_depth;       /* tree depth limit, 1..21 (0 = 21) */
+} AranGpuConfig3d;
+
+typedef struct AranGpuSolver3d AranGpuSolver3d;
+
+/* Creates a solver bound to the current CUDA device and builds the operator
+ * tables for cfg->order.  Replaces aran_solver3d_new + set_functions
+ * (aran/aransolver3d.c:509-661). */
+int aran_gpu_solver3d_create (const AranGpuConfig3d *cfg,
+                              AranGpuSolver3d **out);
+void aran_gpu_solver3d_destroy (AranGpuSolver3d *s);
+
+/* One full solve: tree build, lists, up/near-far/down passes.  xyz is 3n
+ * doubles (AoS), q is n doubles; pot (n) and field (3n, AoS) receive the
+ * potential sum_j q_j/|xi-xj| and field sum_j -q_j (xi-xj)/|xi-xj|^3 of
+ * every particle (either may be NULL).  mem selects host or device pointers;
+ * with host pointers the copies are part of the call.  Replaces
+ * aran_solver3d_insert_point x n + aran_solver3d_solve
+ * (aran/aransolver3d.c:972-978,1135-1202). */
+int aran_gpu_solver3d_solve (AranGpuSolver3d *s, int64_t n, const double *xyz,
+                             const double *q, double *pot, double *field,
+                             int mem);
+
+/* Call counters of the last solve in the order of aran_solver3d_get_stats
+ * (aran/aransolver3d.c:566-586): zero, p2p, p2m, m2m, m2l, l2l, l2p, p2l,
+ * m2p, p2p_remote, m2l_remote. */
+int aran_gpu_solver3d_get_stats (AranGpuSolver3d *s, int64_t stats[11]);
+
+/* Sizes of the last tree: nodes, directed far (M2L) entries, directed near
+ * (P2P) leaf entries, non-empty leaves, depth. */
+int aran_gpu_solver3d_tree_info (AranGpuSolver3d *s, int64_t info[5]);
+
+/* Copies the last tree out for parity checks.  Node id =
+ * (1 << 3*depth) | morton key.  far: (target id, source id) per directed
+ * M2L; near: (target leaf id, source leaf id) per directed P2P block.
+ * perm: sorted position -> input index.  Any pointer may be NULL. */
+int aran_gpu_solver3d_tree_lists (AranGpuSolver3d *s, uint64_t *node_ids,
+                                  int32_t *node_begin, int32_t *node_end,
+                                  uint8_t *node_leaf, uint64_t *far_pairs,
+                                  uint64_t *near_pairs, int32_t *perm);
+
+/* Copies the scaled device expansions of the last solve (debug/parity):
+ * per node, multipole then local coefficients (m >= 0) as interleaved
+ * complex FP64, in LibAran order; unscaled to physical units. */
+int aran_gpu_solver3d_expansions (AranGpuSolver3d *s, double *mult,
+                                  double *local);
+
+/* Stage times of the last solve in ms (CUDA events on the solve stream):
+ * [0] total, [1] keys+sort, [2] tree, [3] lists, [4] p2m, [5] m2m, [6] m2l,
+ * [7] l2l, [8] l2p, [9] p2p (its own stream), [10] h2d, [11] d2h. */
+int aran_gpu_solver3d_timings (AranGpuSolver3d *s, double ms[16]);
+
+/* Number of GPU kernel launches issued by the last solve. */
+int64_t aran_gpu_solver3d_launches (AranGpuSolver3d *s);
+
+/* Last error message of the calling thread. */
+const char *aran_gpu_last_error (void);
+
+/* Library version string. */
+const char *aran_gpu_version (void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
