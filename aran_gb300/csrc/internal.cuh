@@ -87,6 +87,12 @@ struct DevTree {
   DBuf<int> near_off, near_rng;       // CSR over leaves of [lf_a, lf_b) ranges (2 ints)
   DBuf<int> m2l_targets;              // nodes with non-empty far lists
   int n_m2l_targets = 0;
+  DBuf<int2> leaf_be;                 // particle [begin, end) per leaf ordinal
+  DBuf<float4> leaf_chi, leaf_clo;    // FP32 leaf centre split hi + lo; chi.w = close-pair r^2
+  DBuf<int4> big_items;               // (leaf, lf_a, lf_b, 0): chunks of heavy near ranges
+  DBuf<int> parents;                  // internal nodes of depth >= 1 (their children take M2L)
+  int n_parents = 0;
+  int n_big = 0;
   int64_t n_far = 0;
   int64_t n_near_rng = 0;
 };
@@ -136,6 +142,7 @@ struct AranGpuSolver3d {
   aran::DBuf<float> mult32, loc32;
   aran::DBuf<int> scan_tmp;
   aran::DBuf<unsigned long long> stats_dev;
+  aran::DBuf<int> err_dev;               // device error word (bounded waits)
   int64_t stats[11] = {};
   double ms[16] = {};
   int64_t launches = 0;
@@ -151,6 +158,12 @@ void build_lists(AranGpuSolver3d *s);
 void build_tables(AranGpuSolver3d *s);
 // passes.cu
 void run_passes(AranGpuSolver3d *s);
+// m2l.cu
+void launch_m2l(AranGpuSolver3d *s, cudaStream_t st);
+// p2p.cu
+constexpr int kBigRange = 2048;   // near ranges above this many particles are chunked
+void build_p2p_work(AranGpuSolver3d *s);
+void launch_p2p(AranGpuSolver3d *s, cudaStream_t st);
 void compute_stats(AranGpuSolver3d *s);
 void copy_expansions(AranGpuSolver3d *s, double *mult, double *local);
 

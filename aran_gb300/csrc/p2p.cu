@@ -1,0 +1,314 @@
+// p2p.cu -- the near field (P2P) on the device.
+//
+// LibAran calls the user p2p callback for every pair of points of every near
+// leaf pair (near_func, aran/aransolver3d.c:254-324) with the Newton kernels
+// of tests/newtonpot3.c:61-78 (potential) and tests/newtonfield3.c:91-119
+// (field, |r| > 1e-5 guard).  Here every target particle sums its near
+// sources directly (both sides of a pair are evaluated by their own targets
+// instead of the symmetric update).
+//
+// Work decomposition: one block per target leaf; threads-per-target (tpt)
+// grows as the leaf shrinks (n <= 8: 16, <= 16: 8, <= 32: 4, <= 64: 2,
+// else 1), and a target's tpt threads take its near *leaves* round-robin so
+// the per-leaf set-up is amortised over the leaf's points.  Near ranges of
+// more than kBigRange points (a coarse leaf next to a deep subtree, common in
+// clustered sets) are cut into leaf-aligned chunks processed by extra blocks
+// that accumulate atomically.
+//
+// Mixed precision: positions are FP32 relative to their leaf centre, the
+// centre difference comes from FP32 hi+lo centre pairs, per-source-leaf FP32
+// partial sums go into FP64 accumulators, and pairs closer than 1/8 of the
+// target leaf size (where FP32 cancellation would show) are recomputed from
+// the FP64 positions.
+#include <cub/cub.cuh>
+
+#include <type_traits>
+
+#include "internal.cuh"
+
+namespace aran {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__global__ void k_leaf_info(int nleaves, const int *__restrict__ leaf_node,
+                            const int *__restrict__ begin, const int *__restrict__ end,
+                            const uint8_t *__restrict__ depth, const double *__restrict__ center,
+                            double ex, double ey, double ez, int2 *__restrict__ be,
+                            float4 *__restrict__ chi, float4 *__restrict__ clo) {
+  int L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nleaves) return;
+  int node = leaf_node[L];
+  be[L] = make_int2(begin[node], end[node]);
+  double cx = center[3 * node], cy = center[3 * node + 1], cz = center[3 * node + 2];
+  float hx = (float)cx, hy = (float)cy, hz = (float)cz;
+  double h = fmin(ex, fmin(ey, ez)) / ldexp(1.0, depth[node]);
+  float thr = (float)(h * 0.125);
+  chi[L] = make_float4(hx, hy, hz, thr * thr);
+  clo[L] = make_float4((float)(cx - (double)hx), (float)(cy - (double)hy), (float)(cz - (double)hz), 0.f);
+}
+
+__device__ __forceinline__ int rng_count(const int2 *be, int la, int lb) {
+  return be[lb - 1].y - be[la].x;
+}
+
+// heavy ranges -> leaf-aligned chunks; mode 0 counts, mode 1 writes
+__global__ void k_big_items(int nleaves, const int *__restrict__ near_off,
+                            const int *__restrict__ near_rng, const int2 *__restrict__ be,
+                            int *__restrict__ cnt, const int *__restrict__ off,
+                            int4 *__restrict__ items, int mode) {
+  int L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nleaves) return;
+  int k = 0, w = mode ? off[L] : 0;
+  for (int r = near_off[L]; r < near_off[L + 1]; ++r) {
+    int la = near_rng[2 * r], lb = near_rng[2 * r + 1];
+    if (lb <= la) continue;
+    int c = rng_count(be, la, lb);
+    if (c <= kBigRange) continue;
+    int nch = (c + kBigRange - 1) / kBigRange;
+    int p0 = be[la].x;
+    int prev = la;
+    for (int i = 1; i <= nch; ++i) {
+      int nxt = lb;
+      if (i < nch) {
+        // first leaf in [prev, lb) whose begin >= p0 + i*kBigRange
+        int lo = prev, hi = lb, target = p0 + i * kBigRange;
+        while (lo < hi) {
+          int mid = (lo + hi) >> 1;
+          if (be[mid].x < target) lo = mid + 1; else hi = mid;
+        }
+        nxt = lo;
+      }
+      if (mode) items[w + k] = make_int4(L, prev, nxt, 0);
+      ++k;
+      prev = nxt;
+    }
+  }
+  if (!mode) cnt[L] = k;
+}
+
+template <typename T, bool FIELD, bool MIXED, bool BIG>
+__global__ void __launch_bounds__(128) k_p2p(
+    const int4 *__restrict__ items, const int *__restrict__ near_off,
+    const int *__restrict__ near_rng, const int2 *__restrict__ be, const float4 *__restrict__ chi,
+    const float4 *__restrict__ clo, const double *__restrict__ sx, const double *__restrict__ sy,
+    const double *__restrict__ sz, const double *__restrict__ sq,
+    const real4<float> *__restrict__ rel32, double *__restrict__ acc_pot,
+    double *__restrict__ acc_fld) {
+  int L, ia = 0, ib = 0;
+  if (BIG) {
+    int4 it = items[blockIdx.x];
+    L = it.x;
+    ia = it.y;
+    ib = it.z;
+  } else {
+    L = blockIdx.x;
+  }
+  const int2 tbe = be[L];
+  const int b = tbe.x, nt = tbe.y - tbe.x;
+  const int tpt = nt <= 8 ? 16 : (nt <= 16 ? 8 : (nt <= 32 ? 4 : (nt <= 64 ? 2 : 1)));
+  const int gsz = blockDim.x / tpt;
+  const int sub = threadIdx.x % tpt;
+  const bool leaf_strided = nt <= 8;
+  const int r0 = near_off[L], r1 = near_off[L + 1];
+  float4 tch = make_float4(0.f, 0.f, 0.f, 0.f), tcl = tch;
+  if (MIXED) {
+    tch = chi[L];
+    tcl = clo[L];
+  }
+  for (int tb = 0; tb < nt; tb += gsz) {
+    const int ti = tb + threadIdx.x / tpt;
+    const bool active = ti < nt;
+    const int t = b + (active ? ti : 0);
+    double pot = 0, fx = 0, fy = 0, fz = 0;
+    const double tx64 = sx[t], ty64 = sy[t], tz64 = sz[t];
+    float tx = 0.f, ty = 0.f, tz = 0.f;
+    if (MIXED) {
+      real4<float> r = rel32[t];
+      tx = r.x; ty = r.y; tz = r.z;
+    }
+    int kleaf = 0;
+    // tiny target leaves: a target's threads take whole source leaves in turn;
+    // otherwise they split every source leaf's points (keeps the warp converged)
+    auto do_leaf = [&](int lf, int j0, int js) {
+      const int2 sbe = be[lf];
+      if (MIXED) {
+        const float4 sh = chi[lf], sl = clo[lf];
+        // target position relative to the source leaf centre
+        const float ox = tx - ((sh.x - tch.x) + (sl.x - tcl.x));
+        const float oy = ty - ((sh.y - tch.y) + (sl.y - tcl.y));
+        const float oz = tz - ((sh.z - tch.z) + (sl.z - tcl.z));
+        const float thr2 = tch.w;
+        float p0 = 0.f, f0 = 0.f, f1 = 0.f, f2 = 0.f;
+        for (int j = sbe.x + j0; j < sbe.y; j += js) {
+          const real4<float> sj = rel32[j];
+          float dx = ox - sj.x, dy = oy - sj.y, dz = oz - sj.z;
+          float r2 = dx * dx + dy * dy + dz * dz;
+          if (r2 < thr2) {
+            if (j == t) {
+              r2 = 0.f;
+            } else {
+              // close pair: difference from the FP64 positions
+              dx = (float)(tx64 - sx[j]);
+              dy = (float)(ty64 - sy[j]);
+              dz = (float)(tz64 - sz[j]);
+              r2 = dx * dx + dy * dy + dz * dz;
+            }
+          }
+          const bool ok = FIELD ? (r2 > 1e-10f) : (r2 > 0.f);
+          const float inv = ok ? rsqrtf(r2) : 0.f;
+          const float qi = sj.q * inv;
+          p0 += qi;
+          if (FIELD) {
+            const float q3 = qi * inv * inv;
+            f0 -= q3 * dx;
+            f1 -= q3 * dy;
+            f2 -= q3 * dz;
+          }
+        }
+        pot += (double)p0;
+        if (FIELD) {
+          fx += (double)f0;
+          fy += (double)f1;
+          fz += (double)f2;
+        }
+      } else {
+        for (int j = sbe.x + j0; j < sbe.y; j += js) {
+          const double dx = tx64 - sx[j], dy = ty64 - sy[j], dz = tz64 - sz[j];
+          const double r2 = dx * dx + dy * dy + dz * dz;
+          const bool ok = FIELD ? (r2 > 1e-10) : (j != t);
+          const double inv = ok ? rsqrt(r2) : 0.;
+          const double qi = sq[j] * inv;
+          pot += qi;
+          if (FIELD) {
+            const double q3 = qi * inv * inv;
+            fx -= q3 * dx;
+            fy -= q3 * dy;
+            fz -= q3 * dz;
+          }
+        }
+      }
+    };
+    if (BIG) {
+      if (leaf_strided)
+        for (int lf = ia + sub; lf < ib; lf += tpt) do_leaf(lf, 0, 1);
+      else
+        for (int lf = ia; lf < ib; ++lf) do_leaf(lf, sub, tpt);
+    } else {
+      for (int rr = r0; rr < r1; ++rr) {
+        const int la = near_rng[2 * rr], lb = near_rng[2 * rr + 1];
+        if (lb <= la) continue;
+        if (rng_count(be, la, lb) > kBigRange) continue;  // chunked by the BIG pass
+        if (leaf_strided) {
+          for (int lf = la; lf < lb; ++lf, ++kleaf)
+            if (kleaf % tpt == sub) do_leaf(lf, 0, 1);
+        } else {
+          for (int lf = la; lf < lb; ++lf) do_leaf(lf, sub, tpt);
+        }
+      }
+    }
+    for (int o = 1; o < tpt; o <<= 1) {
+      pot += __shfl_xor_sync(kFull, pot, o);
+      if (FIELD) {
+        fx += __shfl_xor_sync(kFull, fx, o);
+        fy += __shfl_xor_sync(kFull, fy, o);
+        fz += __shfl_xor_sync(kFull, fz, o);
+      }
+    }
+    if (active && sub == 0) {
+      if (BIG) {
+        atomicAdd(&acc_pot[t], pot);
+        if (FIELD) {
+          atomicAdd(&acc_fld[3 * (size_t)t], fx);
+          atomicAdd(&acc_fld[3 * (size_t)t + 1], fy);
+          atomicAdd(&acc_fld[3 * (size_t)t + 2], fz);
+        }
+      } else {
+        acc_pot[t] = pot;
+        if (FIELD) {
+          acc_fld[3 * (size_t)t] = fx;
+          acc_fld[3 * (size_t)t + 1] = fy;
+          acc_fld[3 * (size_t)t + 2] = fz;
+        }
+      }
+    }
+  }
+}
+
+template <bool FIELD, bool MIXED, bool BIG>
+void launch_one(AranGpuSolver3d *s, int grid, cudaStream_t st) {
+  DevTree &t = s->tree;
+  using T = typename std::conditional<MIXED, float, double>::type;
+  k_p2p<T, FIELD, MIXED, BIG><<<grid, 128, 0, st>>>(
+      t.big_items.ptr, t.near_off.ptr, t.near_rng.ptr, t.leaf_be.ptr, t.leaf_chi.ptr,
+      t.leaf_clo.ptr, s->sx.ptr, s->sy.ptr, s->sz.ptr, s->sq.ptr, s->rel32.ptr, s->acc_pot.ptr,
+      s->acc_fld.ptr);
+  ACHECK(cudaGetLastError());
+  s->launches++;
+}
+
+template <bool FIELD, bool MIXED>
+void launch_pair(AranGpuSolver3d *s, cudaStream_t st) {
+  launch_one<FIELD, MIXED, false>(s, s->tree.nleaves, st);
+  if (s->tree.n_big) launch_one<FIELD, MIXED, true>(s, s->tree.n_big, st);
+}
+
+}  // namespace
+
+void build_p2p_work(AranGpuSolver3d *s) {
+  cudaStream_t st = s->s0;
+  DevTree &t = s->tree;
+  const int TB = 256;
+  int nl = t.nleaves;
+  t.leaf_be.reserve(nl);
+  t.leaf_chi.reserve(nl);
+  t.leaf_clo.reserve(nl);
+  double ex = s->cfg.ub[0] - s->cfg.lb[0], ey = s->cfg.ub[1] - s->cfg.lb[1],
+         ez = s->cfg.ub[2] - s->cfg.lb[2];
+  k_leaf_info<<<ceil_div(nl, TB), TB, 0, st>>>(nl, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
+                                               t.depth.ptr, t.center.ptr, ex, ey, ez,
+                                               t.leaf_be.ptr, t.leaf_chi.ptr, t.leaf_clo.ptr);
+  ACHECK(cudaGetLastError());
+  s->launches++;
+  DBuf<int> &cnt = s->scan_tmp;
+  cnt.reserve(2 * (size_t)nl + 2);
+  int *off = cnt.ptr + nl + 1;
+  k_big_items<<<ceil_div(nl, TB), TB, 0, st>>>(nl, t.near_off.ptr, t.near_rng.ptr, t.leaf_be.ptr,
+                                               cnt.ptr, nullptr, nullptr, 0);
+  ACHECK(cudaGetLastError());
+  s->launches++;
+  ACHECK(cudaMemsetAsync(cnt.ptr + nl, 0, sizeof(int), st));
+  {
+    size_t bytes = 0;
+    ACHECK(cub::DeviceScan::ExclusiveSum(nullptr, bytes, cnt.ptr, off, nl + 1, st));
+    s->cub_tmp.reserve(bytes);
+    ACHECK(cub::DeviceScan::ExclusiveSum(s->cub_tmp.ptr, bytes, cnt.ptr, off, nl + 1, st));
+    s->launches += 2;
+  }
+  int nbig = 0;
+  ACHECK(cudaMemcpyAsync(&nbig, off + nl, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaStreamSynchronize(st));
+  t.n_big = nbig;
+  if (nbig) {
+    t.big_items.reserve(nbig);
+    k_big_items<<<ceil_div(nl, TB), TB, 0, st>>>(nl, t.near_off.ptr, t.near_rng.ptr,
+                                                 t.leaf_be.ptr, cnt.ptr, off, t.big_items.ptr, 1);
+    ACHECK(cudaGetLastError());
+    s->launches++;
+  }
+}
+
+void launch_p2p(AranGpuSolver3d *s, cudaStream_t st) {
+  const bool mixed = s->cfg.precision == ARAN_PRECISION_MIXED;
+  const bool field = s->cfg.field != 0;
+  if (mixed) {
+    if (field) launch_pair<true, true>(s, st);
+    else launch_pair<false, true>(s, st);
+  } else {
+    if (field) launch_pair<true, false>(s, st);
+    else launch_pair<false, false>(s, st);
+  }
+}
+
+}  // namespace aran

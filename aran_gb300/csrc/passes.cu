@@ -3,8 +3,8 @@
 // LibAran runs them as callbacks from tree traversals (aran/aransolver3d.c):
 //   clear_func :399-410   -> one memset of all expansions
 //   up_func :412-450      -> k_p2m (leaves) + k_m2m_rotate (level by level)
-//   far_func :333-354     -> k_m2l_rotate (every directed far pair)
-//   near_func :254-324    -> k_p2p (every leaf against its near ranges)
+//   far_func :333-354     -> k_m2l_sibling (m2l.cu)
+//   near_func :254-324    -> k_p2p (p2p.cu)
 //   down_func :452-490    -> k_l2l_rotate (level by level) + k_l2p
 // The operators are the "point and shoot" rotation flavour of
 // aran/aransphericalseriesd-rotate.c (rotate to the z axis, translate along
@@ -211,84 +211,6 @@ __global__ void k_m2m_rotate(int cnt, int off, const int *__restrict__ child,
 }
 
 // ---------------------------------------------------------------------------
-// M2L rotate: aran_spherical_seriesd_to_local_rotate
-// (aran/aransphericalseriesd-rotate.c:165-207) with the vertical M2L of
-// aran/aransphericalseriesd-translate.c:609-676.  One warp per target node,
-// looping over its far list; the target local stays in registers.
-// ---------------------------------------------------------------------------
-template <typename T>
-__global__ void k_m2l_rotate(int cnt, int off, const int *__restrict__ far_off,
-                             const int *__restrict__ far_src, const uint16_t *__restrict__ far_dir,
-                             const uint8_t *__restrict__ depth, int p, const T *__restrict__ dirs,
-                             DirOffsets D, const T *__restrict__ vt, const uint8_t *__restrict__ lm_g,
-                             double scale_e, const cplx<T> *__restrict__ mult,
-                             cplx<T> *__restrict__ loc) {
-  extern __shared__ unsigned char smem_raw[];
-  const int nm = tri(p), nl = tri(p + 1);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-  uint8_t *lm = smem_raw;
-  size_t lmb = (2 * nl + 15) & ~15;
-  T *vts = reinterpret_cast<T *>(smem_raw + lmb);
-  size_t vtb = ((size_t)nl * p * sizeof(T) + 15) & ~15;
-  cplx<T> *bufs = reinterpret_cast<cplx<T> *>(smem_raw + lmb + vtb);
-  for (int i = threadIdx.x; i < 2 * nl; i += blockDim.x) lm[i] = lm_g[i];
-  for (int i = threadIdx.x; i < nl * p; i += blockDim.x) vts[i] = vt[i];
-  __syncthreads();
-  const int t = off + blockIdx.x * wpb + w;
-  if (t >= off + cnt) return;
-  const int j0 = far_off[t], j1 = far_off[t + 1];
-  if (j0 == j1) return;
-  cplx<T> *src = bufs + (size_t)w * (nm + nm + nl);
-  cplx<T> *rot = src + nm;
-  cplx<T> *tr = rot + nm;
-  constexpr int KMAX = ((kMaxOrder + 1) * (kMaxOrder + 2) / 2 + 31) / 32;
-  cplx<T> acc[KMAX];
-#pragma unroll
-  for (int k = 0; k < KMAX; ++k) acc[k] = cmake<T>(0, 0);
-  const int K = (nl + 31) / 32;
-  for (int j = j0; j < j1; ++j) {
-    const int s = far_src[j];
-    const T *tab = dirs + (size_t)far_dir[j] * D.stride;
-    load_phased(mult + (size_t)s * nm, nm, lm, tab + D.ph, src, lane);
-    __syncwarp();
-    for (int c = lane; c < nm; c += 32) rot[c] = rot_one(tab + D.ef, tab + D.of, src, lm[2 * c], lm[2 * c + 1]);
-    __syncwarp();
-    const T *rp = tab + D.rp;
-    for (int c = lane; c < nl; c += 32) {
-      int l = lm[2 * c], m = lm[2 * c + 1];
-      const T *vrow = vts + c * p;
-      T re = 0, im = 0;
-      for (int n = m; n < p; ++n) {
-        T f = vrow[n] * rp[l + n + 1];
-        cplx<T> r = rot[tri(n, m)];
-        re += f * r.re;
-        im += f * r.im;
-      }
-      tr[c] = cmake<T>(re, im);
-    }
-    __syncwarp();
-#pragma unroll
-    for (int k = 0; k < KMAX; ++k) {
-      int c = lane + 32 * k;
-      if (k < K && c < nl) {
-        int l = lm[2 * c], mp = lm[2 * c + 1];
-        cplx<T> v = rot_one(tab + D.ei, tab + D.oi, tr, l, mp);
-        T cr = tab[D.ph + 2 * mp], ci = -tab[D.ph + 2 * mp + 1];
-        acc[k].re += v.re * cr - v.im * ci;
-        acc[k].im += v.re * ci + v.im * cr;
-      }
-    }
-    __syncwarp();
-  }
-  const T ih = inv_scale<T>(depth[t], scale_e);
-#pragma unroll
-  for (int k = 0; k < KMAX; ++k) {
-    int c = lane + 32 * k;
-    if (k < K && c < nl) loc[(size_t)t * nl + c] = cmake<T>(acc[k].re * ih, acc[k].im * ih);
-  }
-}
-
-// ---------------------------------------------------------------------------
 // L2L rotate: aran_development3d_l2l_rotate (arandevelopment3d.c:444-451),
 // vertical part aran/aransphericalseriesd-translate.c:301-364.  One warp per
 // non-empty node of the level, adding its parent's translated local.
@@ -448,110 +370,6 @@ __global__ void k_l2p(int nleaves, const int *__restrict__ leaf_node, const int 
   }
 }
 
-// ---------------------------------------------------------------------------
-// P2P: the near_func of aran/aransolver3d.c:254-324 with the Newton kernels
-// of tests/newtonpot3.c:61-78 (potential) and tests/newtonfield3.c:91-119
-// (field, |r| > 1e-5 guard).  One block per target leaf; every target sums
-// its near ranges directly (both sides of a pair are computed by their own
-// targets instead of the reference's symmetric update).  threads-per-target
-// adapts to the leaf size.  MIXED: FP32 positions relative to the leaf
-// centres, shifted per source leaf, per-source-leaf FP32 partial sums added
-// into FP64 accumulators.
-// ---------------------------------------------------------------------------
-template <typename T, bool FIELD, bool MIXED>
-__global__ void __launch_bounds__(128) k_p2p(
-    int nleaves, const int *__restrict__ leaf_node, const int *__restrict__ begin,
-    const int *__restrict__ end, const double *__restrict__ center, const int *__restrict__ near_off,
-    const int *__restrict__ near_rng, const double *__restrict__ sx, const double *__restrict__ sy,
-    const double *__restrict__ sz, const double *__restrict__ sq, const real4<float> *__restrict__ rel32,
-    double *__restrict__ acc_pot, double *__restrict__ acc_fld) {
-  const int L = blockIdx.x;
-  const int node = leaf_node[L];
-  const int b = begin[node], e = end[node];
-  const int nt = e - b;
-  const int tpt = nt <= 32 ? 4 : (nt <= 64 ? 2 : 1);
-  const int gsz = blockDim.x / tpt;
-  const int sub = threadIdx.x % tpt;
-  const int r0 = near_off[L], r1 = near_off[L + 1];
-  const double cx = center[3 * node], cy = center[3 * node + 1], cz = center[3 * node + 2];
-  for (int tb = 0; tb < nt; tb += gsz) {
-    const int ti = tb + threadIdx.x / tpt;
-    const bool active = ti < nt;
-    const int t = b + (active ? ti : 0);
-    double pot = 0, fx = 0, fy = 0, fz = 0;
-    T tx, ty, tz;
-    if (MIXED) {
-      real4<float> r = rel32[t];
-      tx = r.x; ty = r.y; tz = r.z;
-    } else {
-      tx = sx[t]; ty = sy[t]; tz = sz[t];
-    }
-    for (int rr = r0; rr < r1; ++rr) {
-      const int la = near_rng[2 * rr], lb = near_rng[2 * rr + 1];
-      for (int lf = la; lf < lb; ++lf) {
-        const int sn = leaf_node[lf];
-        const int sb = begin[sn], se = end[sn];
-        if (MIXED) {
-          // target relative to the source leaf centre
-          float ox = tx - (float)(center[3 * sn] - cx);
-          float oy = ty - (float)(center[3 * sn + 1] - cy);
-          float oz = tz - (float)(center[3 * sn + 2] - cz);
-          float p0 = 0.f, f0 = 0.f, f1 = 0.f, f2 = 0.f;
-          for (int j = sb + sub; j < se; j += tpt) {
-            real4<float> sj = rel32[j];
-            float dx = ox - sj.x, dy = oy - sj.y, dz = oz - sj.z;
-            float r2 = dx * dx + dy * dy + dz * dz;
-            bool ok = FIELD ? (r2 > 1e-10f) : (r2 > 0.f);
-            float inv = ok ? rsqrtf(r2) : 0.f;
-            float qi = sj.q * inv;
-            p0 += qi;
-            if (FIELD) {
-              float q3 = qi * inv * inv;
-              f0 -= q3 * dx;
-              f1 -= q3 * dy;
-              f2 -= q3 * dz;
-            }
-          }
-          pot += (double)p0;
-          if (FIELD) { fx += (double)f0; fy += (double)f1; fz += (double)f2; }
-        } else {
-          for (int j = sb + sub; j < se; j += tpt) {
-            double dx = (double)tx - sx[j], dy = (double)ty - sy[j], dz = (double)tz - sz[j];
-            double r2 = dx * dx + dy * dy + dz * dz;
-            bool ok = FIELD ? (r2 > 1e-10) : (j != t);
-            double inv = ok ? rsqrt(r2) : 0.;
-            double qi = sq[j] * inv;
-            pot += qi;
-            if (FIELD) {
-              double q3 = qi * inv * inv;
-              fx -= q3 * dx;
-              fy -= q3 * dy;
-              fz -= q3 * dz;
-            }
-          }
-        }
-      }
-    }
-    // reduce over the tpt threads of this target (consecutive lanes)
-    for (int o = 1; o < tpt; o <<= 1) {
-      pot += __shfl_xor_sync(kFull, pot, o);
-      if (FIELD) {
-        fx += __shfl_xor_sync(kFull, fx, o);
-        fy += __shfl_xor_sync(kFull, fy, o);
-        fz += __shfl_xor_sync(kFull, fz, o);
-      }
-    }
-    if (active && sub == 0) {
-      acc_pot[t] = pot;
-      if (FIELD) {
-        acc_fld[3 * (size_t)t] = fx;
-        acc_fld[3 * (size_t)t + 1] = fy;
-        acc_fld[3 * (size_t)t + 2] = fz;
-      }
-    }
-  }
-}
-
 __global__ void k_scatter(int64_t n, const int *__restrict__ perm, const double *__restrict__ acc_pot,
                           const double *__restrict__ acc_fld, double *__restrict__ pot,
                           double *__restrict__ fld) {
@@ -620,29 +438,12 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   // near field on the second stream, as soon as the lists exist
   ACHECK(cudaStreamWaitEvent(s->s1, s->ev[2 * Stage::LISTS + 1], 0));
   ACHECK(cudaEventRecord(s->ev[2 * Stage::P2P], s->s1));
-  {
-    const bool mixed = s->cfg.precision == ARAN_PRECISION_MIXED;
-#define P2P_ARGS                                                                         \
-  t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr, t.center.ptr, t.near_off.ptr,       \
-      t.near_rng.ptr, s->sx.ptr, s->sy.ptr, s->sz.ptr, s->sq.ptr, s->rel32.ptr, s->acc_pot.ptr, \
-      s->acc_fld.ptr
-    if (mixed) {
-      if (field) k_p2p<float, true, true><<<t.nleaves, 128, 0, s->s1>>>(P2P_ARGS);
-      else k_p2p<float, false, true><<<t.nleaves, 128, 0, s->s1>>>(P2P_ARGS);
-    } else {
-      if (field) k_p2p<double, true, false><<<t.nleaves, 128, 0, s->s1>>>(P2P_ARGS);
-      else k_p2p<double, false, false><<<t.nleaves, 128, 0, s->s1>>>(P2P_ARGS);
-    }
-#undef P2P_ARGS
-    ACHECK(cudaGetLastError());
-    s->launches++;
-  }
+  launch_p2p(s, s->s1);
   ACHECK(cudaEventRecord(s->ev[2 * Stage::P2P + 1], s->s1));
 
   // clear (aran/aransolver3d.c:399-410)
   ACHECK(cudaMemsetAsync(multb.ptr, 0, (size_t)t.nnodes * nm * 2 * sizeof(T), st));
   ACHECK(cudaMemsetAsync(locb.ptr, 0, (size_t)t.nnodes * nl * 2 * sizeof(T), st));
-  s->launches += 2;
 
   // P2M
   ACHECK(cudaEventRecord(s->ev[2 * Stage::P2M], st));
@@ -675,20 +476,7 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2M + 1], st));
   // M2L over every node of depth >= 2
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L], st));
-  if (t.nlevels > 2) {
-    DirOffsets D = offsets<T>(p, 0);
-    const int WPB = 4;
-    int off = t.level_off[2], cnt = t.nnodes - off;
-    size_t sm = ((2 * nl + 15) & ~15) + (((size_t)nl * p * sizeof(T) + 15) & ~15) +
-                (size_t)WPB * (2 * nm + nl) * sizeof(cplx<T>) + 64;
-    if (sm > 48 * 1024)
-      ACHECK(cudaFuncSetAttribute(k_m2l_rotate<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_m2l_rotate<T><<<ceil_div(cnt, WPB), WPB * 32, sm, st>>>(
-        cnt, off, t.far_off.ptr, t.far_src.ptr, t.far_dir.ptr, t.depth.ptr, p, tb.dir_m2l.ptr, D,
-        tb.vt.ptr, tb.lm.ptr, s->scale_e, mult, loc);
-    ACHECK(cudaGetLastError());
-    s->launches++;
-  }
+  launch_m2l(s, st);
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L + 1], st));
   // L2L, from depth 3 (depth 0-1 locals are zero: no far pairs above depth 2)
   ACHECK(cudaEventRecord(s->ev[2 * Stage::L2L], st));

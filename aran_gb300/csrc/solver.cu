@@ -82,6 +82,8 @@ int aran_gpu_solver3d_create(const AranGpuConfig3d *cfg, AranGpuSolver3d **out) 
     s->scale_e = std::ldexp(1.0, (int)std::ceil(std::log2(ext)));
     if (s->scale_e < ext) s->scale_e *= 2;
     build_tables(s);
+    s->err_dev.reserve(4);
+    ACHECK(cudaMemset(s->err_dev.ptr, 0, sizeof(int)));
   } catch (const CudaError &ce) {
     int r = from_cuda(ce);
     aran_gpu_solver3d_destroy(s);
@@ -118,7 +120,9 @@ void aran_gpu_solver3d_destroy(AranGpuSolver3d *s) {
   s->rel64.release(); s->rel32.release(); s->acc_pot.release(); s->acc_fld.release();
   s->io_xyz.release(); s->io_q.release(); s->io_pot.release(); s->io_fld.release();
   s->mult64.release(); s->loc64.release(); s->mult32.release(); s->loc32.release();
-  s->scan_tmp.release(); s->stats_dev.release();
+  s->scan_tmp.release(); s->stats_dev.release(); s->err_dev.release();
+  t.leaf_be.release(); t.leaf_chi.release(); t.leaf_clo.release(); t.big_items.release();
+  t.parents.release();
   for (auto &ev : s->ev)
     if (ev) cudaEventDestroy(ev);
   if (s->s0) cudaStreamDestroy(s->s0);
@@ -170,6 +174,11 @@ int aran_gpu_solver3d_solve(AranGpuSolver3d *s, int64_t n, const double *xyz, co
     ACHECK(cudaStreamSynchronize(s->s1));
     ACHECK(cudaGetLastError());
     s->have_tree = true;
+    {
+      int derr = 0;
+      ACHECK(cudaMemcpy(&derr, s->err_dev.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+      if (derr) return fail(ARAN_ERR_TIMEOUT, "a bounded device-side wait gave up (M2L table copy)");
+    }
     // stage times
     auto el = [&](int a0, int a1) {
       float ms = 0;

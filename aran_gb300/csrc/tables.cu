@@ -25,8 +25,17 @@ struct DirLayout {
 
 __host__ __device__ DirLayout dir_layout(int p, int kind) {
   DirLayout d;
-  if (kind == 0) { d.Lf = p; d.Li = p + 1; d.nrp = 2 * p + 2; }       // M2L
-  else if (kind == 1) { d.Lf = p; d.Li = p; d.nrp = p + 1; }          // M2M
+  if (kind == 0) {  // M2L: (E, O) interleaved blocks
+    d.Lf = p; d.Li = p + 1; d.nrp = 2 * p + 2;
+    d.ef = 0;
+    d.of = -1;
+    d.ei = 2 * sq_size(d.Lf);
+    d.oi = -1;
+    d.ph = d.ei + 2 * sq_size(d.Li);
+    d.rp = d.ph + 2 * (p + 1);
+    d.stride = ((d.rp + d.nrp) + 3) & ~3;
+    return d;
+  } else if (kind == 1) { d.Lf = p; d.Li = p; d.nrp = p + 1; }          // M2M
   else { d.Lf = p + 1; d.Li = p + 1; d.nrp = p + 2; }                 // L2L
   d.ef = 0;
   d.of = d.ef + sq_size(d.Lf);
@@ -129,9 +138,21 @@ __global__ void k_dir_tables(int p, int kind, int ndir, double ex, double ey, do
   gen_wigner_d(Lmax, theta, w);
   gen_wigner_d(Lmax, -theta, wm);
   wigner_to_eo(L.Lf, w, eo, eo + sq_size(L.Lf));
-  for (int i = 0; i < 2 * sq_size(L.Lf); ++i) o[L.ef + i] = (T)eo[i];
+  if (kind == 0)
+    for (int i = 0; i < sq_size(L.Lf); ++i) {
+      o[L.ef + 2 * i] = (T)eo[i];
+      o[L.ef + 2 * i + 1] = (T)eo[sq_size(L.Lf) + i];
+    }
+  else
+    for (int i = 0; i < 2 * sq_size(L.Lf); ++i) o[L.ef + i] = (T)eo[i];
   wigner_to_eo(L.Li, wm, eo, eo + sq_size(L.Li));
-  for (int i = 0; i < 2 * sq_size(L.Li); ++i) o[L.ei + i] = (T)eo[i];
+  if (kind == 0)
+    for (int i = 0; i < sq_size(L.Li); ++i) {
+      o[L.ei + 2 * i] = (T)eo[i];
+      o[L.ei + 2 * i + 1] = (T)eo[sq_size(L.Li) + i];
+    }
+  else
+    for (int i = 0; i < 2 * sq_size(L.Li); ++i) o[L.ei + i] = (T)eo[i];
   for (int m = 0; m <= p; ++m) {
     o[L.ph + 2 * m] = (T)cos(m * phi);
     o[L.ph + 2 * m + 1] = (T)sin(m * phi);

@@ -264,6 +264,20 @@ __global__ void k_near(int nleaves, const int *__restrict__ leaf_node, const int
   if (!mode) near_cnt[L] = k;
 }
 
+__global__ void k_parent_flags(int nn, const int *__restrict__ child, const uint8_t *__restrict__ depth,
+                               int *__restrict__ flags) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  flags[i] = (child[i] >= 0 && depth[i] >= 1) ? 1 : 0;
+}
+
+__global__ void k_parent_scatter(int nn, const int *__restrict__ flags, const int *__restrict__ pos,
+                                 int *__restrict__ parents) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  if (flags[i]) parents[pos[i]] = i;
+}
+
 // relative (leaf-centred) particle coordinates for the kernels
 template <typename T>
 __global__ void k_relative(int64_t n, const int *__restrict__ incl, const int *__restrict__ leaf_node,
@@ -488,6 +502,23 @@ void build_lists(AranGpuSolver3d *s) {
                                                 t.lf_begin.ptr, t.lf_end.ptr, nullptr,
                                                 t.near_off.ptr, t.near_rng.ptr, 1);
   s->launches++;
+  // internal nodes of depth >= 1: one M2L block each (their children)
+  {
+    DBuf<int> &fl = s->scan_tmp;
+    fl.reserve(2 * (size_t)nn + 2);
+    k_parent_flags<<<ceil_div(nn, TB), TB, 0, st>>>(nn, t.child.ptr, t.depth.ptr, fl.ptr);
+    s->launches++;
+    ACHECK(cudaMemsetAsync(fl.ptr + nn, 0, sizeof(int), st));
+    exclusive_scan(s, fl.ptr, fl.ptr + nn + 1, nn + 1, st);
+    int np = 0;
+    ACHECK(cudaMemcpyAsync(&np, fl.ptr + nn + 1 + nn, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ACHECK(cudaStreamSynchronize(st));
+    t.n_parents = np;
+    t.parents.reserve(np + 1);
+    k_parent_scatter<<<ceil_div(nn, TB), TB, 0, st>>>(nn, fl.ptr, fl.ptr + nn + 1, t.parents.ptr);
+    s->launches++;
+  }
+  build_p2p_work(s);
   ACHECK(cudaEventRecord(s->ev[2 * Stage::LISTS + 1], st));
 }
 

@@ -1,0 +1,383 @@
+#!/usr/bin/env python3
+"""Benchmark: 3D Newton field FMM particles/s on GB300.
+
+One step = one complete solve (Morton keys, sort, tree, interaction lists,
+P2M, M2M, M2L, L2L, L2P, P2P, scatter) of the workload, inputs resident in
+HBM (``value``) or in pinned host memory with the copies inside the timed
+region (``e2e``, through the same C ABI call a user makes).
+
+Workload (default ``plummer4m``): N = 4,000,000 particles from a Plummer
+sphere (a = 0.05, radial cut 1.0, box [-1,1]^3), charges U[0,1], p = 12,
+leaf capacity 64, potential + field, rotate flavour, mixed precision (FP32
+bulk, FP64 tables/centres/final sums).  The same line reports the plain FP64
+GPU path on the same input (``fp64``), the error of the mixed path against
+it and against an FP64 direct sum on a target subset.
+
+``--impl reference`` times the reference algorithm on the host cores: the
+C restatement of LibAran's solver in oracle/ (the reference itself needs
+glib and libvsg, which are not available), one independent process per core
+on bounded samples of the same workload.
+
+Multi-GPU: one process per GPU (torchrun); each rank solves its own
+replica (the path does not shard: independent solves, no collective on the
+data path); ``value`` = particles of all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "3D FMM particles/s at rel-err≤1e-6 vs plain FP64 GPU path; served p50/p99 latency"
+UNIT = "particles/s"
+
+WORKLOADS = {
+    # name: (generator, n, order, maxbox, lb, ub, description)
+    "plummer4m": ("plummer", 4_000_000, 12, 64, (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0),
+                  "N=4,000,000 Plummer (a=0.05, r<=1), q~U[0,1], p=12, leaf 64, field"),
+    "uniform1m": ("uniform", 1_000_000, 12, 64, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0),
+                  "N=1,000,000 uniform in [0,1]^3, q~U[-1,1], p=12, leaf 64, field"),
+}
+
+
+def m2l_flops(p: int) -> int:
+    """Algorithmic flops of one rotate-flavour M2L: 4[A(p-1) + B(p) + A(p)]
+    with A(L) = (L+1)(L+2)(4L+3)/6 (real d-matrix x complex rotation MACs)
+    and B(p) = p(p+1)(p+2)/3 (vertical translation MACs)."""
+    A = lambda L: (L + 1) * (L + 2) * (4 * L + 3) // 6
+    return 4 * (A(p - 1) + p * (p + 1) * (p + 2) // 3 + A(p))
+
+
+def make_workload(name: str, seed_offset: int = 0):
+    from aran_gb300 import workloads as W
+    gen, n, p, maxbox, lb, ub, desc = WORKLOADS[name]
+    seed = (3 if gen == "plummer" else 2) + 1000 * seed_offset
+    x, q = getattr(W, gen)(n, seed)
+    return x, q
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (200 ms period)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in open(self.path):
+            parts = [s.strip() for s in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------- CPU baseline
+def _cpu_job(args):
+    name, n_sample, seed = args
+    import numpy as np
+    import oracle
+    from aran_gb300 import workloads as W
+    gen, n, p, maxbox, lb, ub, desc = WORKLOADS[name]
+    x, q = getattr(W, gen)(n_sample, 100 + seed)
+    t0 = time.perf_counter()
+    oracle.solve(x, q, order=p, maxbox=maxbox, flavour="rotate", field=True, lb=lb, ub=ub)
+    return n_sample, time.perf_counter() - t0
+
+
+def cpu_baseline(name: str, n_sample: int, procs: int, rounds: int = 1) -> dict:
+    """Times the oracle port of the reference solver: `procs` independent
+    single-threaded processes (the reference has no threading), each solving
+    its own n_sample-particle draw of the workload distribution."""
+    import oracle
+    oracle.build()
+    ctx = mp.get_context("spawn")
+    total_n, t0 = 0, time.perf_counter()
+    with ctx.Pool(procs) as pool:
+        for r in range(rounds):
+            for n_done, _ in pool.map(_cpu_job, [(name, n_sample, r * procs + i) for i in range(procs)]):
+                total_n += n_done
+    el = time.perf_counter() - t0
+    return {"value": total_n / el, "unit": UNIT, "cores": procs, "kind": "port",
+            "sample": f"{procs} processes x {rounds} round(s), each a full solve of its own "
+                      f"{n_sample}-particle draw of the workload distribution "
+                      f"(same p, leaf size, flavour, field); {el:.1f} s wall"}
+
+
+# ----------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    import aran_gb300 as A
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    gen, n, p, maxbox, lb, ub, desc = WORKLOADS[args.workload]
+    x, q = make_workload(args.workload, seed_offset=rank)
+    dev = torch.device("cuda", local)
+    dx = torch.from_numpy(x).to(dev).contiguous()
+    dq = torch.from_numpy(q).to(dev).contiguous()
+    pot = torch.empty(n, dtype=torch.float64, device=dev)
+    fld = torch.empty((n, 3), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def solve_dev(s):
+        s.solve_device(n, dx.data_ptr(), dq.data_ptr(), pot.data_ptr(), fld.data_ptr())
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(s, fn, steps):
+        barrier()
+        t0 = time.perf_counter()
+        stage = []
+        launches = 0
+        for _ in range(steps):
+            flush.fill_(1.0)           # evict L2 between steps (256 MB > 129 MB L2)
+            fn(s)
+            stage.append(s.timings())
+            launches += s.launches()
+        barrier()
+        el = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([el], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        return el, stage, launches
+
+    results = {}
+    # plain FP64 path on the same input (reference point of the metric)
+    with A.Solver3d(lb, ub, maxbox=maxbox, order=p, flavour="rotate", field=True,
+                    precision="fp64") as s64:
+        for _ in range(max(1, min(args.warmup, 2))):
+            solve_dev(s64)
+        el64, st64, _ = timed(s64, solve_dev, max(1, args.fp64_steps))
+        pot64 = pot.cpu().numpy().copy()
+        fld64 = fld.cpu().numpy().copy()
+        results["fp64_s_per_step"] = el64 / max(1, args.fp64_steps)
+        results["fp64_stage_ms"] = {k: round(statistics.mean(d[k] for d in st64), 3) for k in st64[0]}
+
+    s = A.Solver3d(lb, ub, maxbox=maxbox, order=p, flavour="rotate", field=True,
+                   precision=args.precision)
+    for _ in range(args.warmup):
+        solve_dev(s)
+    clocks = ClockSampler(local)
+    clocks.start()
+    el, stages, launches = timed(s, solve_dev, args.steps)
+    clk = clocks.stop()
+    potm = pot.cpu().numpy().copy()
+    fldm = fld.cpu().numpy().copy()
+    info = s.tree_info()
+    stats = s.get_stats()
+
+    # end to end through the host-pointer call: pinned host buffers, H2D and
+    # D2H inside the timed region
+    hx = torch.from_numpy(x).pin_memory()
+    hq = torch.from_numpy(q).pin_memory()
+    hpot = torch.empty(n, dtype=torch.float64).pin_memory()
+    hfld = torch.empty((n, 3), dtype=torch.float64).pin_memory()
+
+    def solve_host(s_):
+        A._check(A.load().aran_gpu_solver3d_solve(
+            s_._h, n, A.C.c_void_p(hx.data_ptr()), A.C.c_void_p(hq.data_ptr()),
+            A.C.c_void_p(hpot.data_ptr()), A.C.c_void_p(hfld.data_ptr()), A.MEM_HOST))
+
+    for _ in range(2):
+        solve_host(s)
+    el_e2e, _, _ = timed(s, solve_host, args.steps)
+    s.close()
+
+    if rank != 0:
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    # accuracy: mixed vs FP64 GPU path, both vs FP64 direct sum on a subset
+    def rl2(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    acc = {"pot_vs_fp64_gpu": rl2(potm, pot64), "field_vs_fp64_gpu": rl2(fldm, fld64)}
+    if args.direct_targets > 0:
+        import oracle
+        tgt = np.random.default_rng(5).choice(n, args.direct_targets, replace=False)
+        rp, rf = oracle.direct(x, q, targets=tgt)
+        acc.update({"targets": args.direct_targets,
+                    "pot_vs_direct": rl2(potm[tgt], rp), "field_vs_direct": rl2(fldm[tgt], rf),
+                    "fp64_pot_vs_direct": rl2(pot64[tgt], rp),
+                    "fp64_field_vs_direct": rl2(fld64[tgt], rf)})
+
+    ms_step = 1e3 * el / args.steps
+    value = world * n * args.steps / el
+    stage_ms = {k: round(statistics.mean(d[k] for d in stages), 4) for k in stages[0]}
+    # roofline of the dominant kernel (M2L): algorithmic flops per launch over
+    # its CUDA-event duration (recorded on the launching stream by the library)
+    flops = info["far"] * m2l_flops(p)
+    m2l_s = stage_ms["m2l"] * 1e-3
+    smax = clk.get("sm_max_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * smax * 1e6 / 1e12
+    achieved = flops / m2l_s / 1e12
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    # algorithmic bytes of the M2L launch: every far source multipole and every
+    # written local once (FP32 complex), at the HBM roofline
+    alg_bytes = (info["far"] * (p * (p + 1) // 2) + info["nodes"] * ((p + 1) * (p + 2) // 2)) * 8
+    roof = {
+        "kernel": "k_m2l_rotate<float>",
+        "bound": "fp32",
+        "achieved": round(achieved, 3), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
+        "frac": round(achieved / fp32_peak, 4),
+        "peak_source": ("FP32 CUDA-core peak 152 SMs x 128 lanes x 2 flop x max SM clock; "
+                        "MEASURED_PEAKS.json holds only HBM and bf16-tensor peaks, and this "
+                        "kernel runs on the FP32 pipes"),
+        "flops_per_launch": flops, "m2l_per_launch": info["far"],
+        "flops_per_m2l": m2l_flops(p),
+        "hbm_view": {"bytes_per_launch": alg_bytes,
+                     "achieved_gbs": round(alg_bytes / m2l_s / 1e9, 1),
+                     "peak_gbs": peaks.get("hbm_gbs", 6803.8),
+                     "frac": round(alg_bytes / m2l_s / 1e9 / peaks.get("hbm_gbs", 6803.8), 4)},
+        "traffic": args.m2l_traffic,
+        "bf16_tensor_peak_tflops": peaks.get("bf16_tflops"),
+    }
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+        "data": "synthetic (seeded Plummer/uniform draws, no dataset)",
+        "config": {"workload": args.workload, "description": desc, "n_per_gpu": n, "order": p,
+                   "maxbox": maxbox, "flavour": "rotate", "precision": args.precision,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "flushed between steps by a 256 MB device write (inside the timed region)"},
+        "fp64": {"value": world * n / results["fp64_s_per_step"], "unit": UNIT,
+                 "ms_per_step": 1e3 * results["fp64_s_per_step"],
+                 "stage_ms": results["fp64_stage_ms"]},
+        "speedup_vs_fp64_gpu": (value / world) / (n / results["fp64_s_per_step"]),
+        "accuracy": acc,
+        "stage_ms": stage_ms,
+        "tree": info, "stats": stats,
+        "roofline": roof,
+        "clocks": clk,
+        "e2e": {"value": world * n * args.steps / el_e2e, "unit": UNIT,
+                "ms_per_step": 1e3 * el_e2e / args.steps,
+                "h2d_bytes_per_step": n * 3 * 8 + n * 8,
+                "d2h_bytes_per_step": n * 8 + n * 3 * 8},
+        "gpu_launches": launches,
+    }
+    if args.cpu_baseline:
+        procs = args.cpu_procs or os.cpu_count() or 1
+        line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_sample, procs)
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    gen, n, p, maxbox, lb, ub, desc = WORKLOADS[args.workload]
+    procs = args.cpu_procs or os.cpu_count() or 1
+    for _ in range(args.warmup if args.ref_warmup else 0):
+        cpu_baseline(args.workload, max(2000, args.cpu_sample // 10), procs)
+    res = cpu_baseline(args.workload, args.cpu_sample, procs, rounds=args.steps)
+    line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": UNIT,
+            "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "description": desc, "order": p,
+                       "maxbox": maxbox, "flavour": "rotate", "precision": "fp64 (reference)"},
+            "cpu_baseline": res,
+            "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="plummer4m", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--direct-targets", type=int, default=1000)
+    ap.add_argument("--cpu-baseline", type=int, default=1)
+    ap.add_argument("--cpu-sample", type=int, default=20000)
+    ap.add_argument("--cpu-procs", type=int, default=0)
+    ap.add_argument("--ref-warmup", type=int, default=0)
+    ap.add_argument("--m2l-traffic", type=float, default=None,
+                    help="dram bytes per M2L launch from an ncu capture (profiles/)")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

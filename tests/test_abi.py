@@ -1,0 +1,84 @@
+"""The C-ABI library builds, loads and exports every symbol include/*.h declares.
+
+No compute call is made here; without a GPU the solver constructor must fail
+loudly (ARAN_ERR_NO_DEVICE) rather than fall back to the CPU.
+"""
+import ctypes as C
+import glob
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b(aran_\w+)\s*\(", text, flags=re.M):
+            names.append(m.group(1))
+    return sorted(set(names))
+
+
+def lib_path():
+    import aran_gb300
+    aran_gb300.load()
+    return aran_gb300.LIB_PATH
+
+
+def test_headers_declare_functions():
+    names = declared_functions()
+    assert "aran_gpu_solver3d_solve" in names
+    assert len(names) >= 10
+
+
+def test_library_exports_every_declared_symbol():
+    path = lib_path()
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_library_loads_with_ctypes():
+    L = C.CDLL(lib_path())
+    for n in declared_functions():
+        assert hasattr(L, n), n
+
+
+def test_python_mirror_lists_exports():
+    import aran_gb300
+    for n in aran_gb300.EXPORTS:
+        assert n in declared_functions()
+
+
+def test_no_device_fails_loudly():
+    import aran_gb300
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(aran_gb300.AranError) as ei:
+        aran_gb300.Solver3d()
+    assert ei.value.code == -3
+
+
+def test_invalid_configs_rejected_before_device_use():
+    import aran_gb300
+    bad = [dict(order=0), dict(order=99), dict(maxbox=0), dict(max_depth=30),
+           dict(precision=7)]
+    for kw in bad:
+        with pytest.raises(aran_gb300.AranError) as ei:
+            aran_gb300.Solver3d(**kw)
+        assert ei.value.code == -1, kw
+    with pytest.raises(aran_gb300.AranError) as ei:
+        aran_gb300.Solver3d((0, 0, 0), (0, 1, 1))
+    assert ei.value.code == -1

@@ -1,0 +1,194 @@
+"""GPU path against the oracle, through the C ABI (libaran_gpu.so).
+
+* tree, far (M2L) and near (P2P) lists and the permutation: bit-exact;
+* call counters of aran_solver3d_get_stats: equal;
+* FP64 path: potential/field within 1e-12 (rel-L2) of the oracle FMM with
+  the same tree and operators (only summation order differs);
+* mixed path: within 3e-6 (rel-L2) of the oracle FMM;
+* both: within the FMM truncation error of the FP64 direct sum.
+"""
+import numpy as np
+import pytest
+
+from aran_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_TOL = 3e-6
+
+
+def unordered(pairs):
+    return set(map(tuple, np.sort(np.asarray(pairs, dtype=np.uint64), axis=1).tolist()))
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def check_lists(s, oracle, x, maxbox, lb, ub, max_depth=21):
+    g = s.tree_lists()
+    o = oracle.tree_lists(x, maxbox=maxbox, lb=lb, ub=ub, max_depth=max_depth)
+    gi = {int(i): (int(b), int(e), int(l)) for i, b, e, l in zip(g["ids"], g["begin"], g["end"], g["leaf"])}
+    oi = {int(i): (int(b), int(e), int(l)) for i, b, e, l in zip(o["ids"], o["begin"], o["end"], o["leaf"])}
+    assert gi == oi
+    far_g = g["far"]
+    assert len(far_g) == 2 * len(o["far"])  # directed vs unordered
+    assert unordered(far_g) == set(map(tuple, o["far"].tolist()))
+    assert unordered(g["near"]) == set(map(tuple, o["near"].tolist()))
+    assert np.array_equal(g["perm"], o["perm"])
+
+
+CASES = [
+    # name, generator, n, maxbox, p, lb, ub
+    ("uniform", lambda n: W.uniform(n, 11), 6000, 20, 8, (0, 0, 0), (1, 1, 1)),
+    ("uniform-p12", lambda n: W.uniform(n, 12), 20000, 64, 12, (0, 0, 0), (1, 1, 1)),
+    ("plummer", lambda n: W.plummer(n, 13), 20000, 32, 10, (-1, -1, -1), (1, 1, 1)),
+    ("blobs", lambda n: W.blobs(n, 14, nblobs=3), 15000, 24, 8, (0, 0, 0), (1, 1, 1)),
+    ("circle-maxbox1", lambda n: W.circle(n), 240, 1, 12, (-1, -1, -1), (1, 1, 1)),
+    ("box-aspect", lambda n: W.uniform(n, 15), 8000, 16, 8, (0, 0, 0), (1.0, 1.5, 3.0)),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_fp64_matches_oracle(aran, oracle, case):
+    name, gen, n, maxbox, p, lb, ub = case
+    x, q = gen(n)
+    with aran.Solver3d(lb, ub, maxbox=maxbox, order=p, field=True, precision="fp64") as s:
+        pot, fld = s.solve(x, q)
+        check_lists(s, oracle, x, maxbox, lb, ub)
+        st = s.get_stats()
+    opot, ost = oracle.solve(x, q, order=p, maxbox=maxbox, field=False, lb=lb, ub=ub)
+    ofld, _ = oracle.solve(x, q, order=p, maxbox=maxbox, field=True, lb=lb, ub=ub)
+    assert rel_l2(pot, opot) < FP64_TOL
+    assert rel_l2(fld, ofld) < FP64_TOL
+    assert st == ost
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_mixed_matches_oracle(aran, oracle, case):
+    name, gen, n, maxbox, p, lb, ub = case
+    x, q = gen(n)
+    with aran.Solver3d(lb, ub, maxbox=maxbox, order=p, field=True, precision="mixed") as s:
+        pot, fld = s.solve(x, q)
+        check_lists(s, oracle, x, maxbox, lb, ub)
+    opot, _ = oracle.solve(x, q, order=p, maxbox=maxbox, field=False, lb=lb, ub=ub)
+    ofld, _ = oracle.solve(x, q, order=p, maxbox=maxbox, field=True, lb=lb, ub=ub)
+    assert rel_l2(pot, opot) < MIXED_TOL
+    assert rel_l2(fld, ofld) < MIXED_TOL
+
+
+@pytest.mark.parametrize("p", [1, 2, 4, 6, 16, 20])
+def test_orders_fp64(aran, oracle, p):
+    x, q = W.uniform(4000, 20 + p)
+    with aran.Solver3d(maxbox=24, order=p, field=True, precision="fp64") as s:
+        pot, fld = s.solve(x, q)
+    opot, _ = oracle.solve(x, q, order=p, maxbox=24, field=False)
+    ofld, _ = oracle.solve(x, q, order=p, maxbox=24, field=True)
+    assert rel_l2(pot, opot) < FP64_TOL
+    assert rel_l2(fld, ofld) < FP64_TOL
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 2e-6), ("mixed", 3e-6)])
+def test_p12_against_direct_sum(aran, oracle, precision, tol):
+    """BASELINE accuracy target: p=12 within ~1e-6 of the FP64 direct sum."""
+    x, q = W.uniform(30000, 2)
+    with aran.Solver3d(maxbox=64, order=12, field=True, precision=precision) as s:
+        pot, fld = s.solve(x, q)
+    rp, rf = oracle.direct(x, q)
+    assert rel_l2(pot, rp) < tol
+    assert rel_l2(fld, rf) < tol
+
+
+def test_single_leaf_is_direct_sum(aran, oracle):
+    x, q = W.uniform(50, 5)
+    with aran.Solver3d(maxbox=64, order=8, field=True, precision="fp64") as s:
+        pot, fld = s.solve(x, q)
+        assert s.tree_info()["nodes"] == 1
+    rp, rf = oracle.direct(x, q)
+    assert np.allclose(pot, rp, rtol=1e-13, atol=0)
+    assert np.allclose(fld, rf, rtol=1e-12, atol=1e-12)
+
+
+def test_one_particle(aran):
+    with aran.Solver3d(maxbox=1, order=4, field=True) as s:
+        pot, fld = s.solve(np.array([[0.3, 0.4, 0.5]]), np.array([2.0]))
+    assert pot[0] == 0.0 and np.all(fld == 0.0)
+
+
+def test_boundary_points_and_depth_limit(aran, oracle):
+    # points on the upper faces (clamped into the last cell) and a depth limit
+    rng = np.random.default_rng(9)
+    x = rng.uniform(0, 1, (3000, 3))
+    x[:100, 0] = 1.0
+    x[100:200, 2] = 0.0
+    q = rng.uniform(-1, 1, 3000)
+    with aran.Solver3d(maxbox=4, order=6, field=False, precision="fp64", max_depth=4) as s:
+        pot, _ = s.solve(x, q)
+        check_lists(s, oracle, x, 4, (0, 0, 0), (1, 1, 1), max_depth=4)
+    opot, _ = oracle.solve(x, q, order=6, maxbox=4, field=False, max_depth=4)
+    assert rel_l2(pot, opot) < FP64_TOL
+
+
+def test_potential_only_solver(aran, oracle):
+    x, q = W.uniform(5000, 6)
+    with aran.Solver3d(maxbox=32, order=8, field=False, precision="fp64") as s:
+        pot, fld = s.solve(x, q)
+        assert fld is None
+    opot, _ = oracle.solve(x, q, order=8, maxbox=32, field=False)
+    assert rel_l2(pot, opot) < FP64_TOL
+
+
+def test_solver_reuse_changing_sizes(aran, oracle):
+    with aran.Solver3d(maxbox=16, order=6, field=True, precision="mixed") as s:
+        for n, seed in ((1000, 1), (20000, 2), (300, 3), (20000, 2)):
+            x, q = W.uniform(n, seed)
+            pot, fld = s.solve(x, q)
+            opot, _ = oracle.solve(x, q, order=6, maxbox=16, field=False)
+            assert rel_l2(pot, opot) < MIXED_TOL
+
+
+def test_error_codes(aran):
+    with aran.Solver3d(maxbox=8, order=4, field=False) as s:
+        with pytest.raises(aran.AranError) as ei:
+            s.solve(np.zeros((0, 3)), np.zeros(0))
+        assert ei.value.code == -1
+    with pytest.raises(aran.AranError) as ei:
+        aran.Solver3d(flavour="normal")
+    assert ei.value.code == -6
+
+
+def test_linearity_and_permutation(aran):
+    """Size-independent properties on 1M particles: the solve is linear in the
+    charges and equivariant under a permutation of the input."""
+    x, q1 = W.uniform(1_000_000, 31)
+    q2 = np.random.default_rng(32).uniform(-1, 1, len(q1))
+    with aran.Solver3d(maxbox=64, order=12, field=True, precision="fp64") as s:
+        p1, f1 = s.solve(x, q1)
+        p2, f2 = s.solve(x, q2)
+        p3, f3 = s.solve(x, q1 + 2.0 * q2)
+        perm = np.random.default_rng(33).permutation(len(q1))
+        p4, f4 = s.solve(x[perm], q1[perm])
+    assert rel_l2(p3, p1 + 2.0 * p2) < 1e-12
+    assert rel_l2(f3, f1 + 2.0 * f2) < 1e-12
+    assert rel_l2(p4, p1[perm]) < 1e-13
+    assert rel_l2(f4, f1[perm]) < 1e-13
+
+
+@pytest.fixture(scope="module")
+def uniform_1m(oracle):
+    x, q = W.uniform(1_000_000, 2)
+    tgt = np.random.default_rng(2).choice(len(q), 10_000, replace=False)
+    rp, rf = oracle.direct(x, q, targets=tgt)
+    return x, q, tgt, rp, rf
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 2e-6), ("mixed", 3e-6)])
+def test_1m_uniform_subset_vs_direct(aran, uniform_1m, precision, tol):
+    """configs[1] size: N=1M uniform, p=12, leaf 64; 10,000 targets against
+    the FP64 direct sum."""
+    x, q, tgt, rp, rf = uniform_1m
+    with aran.Solver3d(maxbox=64, order=12, field=True, precision=precision) as s:
+        pot, fld = s.solve(x, q)
+    assert rel_l2(pot[tgt], rp) < tol
+    assert rel_l2(fld[tgt], rf) < tol
