@@ -30,7 +30,7 @@ EXPORTS = (
     "aran_gpu_solver3d_get_stats", "aran_gpu_solver3d_tree_info",
     "aran_gpu_solver3d_tree_lists", "aran_gpu_solver3d_expansions",
     "aran_gpu_solver3d_timings", "aran_gpu_solver3d_launches", "aran_gpu_last_error",
-    "aran_gpu_version",
+    "aran_gpu_version", "aran_gpu_p2p_direct_noalloc",
 )
 
 
@@ -83,6 +83,8 @@ def load(build_if_missing: bool = True):
     L.aran_gpu_solver3d_timings.restype = C.c_int
     L.aran_gpu_solver3d_launches.argtypes = [vp]
     L.aran_gpu_solver3d_launches.restype = C.c_int64
+    L.aran_gpu_p2p_direct_noalloc.argtypes = [C.c_int64, vp, vp, vp, vp]
+    L.aran_gpu_p2p_direct_noalloc.restype = C.c_int
     L.aran_gpu_last_error.restype = C.c_char_p
     L.aran_gpu_version.restype = C.c_char_p
     _lib = L
@@ -209,6 +211,21 @@ class Solver3d:
 
     def launches(self) -> int:
         return int(load().aran_gpu_solver3d_launches(self._h))
+
+
+NOALLOC_MAX = 131072
+
+
+def p2p_direct_noalloc(n: int, xyz_ptr: int, q_ptr: int, pot_ptr: int | None,
+                       field_ptr: int | None = None) -> None:
+    """Every-pair Newton potential/field of n <= 131072 particles from device
+    pointers, without any device allocation (scratch lives in a static
+    device array of the library).  For callers that may not allocate device
+    memory during a call; calls that overlap on the GPU race on that array."""
+    _check(load().aran_gpu_p2p_direct_noalloc(
+        int(n), C.c_void_p(xyz_ptr), C.c_void_p(q_ptr),
+        C.c_void_p(pot_ptr) if pot_ptr else None,
+        C.c_void_p(field_ptr) if field_ptr else None))
 
 
 def version() -> str:

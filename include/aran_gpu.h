@@ -110,6 +110,19 @@ int aran_gpu_solver3d_timings (AranGpuSolver3d *s, double ms[16]);
 /* Number of GPU kernel launches issued by the last solve. */
 int64_t aran_gpu_solver3d_launches (AranGpuSolver3d *s);
 
+/* Allocation-free Newton near field: every pair of n <= 131072 particles
+ * (potential, and field when d_field is not NULL, with the same rules as the
+ * solver's single-leaf P2P), FP64, device pointers, AoS xyz.  No counterpart
+ * in the reference: it exists for callers that may not allocate device
+ * memory during a call.  Its scratch is a static 4 MiB device array held on
+ * every GPU that loads the library until exit; the first call on a device
+ * looks up that array's address and should precede any stream capture; calls
+ * share the array, so calls that overlap on the GPU race.  Returns
+ * ARAN_ERR_INVALID for n outside [1, 131072]. */
+int aran_gpu_p2p_direct_noalloc (int64_t n, const double *d_xyz,
+                                 const double *d_q, double *d_pot,
+                                 double *d_field);
+
 /* Last error message of the calling thread. */
 const char *aran_gpu_last_error (void);
 
