@@ -73,11 +73,30 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mb, uint32_t parity) {
 }
 
 struct M2LOffsets {
-  int ef, ei, ph, rp, stride;  // in T units; ef/ei interleaved (E, O) pairs
+  int ef, ei, ph, rp, stride;  // in T units; ef/ei: (E, O) pairs, column-major blocks
 };
 
-template <typename T, int NBUF>
-__global__ void __launch_bounds__(256) k_m2l_sibling(
+__device__ __forceinline__ void mbar_arrive(uint64_t *mb) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mb)) : "memory");
+}
+
+// (l, m) of the k-th coefficient in m-major order (m = 0: l = 0..p, m = 1:
+// l = 1..p, ...): the vertical stage walks coefficients in this order so the
+// 32 lanes of a round share m and hence their trip count
+__device__ __forceinline__ void mmajor_lm(int k, int p, int &l, int &m) {
+  m = 0;
+  while (k > p - m) {
+    k -= p + 1 - m;
+    ++m;
+  }
+  l = m + k;
+}
+
+constexpr int kSibWarps = 8;   // consumers: one per child of the parent
+constexpr int kMaxRounds = ((kMaxOrder + 1) * (kMaxOrder + 2) / 2 + 31) / 32;
+
+template <typename T, int NST, int R>
+__global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) k_m2l_sibling(
     int nparents, const int *__restrict__ parents, const int *__restrict__ child,
     const int *__restrict__ begin, const int *__restrict__ end, const int *__restrict__ col,
     const int *__restrict__ ncol, const int *__restrict__ ijk, const uint8_t *__restrict__ depth,
@@ -87,35 +106,54 @@ __global__ void __launch_bounds__(256) k_m2l_sibling(
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int nm = tri(p), nl = tri(p + 1);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  // shared layout: tables | mbarriers | vt | warp buffers | grid | mask | active | lm
+  // shared layout: NST tables | full[NST] | empty[NST] | vertical factors
+  // (m-major) | per-warp buffers | 6x6x6 source grid | offset mask | active list
   size_t off = 0;
   T *tab = reinterpret_cast<T *>(smem_raw);
-  off += (size_t)NBUF * D.stride * sizeof(T);
+  off += (size_t)NST * D.stride * sizeof(T);
   off = (off + 15) & ~(size_t)15;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem_raw + off);
-  off += 2 * sizeof(uint64_t);
-  T *vt = reinterpret_cast<T *>(smem_raw + off);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + off);
+  uint64_t *empty = full + NST;
+  off += 2 * NST * sizeof(uint64_t);
+  T *vtm = reinterpret_cast<T *>(smem_raw + off);
   off += (size_t)nl * p * sizeof(T);
   off = (off + 15) & ~(size_t)15;
   cplx<T> *wbuf = reinterpret_cast<cplx<T> *>(smem_raw + off);
-  off += (size_t)8 * (2 * nm + nl) * sizeof(cplx<T>);
+  off += (size_t)kSibWarps * (nm + nl) * sizeof(cplx<T>);
   int *grid = reinterpret_cast<int *>(smem_raw + off);
   off += 216 * sizeof(int);
   unsigned *mask = reinterpret_cast<unsigned *>(smem_raw + off);
   off += 10 * sizeof(unsigned);
   uint16_t *active = reinterpret_cast<uint16_t *>(smem_raw + off);
   off += 320 * sizeof(uint16_t);
+  uint8_t *lm = smem_raw + off;           // (l, m) of coefficient c (tri order)
+  off += 2 * nl;
+  uint8_t *vmap = smem_raw + off;         // (l, m) of m-major slot k
   __shared__ int s_nact;
 
   const int P = parents[blockIdx.x];
   const int c0 = child[P];
-  // source grid: children of P's internal colleagues, 6x6x6 cells
   for (int i = threadIdx.x; i < 216; i += blockDim.x) grid[i] = -1;
   if (threadIdx.x < 10) mask[threadIdx.x] = 0u;
-  for (int i = threadIdx.x; i < nl * p; i += blockDim.x) vt[i] = vt_g[i];
+  // vertical factors, m-major slot k: vtm[n * nl + k]
+  for (int i = threadIdx.x; i < nl * p; i += blockDim.x) {
+    int k = i % nl, n = i / nl, l, m;
+    mmajor_lm(k, p, l, m);
+    vtm[i] = vt_g[tri(l, m) * p + n];
+  }
+  for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+    int l, m;
+    mmajor_lm(k, p, l, m);
+    vmap[2 * k] = (uint8_t)l;
+    vmap[2 * k + 1] = (uint8_t)m;
+    lm[2 * k] = lm_g[2 * k];
+    lm[2 * k + 1] = lm_g[2 * k + 1];
+  }
   if (threadIdx.x == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
+    for (int b = 0; b < NST; ++b) {
+      mbar_init(&full[b], 1);
+      mbar_init(&empty[b], kSibWarps);
+    }
     fence_mbar_init();
   }
   __syncthreads();
@@ -134,9 +172,8 @@ __global__ void __launch_bounds__(256) k_m2l_sibling(
     grid[gx + 6 * (gy + 6 * gz)] = s;
   }
   __syncthreads();
-  // my target (warp-uniform)
-  const int t = c0 + w;
-  const bool tvalid = end[t] > begin[t];
+  const int t = c0 + (w < kSibWarps ? w : 0);
+  const bool tvalid = w < kSibWarps && end[t] > begin[t];
   const int tx = 2 + (w & 1), ty = 2 + ((w >> 1) & 1), tz = 2 + ((w >> 2) & 1);
   auto source_of = [&](int di) -> int {
     int cx = tx - c_dir_vec[3 * di], cy = ty - c_dir_vec[3 * di + 1], cz = tz - c_dir_vec[3 * di + 2];
@@ -164,110 +201,181 @@ __global__ void __launch_bounds__(256) k_m2l_sibling(
   const int nact = s_nact;
   const uint32_t tbytes = (uint32_t)(D.stride * sizeof(T));
 
-  // per-lane output coefficients
-  constexpr int KMAX = ((kMaxOrder + 1) * (kMaxOrder + 2) / 2 + 31) / 32;
-  cplx<T> acc[KMAX];
-#pragma unroll
-  for (int k = 0; k < KMAX; ++k) acc[k] = cmake<T>(0, 0);
-  cplx<T> *src = wbuf + (size_t)w * (2 * nm + nl);
-  cplx<T> *rot = src + nm;
-  cplx<T> *tr = rot + nm;
-
-  bool ok = true;
-  if (threadIdx.x == 0 && nact > 0) {
-    mbar_expect_tx(&mbar[0], tbytes);
-    bulk_g2s(tab, dirs + (size_t)c_dir_codes[active[0]] * D.stride, tbytes, &mbar[0]);
+  if (w == kSibWarps) {
+    // producer warp: stream the offset tables through the NST-slot ring
+    if (lane == 0)
+      for (int i = 0; i < nact; ++i) {
+        const int b = i % NST;
+        if (i >= NST && !mbar_wait(&empty[b], ((i / NST) - 1) & 1)) {
+          atomicExch(err, 1);
+          break;
+        }
+        mbar_expect_tx(&full[b], tbytes);
+        bulk_g2s(tab + (size_t)b * D.stride, dirs + (size_t)c_dir_codes[active[i]] * D.stride,
+                 tbytes, &full[b]);
+      }
+    return;
   }
+
+  // consumer warp w <-> target child w; its local lives in registers
+  cplx<T> acc[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) acc[r] = cmake<T>(0, 0);
+  // src (phased multipole) and tr (translated, m-major slots) share region A
+  cplx<T> *src = wbuf + (size_t)w * (nm + nl);
+  cplx<T> *tr = src;
+  cplx<T> *rot = src + nl;
+  // the next pair's multipole is fetched one offset ahead into registers
+  cplx<T> pre[R];
+  int next_i = 0, next_s = -1;
+  auto find_next = [&](int from) {
+    next_s = -1;
+    for (next_i = from; next_i < nact; ++next_i) {
+      next_s = tvalid ? source_of(active[next_i]) : -1;
+      if (next_s >= 0) break;
+    }
+  };
+  auto prefetch = [&]() {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      int c = lane + 32 * r;
+      pre[r] = (next_s >= 0 && c < nm) ? mult[(size_t)next_s * nm + c] : cmake<T>(0, 0);
+    }
+  };
+  find_next(0);
+  prefetch();
+
   for (int i = 0; i < nact; ++i) {
-    const int b = NBUF == 2 ? (i & 1) : 0;
-    const uint32_t parity = NBUF == 2 ? ((i >> 1) & 1) : (i & 1);
-    if (NBUF == 2 && threadIdx.x == 0 && i + 1 < nact) {
-      mbar_expect_tx(&mbar[b ^ 1], tbytes);
-      bulk_g2s(tab + (size_t)(b ^ 1) * D.stride,
-               dirs + (size_t)c_dir_codes[active[i + 1]] * D.stride, tbytes, &mbar[b ^ 1]);
-    }
-    if (!mbar_wait(&mbar[b], parity)) {
-      ok = false;
+    const int b = i % NST;
+    if (!mbar_wait(&full[b], (i / NST) & 1)) {
       atomicExch(err, 1);
+      break;
     }
-    if (__syncthreads_or(!ok)) {
-      // a table never arrived: wait (bounded) for the other copy in flight, then stop
-      if (NBUF == 2 && threadIdx.x == 0 && i + 1 < nact) mbar_wait(&mbar[b ^ 1], ((i + 1) >> 1) & 1);
-      __syncthreads();
-      return;
-    }
-    const T *tb = tab + (size_t)b * D.stride;
-    const int s = tvalid ? source_of(active[i]) : -1;
+    const int s = (i == next_i) ? next_s : -1;
     if (s >= 0) {
+      cplx<T> cur[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) cur[r] = pre[r];
+      find_next(i + 1);
+      prefetch();
+      const T *tb = tab + (size_t)b * D.stride;
       const T *ph = tb + D.ph;
       const T *EOf = tb + D.ef;
       const T *EOi = tb + D.ei;
       const T *rp = tb + D.rp;
-      for (int c = lane; c < nm; c += 32) {
-        cplx<T> v = mult[(size_t)s * nm + c];
-        int m = lm_g[2 * c + 1];
-        T cr = ph[2 * m], ci = ph[2 * m + 1];
-        src[c] = cmake<T>(v.re * cr - v.im * ci, v.re * ci + v.im * cr);
-      }
-      __syncwarp();
-      for (int c = lane; c < nm; c += 32) {
-        int l = lm_g[2 * c], mp = lm_g[2 * c + 1];
-        const T *row = EOf + 2 * (sq_off(l) + mp * (l + 1));
-        const cplx<T> *sv = src + tri(l);
-        T re = 0, im = 0;
-        for (int m = 0; m <= l; ++m) {
-          cplx<T> x = sv[m];
-          re += row[2 * m] * x.re;
-          im += row[2 * m + 1] * x.im;
-        }
-        rot[c] = cmake<T>(re, im);
-      }
-      __syncwarp();
-      for (int c = lane; c < nl; c += 32) {
-        int l = lm_g[2 * c], m = lm_g[2 * c + 1];
-        const T *vrow = vt + c * p;
-        T re = 0, im = 0;
-        for (int n = m; n < p; ++n) {
-          T f = vrow[n] * rp[l + n + 1];
-          cplx<T> r = rot[tri(n, m)];
-          re += f * r.re;
-          im += f * r.im;
-        }
-        tr[c] = cmake<T>(re, im);
-      }
-      __syncwarp();
+      // z-phase of the source multipole: e^{i m phi}
 #pragma unroll
-      for (int k = 0; k < KMAX; ++k) {
-        int c = lane + 32 * k;
-        if (c < nl) {
-          int l = lm_g[2 * c], mp = lm_g[2 * c + 1];
-          const T *row = EOi + 2 * (sq_off(l) + mp * (l + 1));
-          const cplx<T> *sv = tr + tri(l);
-          T re = 0, im = 0;
-          for (int m = 0; m <= l; ++m) {
-            cplx<T> x = sv[m];
-            re += row[2 * m] * x.re;
-            im += row[2 * m + 1] * x.im;
-          }
-          T cr = ph[2 * mp], ci = -ph[2 * mp + 1];
-          acc[k].re += re * cr - im * ci;
-          acc[k].im += re * ci + im * cr;
+      for (int r = 0; r < R; ++r) {
+        int c = lane + 32 * r;
+        if (c < nm) {
+          cplx<T> v = cur[r];
+          const int m = lm[2 * c + 1];
+          T cr = ph[2 * m], ci = ph[2 * m + 1];
+          src[c] = cmake<T>(v.re * cr - v.im * ci, v.re * ci + v.im * cr);
         }
       }
       __syncwarp();
+      // rotation to the z axis (degrees < p)
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        int c = lane + 32 * r;
+        if (c < nm) {
+          const int l = lm[2 * c], mp = lm[2 * c + 1];
+          const T *col0 = EOf + 2 * (sq_off(l) + mp);
+          const cplx<T> *sv = src + tri(l);
+          T re0 = 0, im0 = 0, re1 = 0, im1 = 0;
+          int m = 0;
+          for (; m + 1 <= l; m += 2) {
+            cplx<T> x0 = sv[m], x1 = sv[m + 1];
+            const T *e0 = col0 + 2 * m * (l + 1);
+            const T *e1 = e0 + 2 * (l + 1);
+            re0 += e0[0] * x0.re;
+            im0 += e0[1] * x0.im;
+            re1 += e1[0] * x1.re;
+            im1 += e1[1] * x1.im;
+          }
+          if (m <= l) {
+            cplx<T> x0 = sv[m];
+            const T *e0 = col0 + 2 * m * (l + 1);
+            re0 += e0[0] * x0.re;
+            im0 += e0[1] * x0.im;
+          }
+          rot[c] = cmake<T>(re0 + re1, im0 + im1);
+        }
+      }
+      __syncwarp();
+      // translation along z (m-major lanes)
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        int k = lane + 32 * r;
+        if (k < nl) {
+          const int l = vmap[2 * k], m = vmap[2 * k + 1];
+          const T *vcol = vtm + k;
+          const cplx<T> *rv = rot;
+          T re0 = 0, im0 = 0, re1 = 0, im1 = 0;
+          int n = m;
+          for (; n + 1 < p; n += 2) {
+            T f0 = vcol[n * nl] * rp[l + n + 1];
+            T f1 = vcol[(n + 1) * nl] * rp[l + n + 2];
+            cplx<T> a0 = rv[tri(n, m)], a1 = rv[tri(n + 1, m)];
+            re0 += f0 * a0.re;
+            im0 += f0 * a0.im;
+            re1 += f1 * a1.re;
+            im1 += f1 * a1.im;
+          }
+          if (n < p) {
+            T f0 = vcol[n * nl] * rp[l + n + 1];
+            cplx<T> a0 = rv[tri(n, m)];
+            re0 += f0 * a0.re;
+            im0 += f0 * a0.im;
+          }
+          tr[k] = cmake<T>(re0 + re1, im0 + im1);
+        }
+      }
+      __syncwarp();
+      // rotation back (degrees <= p), conjugate z-phase, accumulate
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        int c = lane + 32 * r;
+        if (c < nl) {
+          const int l = lm[2 * c], mp = lm[2 * c + 1];
+          const T *col0 = EOi + 2 * (sq_off(l) + mp);
+          // slot of (l, m) in m-major order: m(p+1) - m(m-1)/2 + (l - m)
+          T re0 = 0, im0 = 0, re1 = 0, im1 = 0;
+          int m = 0, slot = l;
+          for (; m + 1 <= l; m += 2) {
+            const int slot1 = slot + p - m;  // (l, m+1)
+            cplx<T> x0 = tr[slot], x1 = tr[slot1];
+            const T *e0 = col0 + 2 * m * (l + 1);
+            const T *e1 = e0 + 2 * (l + 1);
+            re0 += e0[0] * x0.re;
+            im0 += e0[1] * x0.im;
+            re1 += e1[0] * x1.re;
+            im1 += e1[1] * x1.im;
+            slot = slot1 + p - m - 1;        // (l, m+2)
+          }
+          if (m <= l) {
+            cplx<T> x0 = tr[slot];
+            const T *e0 = col0 + 2 * m * (l + 1);
+            re0 += e0[0] * x0.re;
+            im0 += e0[1] * x0.im;
+          }
+          T re = re0 + re1, im = im0 + im1;
+          T cr = ph[2 * mp], ci = -ph[2 * mp + 1];
+          acc[r].re += re * cr - im * ci;
+          acc[r].im += re * ci + im * cr;
+        }
+      }
     }
-    __syncthreads();  // everyone is done with buffer b before it is refilled
-    if (NBUF == 1 && threadIdx.x == 0 && i + 1 < nact) {
-      mbar_expect_tx(&mbar[0], tbytes);
-      bulk_g2s(tab, dirs + (size_t)c_dir_codes[active[i + 1]] * D.stride, tbytes, &mbar[0]);
-    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[b]);
   }
   if (tvalid && nact > 0) {
     const T ih = (T)(ldexp(1.0, depth[t]) / scale_e);
 #pragma unroll
-    for (int k = 0; k < KMAX; ++k) {
-      int c = lane + 32 * k;
-      if (c < nl) loc[(size_t)t * nl + c] = cmake<T>(acc[k].re * ih, acc[k].im * ih);
+    for (int r = 0; r < R; ++r) {
+      int c = lane + 32 * r;
+      if (c < nl) loc[(size_t)t * nl + c] = cmake<T>(acc[r].re * ih, acc[r].im * ih);
     }
   }
 }
@@ -294,17 +402,35 @@ void upload_codes(int device) {
   if (device >= 0 && device < 64) g_codes_ready[device] = true;
 }
 
-template <typename T, int NBUF>
+template <typename T, int NST>
 size_t m2l_smem(int p, int stride) {
   int nm = tri(p), nl = tri(p + 1);
-  size_t off = (size_t)NBUF * stride * sizeof(T);
+  size_t off = (size_t)NST * stride * sizeof(T);
   off = (off + 15) & ~(size_t)15;
-  off += 2 * sizeof(uint64_t);
+  off += 2 * NST * sizeof(uint64_t);
   off += (size_t)nl * p * sizeof(T);
   off = (off + 15) & ~(size_t)15;
-  off += (size_t)8 * (2 * nm + nl) * sizeof(cplx<T>);
-  off += 216 * sizeof(int) + 10 * sizeof(unsigned) + 320 * sizeof(uint16_t);
+  off += (size_t)kSibWarps * (nm + nl) * sizeof(cplx<T>);
+  off += 216 * sizeof(int) + 10 * sizeof(unsigned) + 320 * sizeof(uint16_t) + 4 * nl;
   return off + 64;
+}
+
+template <typename T, int NST, int R>
+bool try_launch(AranGpuSolver3d *s, OpTables<T> &tb, const M2LOffsets &D, const cplx<T> *mult,
+                cplx<T> *loc, cudaStream_t st, int dev_smem) {
+  DevTree &t = s->tree;
+  const int p = s->cfg.order;
+  size_t sm = m2l_smem<T, NST>(p, D.stride);
+  if ((int)sm > dev_smem) return false;
+  ACHECK(cudaFuncSetAttribute(k_m2l_sibling<T, NST, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sm));
+  k_m2l_sibling<T, NST, R><<<t.n_parents, 32 * (kSibWarps + 1), sm, st>>>(
+      t.n_parents, t.parents.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
+      t.ijk.ptr, t.depth.ptr, p, tb.dir_m2l.ptr, D, tb.vt.ptr, tb.lm.ptr, s->scale_e, mult, loc,
+      s->err_dev.ptr);
+  ACHECK(cudaGetLastError());
+  s->launches++;
+  return true;
 }
 
 template <typename T>
@@ -322,25 +448,19 @@ void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const cplx<T> *mult, cplx<T> 
   D.stride = dir_offset(p, 0, 6);
   int dev_smem = 0;
   ACHECK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
-  size_t sm2 = m2l_smem<T, 2>(p, D.stride);
-  size_t sm1 = m2l_smem<T, 1>(p, D.stride);
-  ACHECK(cudaMemsetAsync(s->err_dev.ptr, 0, sizeof(int), st));
-  if ((int)sm2 <= dev_smem) {
-    ACHECK(cudaFuncSetAttribute(k_m2l_sibling<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
-    k_m2l_sibling<T, 2><<<t.n_parents, 256, sm2, st>>>(
-        t.n_parents, t.parents.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
-        t.ijk.ptr, t.depth.ptr, p, tb.dir_m2l.ptr, D, tb.vt.ptr, tb.lm.ptr, s->scale_e, mult, loc,
-        s->err_dev.ptr);
+  // R = rounds of 32 lanes over the tri(p+1) local coefficients
+  const int nl = tri(p + 1);
+  if (nl <= 96) {
+    if (try_launch<T, 3, 3>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 3>(s, tb, D, mult, loc, st, dev_smem)) return;
+  } else if (nl <= 160) {
+    if (try_launch<T, 3, 5>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 5>(s, tb, D, mult, loc, st, dev_smem)) return;
   } else {
-    if ((int)sm1 > dev_smem) throw CudaError{cudaErrorInvalidConfiguration, "M2L shared memory exceeds the device limit"};
-    ACHECK(cudaFuncSetAttribute(k_m2l_sibling<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
-    k_m2l_sibling<T, 1><<<t.n_parents, 256, sm1, st>>>(
-        t.n_parents, t.parents.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
-        t.ijk.ptr, t.depth.ptr, p, tb.dir_m2l.ptr, D, tb.vt.ptr, tb.lm.ptr, s->scale_e, mult, loc,
-        s->err_dev.ptr);
+    if (try_launch<T, 3, kMaxRounds>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, kMaxRounds>(s, tb, D, mult, loc, st, dev_smem)) return;
   }
-  ACHECK(cudaGetLastError());
-  s->launches++;
+  throw CudaError{cudaErrorInvalidConfiguration, "M2L shared memory exceeds the device limit"};
 }
 
 }  // namespace

@@ -145,6 +145,7 @@ int aran_gpu_solver3d_solve(AranGpuSolver3d *s, int64_t n, const double *xyz, co
     const double *dx = xyz, *dq = q;
     double *dpot = pot, *dfld = field;
     ACHECK(cudaEventRecord(s->ev[2 * Stage::TOTAL], st));
+    ACHECK(cudaMemsetAsync(s->err_dev.ptr, 0, sizeof(int), st));
     ACHECK(cudaEventRecord(s->ev[2 * Stage::H2D], st));
     if (mem == ARAN_MEM_HOST) {
       s->io_xyz.reserve(3 * n);

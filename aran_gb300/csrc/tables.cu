@@ -25,7 +25,7 @@ struct DirLayout {
 
 __host__ __device__ DirLayout dir_layout(int p, int kind) {
   DirLayout d;
-  if (kind == 0) {  // M2L: (E, O) interleaved blocks
+  if (kind == 0) {  // M2L: (E, O) interleaved, column-major blocks
     d.Lf = p; d.Li = p + 1; d.nrp = 2 * p + 2;
     d.ef = 0;
     d.of = -1;
@@ -137,20 +137,26 @@ __global__ void k_dir_tables(int p, int kind, int ndir, double ex, double ey, do
   double *eo = wm + wig_size(Lmax);
   gen_wigner_d(Lmax, theta, w);
   gen_wigner_d(Lmax, -theta, wm);
+  // M2L blocks go column-major ([l][m][m'], (E, O) interleaved) so the lanes
+  // of a warp, one output order m' each, read consecutive words
+  auto put_cm = [&](int Lb, int base) {
+    for (int l = 0; l < Lb; ++l)
+      for (int mp = 0; mp <= l; ++mp)
+        for (int m = 0; m <= l; ++m) {
+          int src = sq_off(l) + mp * (l + 1) + m;
+          int dst = sq_off(l) + m * (l + 1) + mp;
+          o[base + 2 * dst] = (T)eo[src];
+          o[base + 2 * dst + 1] = (T)eo[sq_size(Lb) + src];
+        }
+  };
   wigner_to_eo(L.Lf, w, eo, eo + sq_size(L.Lf));
   if (kind == 0)
-    for (int i = 0; i < sq_size(L.Lf); ++i) {
-      o[L.ef + 2 * i] = (T)eo[i];
-      o[L.ef + 2 * i + 1] = (T)eo[sq_size(L.Lf) + i];
-    }
+    put_cm(L.Lf, L.ef);
   else
     for (int i = 0; i < 2 * sq_size(L.Lf); ++i) o[L.ef + i] = (T)eo[i];
   wigner_to_eo(L.Li, wm, eo, eo + sq_size(L.Li));
   if (kind == 0)
-    for (int i = 0; i < sq_size(L.Li); ++i) {
-      o[L.ei + 2 * i] = (T)eo[i];
-      o[L.ei + 2 * i + 1] = (T)eo[sq_size(L.Li) + i];
-    }
+    put_cm(L.Li, L.ei);
   else
     for (int i = 0; i < 2 * sq_size(L.Li); ++i) o[L.ei + i] = (T)eo[i];
   for (int m = 0; m <= p; ++m) {
