@@ -113,6 +113,22 @@ struct OpTables {
   DBuf<uint8_t> lm; // (l,m) of coefficient index, 2*tri(p+1)
 };
 
+// tables of the kkylin flavour (kkylin.cu): alpha/beta and, per direction
+// (343 M2L offsets, 8 M2M and 8 L2L octants), r, cos/sin theta, cos/sin phi
+// and the harmonics of the direction
+template <typename T>
+struct KkTables {
+  int p = -1;
+  DBuf<T> alpha, beta, dirs[3];
+  int stride[3] = {0, 0, 0};
+  void release() {
+    alpha.release();
+    beta.release();
+    for (auto &d : dirs) d.release();
+    p = -1;
+  }
+};
+
 struct Stage {
   enum { TOTAL, SORT, TREE, LISTS, P2M, M2M, M2L, L2L, L2P, P2P, H2D, D2H, NSTAGE };
 };
@@ -128,6 +144,8 @@ struct AranGpuSolver3d {
   double scale_e = 1.;   // 2^E >= root extent
   aran::OpTables<double> t64;
   aran::OpTables<float> t32;
+  aran::KkTables<double> kk64;
+  aran::KkTables<float> kk32;
   aran::DevTree tree;
   // particles (sorted)
   aran::DBuf<uint64_t> keys_in, keys_out;
@@ -158,6 +176,9 @@ void build_lists(AranGpuSolver3d *s);
 void build_tables(AranGpuSolver3d *s);
 // passes.cu
 void run_passes(AranGpuSolver3d *s);
+// kkylin.cu: stage 0 = M2M, 1 = M2L, 2 = L2L
+void build_kkylin_tables(AranGpuSolver3d *s);
+void kkylin_pass(AranGpuSolver3d *s, int stage);
 // m2l.cu
 void launch_m2l(AranGpuSolver3d *s, cudaStream_t st);
 // p2p.cu

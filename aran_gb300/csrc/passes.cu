@@ -459,7 +459,9 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   ACHECK(cudaEventRecord(s->ev[2 * Stage::P2M + 1], st));
   // M2M, deepest level first
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2M], st));
-  {
+  const bool kk = s->cfg.flavour == ARAN_FLAVOUR_KKYLIN;
+  if (kk) kkylin_pass(s, 0);
+  else {
     DirOffsets D = offsets<T>(p, 1);
     const int WPB = 4;
     size_t sm = ((2 * nl + 15) & ~15) + (size_t)WPB * 2 * nm * sizeof(cplx<T>) + 64;
@@ -476,11 +478,13 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2M + 1], st));
   // M2L over every node of depth >= 2
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L], st));
-  launch_m2l(s, st);
+  if (kk) kkylin_pass(s, 1);
+  else launch_m2l(s, st);
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L + 1], st));
   // L2L, from depth 3 (depth 0-1 locals are zero: no far pairs above depth 2)
   ACHECK(cudaEventRecord(s->ev[2 * Stage::L2L], st));
-  {
+  if (kk) kkylin_pass(s, 2);
+  else {
     DirOffsets D = offsets<T>(p, 2);
     const int WPB = 4;
     size_t sm = ((2 * nl + 15) & ~15) + (size_t)WPB * 2 * nl * sizeof(cplx<T>) + 64;

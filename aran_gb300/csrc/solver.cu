@@ -41,8 +41,11 @@ int check_config(const AranGpuConfig3d *c) {
   if (c->maxbox < 1) return fail(ARAN_ERR_INVALID, "maxbox must be >= 1");
   if (c->order < 1 || c->order > kMaxOrder)
     return fail(ARAN_ERR_INVALID, "order must be in [1, " + std::to_string(kMaxOrder) + "]");
-  if (c->flavour != ARAN_FLAVOUR_ROTATE)
-    return fail(ARAN_ERR_UNSUPPORTED, "only the rotate flavour is available in this build");
+  if (c->flavour == ARAN_FLAVOUR_NORMAL)
+    return fail(ARAN_ERR_UNSUPPORTED, "the normal O(p^4) flavour is not available on the GPU; "
+                                      "use ARAN_FLAVOUR_ROTATE or ARAN_FLAVOUR_KKYLIN");
+  if (c->flavour != ARAN_FLAVOUR_ROTATE && c->flavour != ARAN_FLAVOUR_KKYLIN)
+    return fail(ARAN_ERR_INVALID, "unknown flavour");
   if (c->precision != ARAN_PRECISION_FP64 && c->precision != ARAN_PRECISION_MIXED)
     return fail(ARAN_ERR_INVALID, "unknown precision");
   if (c->max_depth < 0 || c->max_depth > kKeyBits)
@@ -82,6 +85,7 @@ int aran_gpu_solver3d_create(const AranGpuConfig3d *cfg, AranGpuSolver3d **out) 
     s->scale_e = std::ldexp(1.0, (int)std::ceil(std::log2(ext)));
     if (s->scale_e < ext) s->scale_e *= 2;
     build_tables(s);
+    if (cfg->flavour == ARAN_FLAVOUR_KKYLIN) build_kkylin_tables(s);
     s->err_dev.reserve(4);
     ACHECK(cudaMemset(s->err_dev.ptr, 0, sizeof(int)));
   } catch (const CudaError &ce) {
@@ -123,6 +127,8 @@ void aran_gpu_solver3d_destroy(AranGpuSolver3d *s) {
   s->scan_tmp.release(); s->stats_dev.release(); s->err_dev.release();
   t.leaf_be.release(); t.leaf_chi.release(); t.leaf_clo.release(); t.big_items.release();
   t.parents.release();
+  s->kk64.release();
+  s->kk32.release();
   for (auto &ev : s->ev)
     if (ev) cudaEventDestroy(ev);
   if (s->s0) cudaStreamDestroy(s->s0);

@@ -158,6 +158,28 @@ def test_error_codes(aran):
     assert ei.value.code == -6
 
 
+KK_CASES = [
+    ("uniform", lambda n: W.uniform(n, 41), 6000, 20, 8, (0, 0, 0), (1, 1, 1)),
+    ("plummer", lambda n: W.plummer(n, 42), 15000, 32, 12, (-1, -1, -1), (1, 1, 1)),
+    ("box-aspect", lambda n: W.uniform(n, 43), 6000, 16, 6, (0, 0, 0), (1.0, 1.5, 3.0)),
+]
+
+
+@pytest.mark.parametrize("case", KK_CASES, ids=[c[0] for c in KK_CASES])
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_kkylin_matches_oracle(aran, oracle, case, precision, tol):
+    """kkylin flavour (aran_development3d_*_kkylin) against the oracle's kkylin solve."""
+    name, gen, n, maxbox, p, lb, ub = case
+    x, q = gen(n)
+    with aran.Solver3d(lb, ub, maxbox=maxbox, order=p, flavour="kkylin", field=True,
+                       precision=precision) as s:
+        pot, fld = s.solve(x, q)
+    opot, _ = oracle.solve(x, q, order=p, maxbox=maxbox, flavour="kkylin", field=False, lb=lb, ub=ub)
+    ofld, _ = oracle.solve(x, q, order=p, maxbox=maxbox, flavour="kkylin", field=True, lb=lb, ub=ub)
+    assert rel_l2(pot, opot) < tol
+    assert rel_l2(fld, ofld) < tol
+
+
 def test_linearity_and_permutation(aran):
     """Size-independent properties on 1M particles: the solve is linear in the
     charges and equivariant under a permutation of the input."""
