@@ -30,7 +30,9 @@ EXPORTS = (
     "aran_gpu_solver3d_get_stats", "aran_gpu_solver3d_tree_info",
     "aran_gpu_solver3d_tree_lists", "aran_gpu_solver3d_expansions",
     "aran_gpu_solver3d_timings", "aran_gpu_solver3d_launches", "aran_gpu_last_error",
-    "aran_gpu_version", "aran_gpu_p2p_direct_noalloc",
+    "aran_gpu_version", "aran_gpu_p2p_direct_noalloc", "aran_gpu_footprint_bytes",
+    "aran_gpu_server_create", "aran_gpu_server_submit", "aran_gpu_server_wait",
+    "aran_gpu_server_cancel", "aran_gpu_server_destroy",
 )
 
 
@@ -46,6 +48,16 @@ class Config3d(C.Structure):
     _fields_ = [("lb", C.c_double * 3), ("ub", C.c_double * 3), ("maxbox", C.c_int),
                 ("order", C.c_int), ("flavour", C.c_int), ("field", C.c_int),
                 ("precision", C.c_int), ("max_depth", C.c_int)]
+
+
+class Request3d(C.Structure):
+    _fields_ = [("cfg", Config3d), ("n", C.c_int64), ("xyz", C.c_void_p), ("q", C.c_void_p),
+                ("pot", C.c_void_p), ("field", C.c_void_p)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("submit_s", C.c_double), ("start_s", C.c_double),
+                ("end_s", C.c_double), ("slot", C.c_int), ("footprint_bytes", C.c_int64)]
 
 
 _lib = None
@@ -85,6 +97,18 @@ def load(build_if_missing: bool = True):
     L.aran_gpu_solver3d_launches.restype = C.c_int64
     L.aran_gpu_p2p_direct_noalloc.argtypes = [C.c_int64, vp, vp, vp, vp]
     L.aran_gpu_p2p_direct_noalloc.restype = C.c_int
+    L.aran_gpu_footprint_bytes.argtypes = [C.POINTER(Config3d), C.c_int64]
+    L.aran_gpu_footprint_bytes.restype = C.c_int64
+    L.aran_gpu_server_create.argtypes = [C.c_int, C.c_double, C.POINTER(vp)]
+    L.aran_gpu_server_create.restype = C.c_int
+    L.aran_gpu_server_submit.argtypes = [vp, C.POINTER(Request3d), C.POINTER(C.c_int64)]
+    L.aran_gpu_server_submit.restype = C.c_int
+    L.aran_gpu_server_wait.argtypes = [vp, C.c_int64, C.c_double, C.POINTER(RequestInfo)]
+    L.aran_gpu_server_wait.restype = C.c_int
+    L.aran_gpu_server_cancel.argtypes = [vp, C.c_int64]
+    L.aran_gpu_server_cancel.restype = C.c_int
+    L.aran_gpu_server_destroy.argtypes = [vp]
+    L.aran_gpu_server_destroy.restype = None
     L.aran_gpu_last_error.restype = C.c_char_p
     L.aran_gpu_version.restype = C.c_char_p
     _lib = L
@@ -98,6 +122,85 @@ def _check(rc: int):
 
 def _ptr(a):
     return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def make_config(lbound=(0.0, 0.0, 0.0), ubound=(1.0, 1.0, 1.0), *, maxbox=64, order=12,
+                flavour="rotate", field=True, precision="fp64", max_depth=21) -> Config3d:
+    cfg = Config3d()
+    for k in range(3):
+        cfg.lb[k], cfg.ub[k] = float(lbound[k]), float(ubound[k])
+    cfg.maxbox, cfg.order = int(maxbox), int(order)
+    cfg.flavour = FLAVOURS[flavour] if isinstance(flavour, str) else int(flavour)
+    cfg.field = int(bool(field))
+    cfg.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    cfg.max_depth = int(max_depth)
+    return cfg
+
+
+def footprint_bytes(n: int, **cfg_kw) -> int:
+    """Estimated device memory of one solve (the server's admission unit)."""
+    return int(load().aran_gpu_footprint_bytes(C.byref(make_config(**cfg_kw)), int(n)))
+
+
+class Server:
+    """Request loop for independent solves on one GPU (continuous batching).
+
+    ``nslots`` solves run concurrently (each slot a native worker thread with
+    its own streams and resident solvers); a request starts when a slot is
+    free and its estimated footprint fits ``hbm_budget_bytes`` next to the
+    running ones.  ``submit`` returns a ticket, ``wait`` the outputs and the
+    request's timestamps (seconds since the server started)."""
+
+    def __init__(self, nslots=4, hbm_budget_bytes=150e9):
+        h = C.c_void_p()
+        _check(load().aran_gpu_server_create(int(nslots), float(hbm_budget_bytes), C.byref(h)))
+        self._h = h
+        self._live = {}
+
+    def submit(self, xyz, q, **cfg_kw) -> int:
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        n = len(q)
+        cfg = make_config(**cfg_kw)
+        pot = np.empty(n)
+        fld = np.empty((n, 3)) if cfg.field else None
+        req = Request3d(cfg, n, xyz.ctypes.data, q.ctypes.data, pot.ctypes.data,
+                        fld.ctypes.data if fld is not None else None)
+        t = C.c_int64()
+        _check(load().aran_gpu_server_submit(self._h, C.byref(req), C.byref(t)))
+        self._live[t.value] = (xyz, q, pot, fld)
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = -1.0):
+        info = RequestInfo()
+        rc = load().aran_gpu_server_wait(self._h, int(ticket), float(timeout), C.byref(info))
+        if rc == -5:  # still running
+            raise AranError(rc, load().aran_gpu_last_error().decode())
+        xyz, q, pot, fld = self._live.pop(int(ticket))
+        d = {"status": info.status, "submit_s": info.submit_s, "start_s": info.start_s,
+             "end_s": info.end_s, "slot": info.slot, "footprint_bytes": info.footprint_bytes}
+        _check(rc)
+        return pot, fld, d
+
+    def cancel(self, ticket: int):
+        _check(load().aran_gpu_server_cancel(self._h, int(ticket)))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().aran_gpu_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Solver3d:

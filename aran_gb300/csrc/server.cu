@@ -1,0 +1,286 @@
+// server.cu -- request loop for many independent solves on one GPU.
+//
+// Requests (a configuration plus host arrays) arrive through
+// aran_gpu_server_submit and are admitted as soon as a slot is free and
+// their estimated device footprint fits the HBM budget next to the requests
+// already running.  Each slot is a host worker thread with its own cached
+// solvers (per configuration) and therefore its own CUDA streams, so the
+// kernels of concurrent requests overlap on the device; trees, expansions
+// and tables stay resident in the slot's solvers between requests.  Queueing
+// is first-fit in arrival order: a request that does not fit yet does not
+// block smaller ones behind it.  Completion, status and timestamps (submit,
+// start, end) are kept per ticket for latency statistics.
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <tuple>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace aran {
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Job {
+  int64_t ticket;
+  AranGpuRequest3d req;
+  int64_t footprint;
+  double t_submit = 0, t_start = 0, t_end = 0;
+  int status = 1;  // 1 = pending, 0 = ok, < 0 = error
+  int slot = -1;
+  std::string error;
+};
+
+struct ConfigKey {
+  AranGpuConfig3d c;
+  bool operator<(const ConfigKey &o) const { return std::memcmp(&c, &o.c, sizeof(c)) < 0; }
+};
+
+}  // namespace
+
+int64_t footprint_bytes(const AranGpuConfig3d *c, int64_t n) {
+  const int p = c->order;
+  const int64_t real = c->precision == ARAN_PRECISION_MIXED ? 4 : 8;
+  const int64_t nodes = 16 + (8 * n) / (c->maxbox > 1 ? c->maxbox : 2) + n / 8;
+  int64_t b = 0;
+  b += n * (3 * 8 + 8);            // staged inputs
+  b += n * (4 * 8);                // outputs (pot + field) staged
+  b += n * (4 * 8 + 2 * 8 + 8);    // sorted positions/charges, keys (2x), perm/idx
+  b += n * (4 * real + 4 * 8);     // relative coordinates, accumulators
+  b += nodes * (8 + 12 + 1 + 16 + 24 + 27 * 4 + 4 * 4 + 8);       // node arrays
+  b += nodes * (int64_t)(tri(p) + tri(p + 1)) * 2 * real;          // expansions
+  b += nodes * (189 * 6 + 8) + nodes * 60 * 8;                     // far/near lists
+  return b + (64ll << 20);
+}
+
+}  // namespace aran
+
+struct AranGpuServer {
+  int device = 0;
+  int nslots = 0;
+  int64_t budget = 0;
+  int64_t in_use = 0;
+  bool stopping = false;
+  int64_t next_ticket = 1;
+  aran::Clock::time_point t0;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<int64_t> queue;
+  std::map<int64_t, std::unique_ptr<aran::Job>> jobs;
+  std::vector<std::thread> workers;
+};
+
+namespace aran {
+namespace {
+
+double now_s(AranGpuServer *sv) {
+  return std::chrono::duration<double>(Clock::now() - sv->t0).count();
+}
+
+void worker_main(AranGpuServer *sv, int slot) {
+  cudaSetDevice(sv->device);
+  std::map<ConfigKey, AranGpuSolver3d *> solvers;
+  for (;;) {
+    Job *job = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(sv->mu);
+      for (;;) {
+        if (sv->stopping) break;
+        // first fit in arrival order
+        for (auto it = sv->queue.begin(); it != sv->queue.end(); ++it) {
+          Job *j = sv->jobs[*it].get();
+          if (sv->in_use + j->footprint <= sv->budget) {
+            job = j;
+            sv->queue.erase(it);
+            sv->in_use += j->footprint;
+            break;
+          }
+        }
+        if (job) break;
+        sv->cv_work.wait(lk);
+      }
+      if (!job) break;
+      job->slot = slot;
+      job->t_start = now_s(sv);
+    }
+    // run the solve outside the lock
+    int rc = ARAN_OK;
+    std::string err;
+    ConfigKey key{job->req.cfg};
+    AranGpuSolver3d *s = nullptr;
+    auto f = solvers.find(key);
+    if (f != solvers.end()) s = f->second;
+    else {
+      rc = aran_gpu_solver3d_create(&job->req.cfg, &s);
+      if (rc == ARAN_OK) solvers[key] = s;
+      else err = aran_gpu_last_error();
+    }
+    if (rc == ARAN_OK) {
+      rc = aran_gpu_solver3d_solve(s, job->req.n, job->req.xyz, job->req.q, job->req.pot,
+                                   job->req.field, ARAN_MEM_HOST);
+      if (rc != ARAN_OK) err = aran_gpu_last_error();
+    }
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      job->t_end = now_s(sv);
+      job->status = rc;
+      job->error = err;
+      sv->in_use -= job->footprint;
+    }
+    sv->cv_done.notify_all();
+    sv->cv_work.notify_all();
+  }
+  for (auto &kv : solvers) aran_gpu_solver3d_destroy(kv.second);
+}
+
+}  // namespace
+}  // namespace aran
+
+using namespace aran;
+
+extern "C" {
+
+int64_t aran_gpu_footprint_bytes(const AranGpuConfig3d *cfg, int64_t n) {
+  if (!cfg || n < 1) return -1;
+  return footprint_bytes(cfg, n);
+}
+
+int aran_gpu_server_create(int nslots, double hbm_budget_bytes, AranGpuServer **out) {
+  if (!out) {
+    set_error("out is NULL");
+    return ARAN_ERR_INVALID;
+  }
+  *out = nullptr;
+  if (nslots < 1 || nslots > 64) {
+    set_error("nslots must be in [1, 64]");
+    return ARAN_ERR_INVALID;
+  }
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    set_error(std::string("no CUDA device available: ") + cudaGetErrorString(e));
+    return ARAN_ERR_NO_DEVICE;
+  }
+  AranGpuServer *sv = new AranGpuServer();
+  cudaGetDevice(&sv->device);
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  sv->budget = hbm_budget_bytes > 0 ? (int64_t)hbm_budget_bytes : (int64_t)(0.8 * (double)free_b);
+  sv->nslots = nslots;
+  sv->t0 = Clock::now();
+  for (int i = 0; i < nslots; ++i) sv->workers.emplace_back(worker_main, sv, i);
+  *out = sv;
+  return ARAN_OK;
+}
+
+int aran_gpu_server_submit(AranGpuServer *sv, const AranGpuRequest3d *req, int64_t *ticket) {
+  if (!sv || !req || !ticket) {
+    set_error("NULL argument");
+    return ARAN_ERR_INVALID;
+  }
+  if (req->n < 1 || !req->xyz || !req->q || (!req->pot && !req->field)) {
+    set_error("request needs n >= 1, xyz, q and an output");
+    return ARAN_ERR_INVALID;
+  }
+  int64_t fp = footprint_bytes(&req->cfg, req->n);
+  std::lock_guard<std::mutex> lk(sv->mu);
+  if (fp > sv->budget) {
+    set_error("request footprint " + std::to_string(fp) + " B exceeds the HBM budget " +
+              std::to_string(sv->budget) + " B");
+    return ARAN_ERR_OOM;
+  }
+  auto job = std::make_unique<Job>();
+  job->ticket = sv->next_ticket++;
+  job->req = *req;
+  job->footprint = fp;
+  job->t_submit = now_s(sv);
+  *ticket = job->ticket;
+  sv->queue.push_back(job->ticket);
+  sv->jobs[job->ticket] = std::move(job);
+  sv->cv_work.notify_one();
+  return ARAN_OK;
+}
+
+int aran_gpu_server_wait(AranGpuServer *sv, int64_t ticket, double timeout_s,
+                         AranGpuRequestInfo *info) {
+  if (!sv) {
+    set_error("server is NULL");
+    return ARAN_ERR_INVALID;
+  }
+  std::unique_lock<std::mutex> lk(sv->mu);
+  auto it = sv->jobs.find(ticket);
+  if (it == sv->jobs.end()) {
+    set_error("unknown ticket");
+    return ARAN_ERR_INVALID;
+  }
+  Job *j = it->second.get();
+  auto pred = [&] { return j->status != 1; };
+  if (timeout_s < 0) sv->cv_done.wait(lk, pred);
+  else if (!sv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) {
+    set_error("request still running");
+    return ARAN_ERR_TIMEOUT;
+  }
+  if (info) {
+    info->status = j->status;
+    info->submit_s = j->t_submit;
+    info->start_s = j->t_start;
+    info->end_s = j->t_end;
+    info->slot = j->slot;
+    info->footprint_bytes = j->footprint;
+  }
+  int st = j->status;
+  if (st != ARAN_OK) set_error(j->error);
+  sv->jobs.erase(it);
+  return st;
+}
+
+int aran_gpu_server_cancel(AranGpuServer *sv, int64_t ticket) {
+  if (!sv) {
+    set_error("server is NULL");
+    return ARAN_ERR_INVALID;
+  }
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    for (auto it = sv->queue.begin(); it != sv->queue.end(); ++it)
+      if (*it == ticket) {
+        sv->queue.erase(it);
+        Job *j = sv->jobs[ticket].get();
+        j->status = ARAN_ERR_CANCELLED;
+        j->error = "request cancelled before it started";
+        j->t_start = j->t_end = now_s(sv);
+        sv->cv_done.notify_all();
+        return ARAN_OK;
+      }
+  }
+  set_error("request is not queued (unknown, running or finished)");
+  return ARAN_ERR_INVALID;
+}
+
+void aran_gpu_server_destroy(AranGpuServer *sv) {
+  if (!sv) return;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->stopping = true;
+    // requests that never started are cancelled
+    for (int64_t t : sv->queue) {
+      Job *j = sv->jobs[t].get();
+      j->status = ARAN_ERR_CANCELLED;
+      j->error = "server destroyed before the request started";
+    }
+    sv->queue.clear();
+  }
+  sv->cv_done.notify_all();
+  sv->cv_work.notify_all();
+  for (auto &t : sv->workers) t.join();
+  delete sv;
+}
+
+}  // extern "C"

@@ -120,6 +120,59 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
+# ------------------------------------------------------------------ serving
+def serving_stream(nreq: int, rate: float, seed: int = 5):
+    """Poisson arrivals of 3D potential+field solves: N log-uniform in
+    [1e3, 2e6], requested tolerance 1e-4/1e-6/1e-9 -> p = 6/10/16, half
+    uniform in [0,1]^3, half Plummer in [-1,1]^3."""
+    import numpy as np
+    from aran_gb300 import workloads as W
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    reqs = []
+    for i in range(nreq):
+        n = int(np.exp(rng.uniform(np.log(1e3), np.log(2e6))))
+        p = (6, 10, 16)[int(rng.integers(0, 3))]
+        if rng.uniform() < 0.5:
+            x, q = W.uniform(n, 1000 + i)
+            lb, ub = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)
+        else:
+            x, q = W.plummer(n, 1000 + i)
+            lb, ub = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
+        reqs.append((float(arrivals[i]), x, q, dict(lbound=lb, ubound=ub, maxbox=64, order=p,
+                                                     field=True)))
+    return reqs
+
+
+def run_serving(reqs, precision: str, nslots: int = 4, budget: float = 150e9) -> dict:
+    import numpy as np
+    import aran_gb300 as A
+    with A.Server(nslots=nslots, hbm_budget_bytes=budget) as sv:
+        # one warm request per configuration so table builds stay out of the stream
+        seen = set()
+        for _, x, q, kw in reqs:
+            key = (kw["order"], kw["lbound"])
+            if key not in seen:
+                seen.add(key)
+                sv.wait(sv.submit(x[:2000], q[:2000], precision=precision, **kw))
+        t0 = time.perf_counter()
+        tickets = []
+        for arr, x, q, kw in reqs:
+            dt = arr - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            tickets.append(sv.submit(x, q, precision=precision, **kw))
+        infos = [sv.wait(t)[2] for t in tickets]
+    lat = np.array([i["end_s"] - i["submit_s"] for i in infos])
+    span = max(i["end_s"] for i in infos) - min(i["submit_s"] for i in infos)
+    npart = sum(len(r[2]) for r in reqs)
+    return {"precision": precision, "requests": len(reqs),
+            "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "throughput": npart / span, "unit": UNIT,
+            "mean_queue_ms": float(np.mean([i["start_s"] - i["submit_s"] for i in infos]) * 1e3)}
+
+
 # ------------------------------------------------------------- CPU baseline
 def _cpu_job(args):
     name, n_sample, seed = args
@@ -324,6 +377,15 @@ def run_gpu(args):
                 "d2h_bytes_per_step": n * 8 + n * 3 * 8},
         "gpu_launches": launches,
     }
+    if args.serving_requests > 0:
+        reqs = serving_stream(args.serving_requests, args.serving_rate)
+        line["serving"] = {
+            "stream": (f"{args.serving_requests} Poisson arrivals at {args.serving_rate}/s, N "
+                       "log-uniform [1e3, 2e6], p in {6,10,16}, half uniform / half Plummer, "
+                       "4 slots, 150 GB HBM admission budget"),
+            "mixed": run_serving(reqs, "mixed"),
+            "fp64": run_serving(reqs, "fp64"),
+        }
     if args.cpu_baseline:
         procs = args.cpu_procs or os.cpu_count() or 1
         line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_sample, procs)
@@ -368,6 +430,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=20000)
     ap.add_argument("--cpu-procs", type=int, default=0)
     ap.add_argument("--ref-warmup", type=int, default=0)
+    ap.add_argument("--serving-requests", type=int, default=48)
+    ap.add_argument("--serving-rate", type=float, default=16.0)
     ap.add_argument("--m2l-traffic", type=float, default=None,
                     help="dram bytes per M2L launch from an ncu capture (profiles/)")
     args = ap.parse_args()

@@ -31,6 +31,7 @@ extern "C" {
 #define ARAN_ERR_OOM (-4)          /* device memory exhausted */
 #define ARAN_ERR_TIMEOUT (-5)      /* a bounded device-side wait gave up */
 #define ARAN_ERR_UNSUPPORTED (-6)
+#define ARAN_ERR_CANCELLED (-7)    /* a queued request was cancelled */
 
 /* M2M/M2L/L2L flavours: aran_development3d_{m2l,m2l_kkylin,m2l_rotate}
  * (aran/arandevelopment3d.c:306-313,362-369,423-430) */
@@ -122,6 +123,53 @@ int64_t aran_gpu_solver3d_launches (AranGpuSolver3d *s);
 int aran_gpu_p2p_direct_noalloc (int64_t n, const double *d_xyz,
                                  const double *d_q, double *d_pot,
                                  double *d_field);
+
+/* ---- request loop (continuous batching of independent solves) ---------
+ * No counterpart in the reference (which solves one system per call); it
+ * serves many aran_solver3d_solve-equivalent requests on one GPU. */
+
+typedef struct
+{
+  AranGpuConfig3d cfg;
+  int64_t n;
+  const double *xyz;   /* host, 3n, valid until the request completes */
+  const double *q;     /* host, n */
+  double *pot;         /* host, n (or NULL) */
+  double *field;       /* host, 3n (or NULL) */
+} AranGpuRequest3d;
+
+typedef struct
+{
+  int status;          /* ARAN_OK or the request's error code */
+  double submit_s;     /* seconds since the server was created */
+  double start_s;
+  double end_s;
+  int slot;
+  int64_t footprint_bytes;
+} AranGpuRequestInfo;
+
+typedef struct AranGpuServer AranGpuServer;
+
+/* Estimated device memory of one solve (particles, tree, lists, expansions). */
+int64_t aran_gpu_footprint_bytes (const AranGpuConfig3d *cfg, int64_t n);
+
+/* nslots concurrent solves (host worker threads with their own streams and
+ * resident solvers) under an HBM admission budget (<= 0: 80% of free). */
+int aran_gpu_server_create (int nslots, double hbm_budget_bytes,
+                            AranGpuServer **out);
+/* Queues a request; it starts when a slot is free and its footprint fits the
+ * budget next to the running ones (first fit in arrival order).  A request
+ * larger than the whole budget is refused with ARAN_ERR_OOM. */
+int aran_gpu_server_submit (AranGpuServer *sv, const AranGpuRequest3d *req,
+                            int64_t *ticket);
+/* Waits for a request (timeout_s < 0: forever); returns its status and
+ * fills info.  A ticket can be waited for once. */
+int aran_gpu_server_wait (AranGpuServer *sv, int64_t ticket, double timeout_s,
+                          AranGpuRequestInfo *info);
+/* Cancels a request that has not started (ARAN_ERR_CANCELLED for waiters). */
+int aran_gpu_server_cancel (AranGpuServer *sv, int64_t ticket);
+/* Finishes running requests, cancels queued ones, frees everything. */
+void aran_gpu_server_destroy (AranGpuServer *sv);
 
 /* Last error message of the calling thread. */
 const char *aran_gpu_last_error (void);

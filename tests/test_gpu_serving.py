@@ -1,0 +1,98 @@
+"""The request loop (continuous batching of independent solves).
+
+* every result is the same alone and in the mix: a burst of requests of
+  different sizes, orders, distributions and precisions, served concurrently,
+  matches each request solved alone (rel-L2 1e-10; the only difference is the
+  order of FP64 atomic additions in the chunked near field);
+* admission respects the HBM budget: requests whose footprints do not fit
+  together never run at the same time; a request larger than the budget is
+  refused at submission;
+* a queued request can be cancelled; the others complete.
+"""
+import numpy as np
+import pytest
+
+from aran_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def requests():
+    rng = np.random.default_rng(77)
+    out = []
+    for i in range(10):
+        n = int(np.exp(rng.uniform(np.log(2000), np.log(150000))))
+        p = [6, 10, 16][i % 3]
+        if i % 2:
+            x, q = W.plummer(n, 200 + i)
+            lb, ub = (-1, -1, -1), (1, 1, 1)
+        else:
+            x, q = W.uniform(n, 200 + i)
+            lb, ub = (0, 0, 0), (1, 1, 1)
+        prec = "mixed" if i % 4 else "fp64"
+        out.append((x, q, dict(lbound=lb, ubound=ub, maxbox=32, order=p, field=True,
+                               precision=prec)))
+    return out
+
+
+def test_same_alone_and_in_the_mix(aran):
+    reqs = requests()
+    alone = []
+    for x, q, kw in reqs:
+        kw2 = dict(kw)
+        lb, ub = kw2.pop("lbound"), kw2.pop("ubound")
+        with aran.Solver3d(lb, ub, **kw2) as s:
+            alone.append(s.solve(x, q))
+    with aran.Server(nslots=4, hbm_budget_bytes=100e9) as sv:
+        tickets = [sv.submit(x, q, **kw) for x, q, kw in reqs]
+        mixed = [sv.wait(t) for t in tickets]
+    overlaps = 0
+    infos = [m[2] for m in mixed]
+    for i, a in enumerate(infos):
+        for b in infos[i + 1:]:
+            overlaps += a["start_s"] < b["end_s"] and b["start_s"] < a["end_s"]
+    assert overlaps > 0, "requests should run concurrently"
+    for (pa, fa), (pm, fm, info) in zip(alone, mixed):
+        assert info["status"] == 0
+        assert rel_l2(pm, pa) < TOL
+        assert rel_l2(fm, fa) < TOL
+
+
+def test_admission_budget(aran):
+    n = 200_000
+    fp = aran.footprint_bytes(n, maxbox=32, order=10, precision="mixed")
+    with aran.Server(nslots=4, hbm_budget_bytes=1.5 * fp) as sv:
+        tickets = []
+        for i in range(3):
+            x, q = W.uniform(n, 300 + i)
+            tickets.append(sv.submit(x, q, maxbox=32, order=10, precision="mixed"))
+        infos = [sv.wait(t)[2] for t in tickets]
+        for i, a in enumerate(infos):
+            for b in infos[i + 1:]:
+                assert not (a["start_s"] < b["end_s"] and b["start_s"] < a["end_s"])
+        x, q = W.uniform(2 * n, 9)
+        with pytest.raises(aran.AranError) as ei:
+            sv.submit(x, q, maxbox=32, order=10, precision="mixed")
+        assert ei.value.code == -4
+
+
+def test_cancel_queued_request(aran):
+    with aran.Server(nslots=1, hbm_budget_bytes=100e9) as sv:
+        big = W.uniform(400_000, 11)
+        t0 = sv.submit(*big, maxbox=64, order=12, precision="fp64")
+        small = [W.uniform(5000, 12 + i) for i in range(3)]
+        ts = [sv.submit(*s, maxbox=32, order=6) for s in small]
+        sv.cancel(ts[1])
+        pot0, _, info0 = sv.wait(t0)
+        assert info0["status"] == 0
+        with pytest.raises(aran.AranError) as ei:
+            sv.wait(ts[1])
+        assert ei.value.code == -7
+        for t in (ts[0], ts[2]):
+            assert sv.wait(t)[2]["status"] == 0
