@@ -14,16 +14,19 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(ROOT, "_build", "aran_gpu")
 LIB = os.path.join(HERE, "libaran_gpu.so")
-SOURCES = ["tables.cu", "tree.cu", "passes.cu", "p2p.cu", "m2l.cu", "kkylin.cu", "noalloc.cu", "server.cu", "solver.cu"]
+SOURCES = ["tables.cu", "tree.cu", "passes.cu", "p2p.cu", "m2l.cu", "kkylin.cu", "noalloc.cu", "server.cu", "solver.cu", "compat.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-         "-I/usr/local/cuda/include/cccl", "--expt-relaxed-constexpr"]
+         "-I/usr/local/cuda/include/cccl", "-I" + os.path.join(ROOT, "include"),
+         "--expt-relaxed-constexpr"]
 
 
 def _deps() -> list[str]:
     out = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh"))]
-    out.append(os.path.join(ROOT, "include", "aran_gpu.h"))
+    for sub in ("", "aran", "vsg"):
+        d = os.path.join(ROOT, "include", sub)
+        out += [os.path.join(d, f) for f in os.listdir(d) if f.endswith(".h")]
     return out
 
 

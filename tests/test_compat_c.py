@@ -1,0 +1,105 @@
+"""LibAran's own C API on the GPU library.
+
+tests/c/newton_compat.c is a Newton program written against the LibAran
+headers (aran/aransolver3d.h, aran/arandevelopment3d.h, vsg/vsgd.h) in the
+call sequence of the reference's tests/newtonfield3.c and tests/newtonpot3.c.
+It is compiled with gcc against include/ and linked with libaran_gpu.so; it
+checks every particle against a double-precision direct sum and prints the
+largest relative error.
+
+* without a GPU the solve refuses loudly (no CPU fallback);
+* rotate and kkylin operator addresses select the two GPU flavours, for the
+  potential (gcomplex128 accumulator) and the field (VsgVector3d);
+* results accumulate into the points like the reference callbacks (two
+  solves give twice the field);
+* the normal flavour and a missing layout are refused and leave the points
+  untouched.
+"""
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "c", "newton_compat.c")
+
+
+@pytest.fixture(scope="module")
+def exe(tmp_path_factory):
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    import aran_gb300
+    aran_gb300.load()
+    libdir = os.path.dirname(aran_gb300.LIB_PATH)
+    out = str(tmp_path_factory.mktemp("compat") / "newton_compat")
+    cmd = ["gcc", "-std=c11", "-O2", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"),
+           SRC, "-L" + libdir, "-laran_gpu", "-Wl,-rpath," + libdir, "-lm", "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+def run(exe, *args):
+    r = subprocess.run([exe] + [str(a) for a in args], capture_output=True, text=True,
+                       timeout=600)
+    return r.returncode, r.stdout + r.stderr
+
+
+def parse(out):
+    return {k: float(v) for k, v in re.findall(r"(\w+)=([-+0-9.e]+)", out)}
+
+
+def test_no_device_refuses(exe):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    rc, out = run(exe, 1000, 8, "rotate", "field", "fp64")
+    assert rc == 2, out
+    assert "error:" in out and "CUDA" in out
+
+
+# largest per-particle relative error over 20,000 uniform particles in
+# [-1,1]^3, leaf 32 (the reference's own accuracy tests accept 1e-3)
+CASES = [
+    ("rotate", "field", "fp64", 12, 2e-5),
+    ("rotate", "pot", "fp64", 12, 5e-7),
+    ("rotate", "field", "mixed", 12, 5e-5),
+    ("rotate", "pot", "mixed", 8, 5e-5),
+    ("kkylin", "field", "fp64", 10, 1e-4),
+    ("kkylin", "pot", "mixed", 10, 2e-5),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("flavour,kind,prec,order,tol", CASES)
+def test_newton_program(exe, flavour, kind, prec, order, tol):
+    rc, out = run(exe, 20000, order, flavour, kind, prec)
+    assert rc == 0, out
+    v = parse(out)
+    assert v["maxerr"] < tol, out
+    assert v["host_calls"] == 0
+    assert v["p2p"] > 0 and v["m2l"] > 0 and v["p2m"] > 0 and v["l2p"] > 0
+    assert v["depth"] >= 3
+
+
+@pytest.mark.gpu
+def test_results_accumulate(exe):
+    rc, out = run(exe, 8000, 10, "rotate", "field", "fp64", "twice")
+    assert rc == 0, out
+    assert parse(out)["maxerr"] < 1e-4, out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("args,msg", [
+    ((4000, 8, "normal", "field", "fp64"), "rotate or the kkylin"),
+    ((4000, 8, "rotate", "field", "fp64", "nolayout"), "set_newton_layout"),
+])
+def test_refused_solves_leave_points_untouched(exe, args, msg):
+    rc, out = run(exe, *args)
+    assert rc == 2, out
+    assert msg in out
