@@ -89,11 +89,15 @@ def lib():
         L.or_morton_key.restype = C.c_uint64
         L.or_morton_key.argtypes = [dp, dp, dp]
         L.or_direct.argtypes = [C.c_int, dp, dp, C.c_int, i32p, dp, dp, C.c_int]
-        if hasattr(L, "or_laurent_solve2d"):
-            L.or_laurent_solve2d.argtypes = [C.c_int, dp, dp, dp, dp, C.c_int,
-                                             C.c_int, dp, i64p]
-            L.or_direct2d.argtypes = [C.c_int, dp, dp, dp]
-            L.or_laurent_p2m.argtypes = [C.c_double] * 5 + [C.c_int, dp]
+        L.or2_p2m.argtypes = [C.c_double] * 5 + [C.c_int, dp]
+        L.or2_p2l.argtypes = [C.c_double] * 5 + [C.c_int, dp]
+        for f in (L.or2_translate, L.or2_to_taylor):
+            f.argtypes = [C.c_int, C.c_int, dp, C.c_double, C.c_double, C.c_int, C.c_int,
+                          dp, C.c_double, C.c_double]
+        L.or2_evaluate.argtypes = [C.c_int, C.c_int, dp, C.c_double, C.c_double, dp]
+        L.or2_solve.restype = C.c_int
+        L.or2_solve.argtypes = [C.c_void_p, C.c_int, i64p, dp, dp, dp, dp, i64p]
+        L.or2_direct.argtypes = [C.c_int, dp, dp, C.c_int, i32p, dp]
         _lib = L
     return _lib
 
@@ -276,3 +280,89 @@ def direct(xyz, q, targets=None, nthreads=0):
     tp = None if targets_arr is None else targets_arr.ctypes.data_as(C.POINTER(C.c_int32))
     lib().or_direct(n, _dp(xyz), _dp(q), nt, tp, _dp(pot), _dp(fld), nthreads)
     return pot, fld
+
+
+# ------------------------------------------------------------------------ 2D
+class Solve2Config(C.Structure):
+    _fields_ = [("maxbox", C.c_int), ("order", C.c_int), ("max_depth", C.c_int)]
+
+
+def laurent(posdeg: int, negdeg: int) -> np.ndarray:
+    """Zero Laurent series; index posdeg - i holds the term of degree i."""
+    return np.zeros(posdeg + negdeg + 1, dtype=np.complex128)
+
+
+def p2m2d(z, q, center, negdeg, out=None):
+    out = laurent(0, negdeg) if out is None else out
+    lib().or2_p2m(float(np.real(z)), float(np.imag(z)), float(q), float(np.real(center)),
+                  float(np.imag(center)), negdeg, _dp(out.view(np.float64)))
+    return out
+
+
+def p2l2d(z, q, center, posdeg, out=None):
+    out = laurent(posdeg, 0) if out is None else out
+    lib().or2_p2l(float(np.real(z)), float(np.imag(z)), float(q), float(np.real(center)),
+                  float(np.imag(center)), posdeg, _dp(out.view(np.float64)))
+    return out
+
+
+def _laurent_op(f, src, sdeg, zsrc, ddeg, zdst, out):
+    sp, sn = sdeg
+    dp_, dn = ddeg
+    out = laurent(dp_, dn) if out is None else out
+    src = np.ascontiguousarray(src, np.complex128)
+    f(sp, sn, _dp(src.view(np.float64)), float(np.real(zsrc)), float(np.imag(zsrc)), dp_, dn,
+      _dp(out.view(np.float64)), float(np.real(zdst)), float(np.imag(zdst)))
+    return out
+
+
+def translate2d(src, sdeg, zsrc, ddeg, zdst, out=None):
+    """aran_laurent_seriesd_translate (M2M / L2L)."""
+    return _laurent_op(lib().or2_translate, src, sdeg, zsrc, ddeg, zdst, out)
+
+
+def to_taylor2d(src, sdeg, zsrc, ddeg, zdst, out=None):
+    """aran_laurent_seriesd_to_taylor (M2L)."""
+    return _laurent_op(lib().or2_to_taylor, src, sdeg, zsrc, ddeg, zdst, out)
+
+
+def evaluate2d(s, deg, z) -> complex:
+    out = np.zeros(2)
+    s = np.ascontiguousarray(s, np.complex128)
+    lib().or2_evaluate(deg[0], deg[1], _dp(s.view(np.float64)), float(np.real(z)),
+                       float(np.imag(z)), _dp(out))
+    return complex(out[0], out[1])
+
+
+def solve2d(xy, q, offsets, boxes, maxbox, order, max_depth=21):
+    """2D FMM of sum_j q_j/(z_i - z_j) over independent systems.
+
+    xy (n, 2), q (n,), offsets (nsys + 1,), boxes (nsys, 4) = lbx, lby, ubx, uby.
+    Returns (complex accumulators (n,), stats dict summed over systems)."""
+    xy = np.ascontiguousarray(xy, np.float64)
+    q = np.ascontiguousarray(q, np.float64)
+    offs = np.ascontiguousarray(offsets, np.int64)
+    boxes = np.ascontiguousarray(boxes, np.float64)
+    acc = np.zeros(2 * len(q))
+    st = np.zeros(NSTATS, np.int64)
+    c = Solve2Config(maxbox, order, max_depth)
+    rc = lib().or2_solve(C.byref(c), len(offs) - 1, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                         _dp(xy), _dp(q), _dp(boxes), _dp(acc),
+                         st.ctypes.data_as(C.POINTER(C.c_int64)))
+    if rc != 0:
+        raise ValueError("or2_solve rejected the configuration")
+    return acc.view(np.complex128), dict(zip(STAT_NAMES, st.tolist()))
+
+
+def direct2d(xy, q, targets=None):
+    """FP64 direct sum of sum_{j != i} q_j/(z_i - z_j) for one system."""
+    xy = np.ascontiguousarray(xy, np.float64)
+    q = np.ascontiguousarray(q, np.float64)
+    if targets is None:
+        nt, tp = len(q), None
+    else:
+        targets = np.ascontiguousarray(targets, np.int32)
+        nt, tp = len(targets), targets.ctypes.data_as(C.POINTER(C.c_int32))
+    acc = np.zeros(2 * nt)
+    lib().or2_direct(len(q), _dp(xy), _dp(q), nt, tp, _dp(acc))
+    return acc.view(np.complex128)

@@ -115,14 +115,42 @@ void or_direct (int n, const double *xyz, const double *q, int nt,
                 const int32_t *targets, double *pot, double *field,
                 int nthreads);
 
-/* ---- 2D Laurent series (aran/aranlaurentseriesd.c) ---------------------- */
-void or_laurent_p2m (double zx, double zy, double q, double cx, double cy,
-                     int negdeg, double *neg /* negdeg complex */);
-void or_laurent_solve2d (int n, const double *xy, const double *q,
-                         const double lb[2], const double ub[2], int maxbox,
-                         int order, double *acc /* 2n */,
-                         int64_t stats[OR_NSTATS]);
-void or_direct2d (int n, const double *xy, const double *q, double *acc);
+/* ---- 2D: Laurent series and the Cauchy-kernel solve --------------------
+ * A Laurent series of degrees (posdeg, negdeg) holds posdeg + negdeg + 1
+ * complex terms (interleaved re, im); the term of degree i,
+ * -negdeg <= i <= posdeg, sits at index posdeg - i
+ * (aran/aranlaurentseriesd.c:37-43).  A 2D development is a multipole
+ * laurent(0, p) and a local laurent(p, 0) (aran/arandevelopment2d.c:64-73). */
+void or2_p2m (double x, double y, double q, double cx, double cy, int negdeg,
+              double *mult);
+void or2_p2l (double x, double y, double q, double cx, double cy, int posdeg,
+              double *loc);
+void or2_translate (int sp, int sn, const double *src, double zsx, double zsy,
+                    int dp, int dn, double *dst, double zdx, double zdy);
+void or2_to_taylor (int sp, int sn, const double *src, double zsx, double zsy,
+                    int dp, int dn, double *dst, double zdx, double zdy);
+void or2_evaluate (int pd, int nd, const double *s, double zx, double zy,
+                   double out[2]);
+
+typedef struct
+{
+  int maxbox;         /* leaf capacity */
+  int order;          /* p: aran_development2d_new (0, p) */
+  int max_depth;      /* <= 21 (0: 21) */
+} Or2Config;
+
+/* Solves nsys independent 2D systems (system s holds particles
+ * offs[s]..offs[s+1]-1 in the box box[4s..4s+3] = lbx, lby, ubx, uby):
+ * acc_i = sum_j q_j / (z_i - z_j), j != i, the kernel of tests/dummypot.c,
+ * as the reference solver computes it (P2P, P2M, M2M, M2L, L2L, L2P over a
+ * quadtree with the traversal rules of the 3D oracle).  acc holds 2 doubles
+ * per particle; stats are summed over the systems. */
+int or2_solve (const Or2Config *cfg, int nsys, const int64_t *offs,
+               const double *xy, const double *q, const double *box,
+               double *acc, int64_t stats[OR_NSTATS]);
+/* FP64 direct sum of the same kernel for the listed targets of one system */
+void or2_direct (int n, const double *xy, const double *q, int nt,
+                 const int32_t *targets, double *acc);
 
 #ifdef __cplusplus
 }

@@ -353,3 +353,99 @@ def test_direct_sum_small(oracle):
     ref_f = (-q[None, :, None] * d / r[:, :, None] ** 3).sum(1)
     assert np.allclose(pot, ref_p, rtol=1e-12, atol=0)
     assert np.allclose(fld, ref_f, rtol=1e-10, atol=1e-12)
+
+
+# ------------------------------------------------------------------------ 2D
+# tests/laurent.c: the series of 1/(z-1) (a_{-i} = 1, order 24) checked in
+# rings outside radius 2, translated to 2i (ring radius 4) and re-expanded as
+# a Taylor series at 6i (disk of radius 2), tolerance 1e-7.
+def _rings(oracle, s, deg, center, radius, f, inner):
+    worst = 0.0
+    pts = [0j] if inner else []
+    for i in range(11):
+        r = i * radius / 10 + (0 if inner else radius)
+        pts += [r * np.exp(2j * np.pi * j / i) for j in range(i)]
+    for z in pts:
+        ref = f(z + center)
+        worst = max(worst, abs((ref - oracle.evaluate2d(s, deg, z)) / ref))
+    return worst
+
+
+def test_laurent_series_of_inverse_z_minus_one(oracle):
+    order = 24
+    f = lambda z: 1 / (z - 1)
+    als = oracle.laurent(0, order)
+    als[1:] = 1.0
+    assert _rings(oracle, als, (0, order), 0, 2.0, f, False) < 1e-7
+    alst = oracle.translate2d(als, (0, order), 0, (0, order), 2j)
+    assert _rings(oracle, alst, (0, order), 2j, 4.0, f, False) < 1e-7
+    alstt = oracle.to_taylor2d(als, (0, order), 0, (order, 0), 6j)
+    assert _rings(oracle, alstt, (order, 0), 6j, 2.0, f, True) < 1e-7
+
+
+def test_laurent_storage_order(oracle):
+    # degree i of a (posdeg, negdeg) series sits at posdeg - i
+    s = oracle.p2m2d(0.3 + 0.1j, 2.0, 0.0, 5)
+    d = 0.3 + 0.1j
+    assert s[0] == 0
+    np.testing.assert_allclose(s[1:5], 2.0 * d ** np.arange(4), rtol=1e-15)
+    assert s[5] == 0  # a_{-negdeg} is never filled (loop i < negdeg)
+
+
+def test_p2l2d_is_the_cauchy_kernel(oracle):
+    # tests/p2l2.c: source (3, -1), charge 1, centre (5, 0), degree 29,
+    # points of the half disk of radius 1 (N = 10 x 10); the local value is
+    # 1/(z - zp) (the p2l2.c check compares its negation and never fails)
+    zp, c, deg = 3 - 1j, 5 + 0j, 29
+    loc = oracle.p2l2d(zp, 1.0, c, deg)
+    worst = 0.0
+    for j in range(10):
+        t = np.pi * j / 9
+        for k in range(10):
+            w = (k / 9) * np.exp(1j * t)
+            ref = 1 / (w + c - zp)
+            worst = max(worst, abs(oracle.evaluate2d(loc, (deg, 0), w) - ref) / abs(ref))
+    assert worst < 1e-9
+
+
+def _circle(n, r=0.9):
+    t = 2 * np.pi * np.arange(n) / n
+    return np.stack([r * np.cos(t), r * np.sin(t)], 1)
+
+
+# tests/dummypot.at: (np, order, maxbox, err); distribution circle of radius
+# 0.9 unless "random" (uniform in [-0.9, 0.9]^2), unit densities, box [-1,1]^2
+DUMMYPOT_AT = [
+    ("circle", 12, 20, 1, 1e-6),
+    ("circle", 2400, 20, 1, 1e-6),
+    ("circle", 240, 40, 1, 1e-8),
+    ("random", 240, 20, 1, 1e-6),
+    ("circle", 240, 20, 10, 1e-8),
+    ("circle", 2400, 20, 10, 1e-6),
+]
+
+
+@pytest.mark.parametrize("dist,n,order,maxbox,tol", DUMMYPOT_AT)
+def test_dummypot_cases(oracle, dist, n, order, maxbox, tol):
+    xy = _circle(n) if dist == "circle" else np.random.default_rng(0).uniform(-0.9, 0.9, (n, 2))
+    q = np.ones(n)
+    acc, st = oracle.solve2d(xy, q, [0, n], [[-1, -1, 1, 1]], maxbox, order)
+    ref = oracle.direct2d(xy, q)
+    err = np.abs(acc - ref) / np.maximum(np.abs(acc), np.abs(ref))
+    assert err.max() < tol
+    assert st["p2m"] == n and st["l2p"] == n
+
+
+def test_solve2d_systems_are_independent(oracle):
+    rng = np.random.default_rng(3)
+    sizes = [300, 1, 0, 1200]
+    xy = rng.uniform(-1, 1, (sum(sizes), 2))
+    q = rng.uniform(-1, 1, sum(sizes))
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    boxes = np.tile([-1.0, -1.0, 1.0, 1.0], (len(sizes), 1))
+    acc, _ = oracle.solve2d(xy, q, offs, boxes, 16, 20)
+    for s in range(len(sizes)):
+        a, b = offs[s], offs[s + 1]
+        if b > a:
+            one, _ = oracle.solve2d(xy[a:b], q[a:b], [0, b - a], boxes[s:s + 1], 16, 20)
+            np.testing.assert_array_equal(acc[a:b], one)
