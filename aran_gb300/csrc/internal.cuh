@@ -20,6 +20,22 @@ struct CudaError {
   std::string where;
 };
 
+// sets the thread's last error and returns the status code
+inline int fail(int code, const std::string &msg) {
+  set_error(msg);
+  return code;
+}
+
+// status code and message of a CUDA runtime failure
+inline int from_cuda(const CudaError &e) {
+  std::string m = std::string("CUDA error ") + cudaGetErrorName(e.code) + ": " +
+                  cudaGetErrorString(e.code) + " in " + e.where;
+  set_error(m);
+  if (e.code == cudaErrorMemoryAllocation) return ARAN_ERR_OOM;
+  if (e.code == cudaErrorNoDevice || e.code == cudaErrorInsufficientDriver) return ARAN_ERR_NO_DEVICE;
+  return ARAN_ERR_CUDA;
+}
+
 #define ACHECK(call)                                                          \
   do {                                                                        \
     cudaError_t e_ = (call);                                                  \

@@ -19,20 +19,6 @@ void scatter_outputs(AranGpuSolver3d *s, double *pot, double *fld);
 
 namespace {
 
-int fail(int code, const std::string &msg) {
-  set_error(msg);
-  return code;
-}
-
-int from_cuda(const CudaError &e) {
-  std::string m = std::string("CUDA error ") + cudaGetErrorName(e.code) + ": " +
-                  cudaGetErrorString(e.code) + " in " + e.where;
-  set_error(m);
-  if (e.code == cudaErrorMemoryAllocation) return ARAN_ERR_OOM;
-  if (e.code == cudaErrorNoDevice || e.code == cudaErrorInsufficientDriver) return ARAN_ERR_NO_DEVICE;
-  return ARAN_ERR_CUDA;
-}
-
 int check_config(const AranGpuConfig3d *c) {
   if (!c) return fail(ARAN_ERR_INVALID, "config is NULL");
   for (int a = 0; a < 3; ++a)
