@@ -33,6 +33,9 @@ EXPORTS = (
     "aran_gpu_version", "aran_gpu_p2p_direct_noalloc", "aran_gpu_footprint_bytes",
     "aran_gpu_server_create", "aran_gpu_server_submit", "aran_gpu_server_wait",
     "aran_gpu_server_cancel", "aran_gpu_server_destroy",
+    "aran_gpu_solver2d_create", "aran_gpu_solver2d_destroy", "aran_gpu_solver2d_solve",
+    "aran_gpu_solver2d_get_stats", "aran_gpu_solver2d_timings", "aran_gpu_solver2d_tree_info",
+    "aran_gpu_solver2d_launches",
 )
 
 
@@ -48,6 +51,10 @@ class Config3d(C.Structure):
     _fields_ = [("lb", C.c_double * 3), ("ub", C.c_double * 3), ("maxbox", C.c_int),
                 ("order", C.c_int), ("flavour", C.c_int), ("field", C.c_int),
                 ("precision", C.c_int), ("max_depth", C.c_int)]
+
+
+class Config2d(C.Structure):
+    _fields_ = [("maxbox", C.c_int), ("order", C.c_int), ("max_depth", C.c_int)]
 
 
 class Request3d(C.Structure):
@@ -109,6 +116,19 @@ def load(build_if_missing: bool = True):
     L.aran_gpu_server_cancel.restype = C.c_int
     L.aran_gpu_server_destroy.argtypes = [vp]
     L.aran_gpu_server_destroy.restype = None
+    L.aran_gpu_solver2d_create.argtypes = [C.POINTER(Config2d), C.POINTER(vp)]
+    L.aran_gpu_solver2d_create.restype = C.c_int
+    L.aran_gpu_solver2d_destroy.argtypes = [vp]
+    L.aran_gpu_solver2d_destroy.restype = None
+    L.aran_gpu_solver2d_solve.argtypes = [vp, C.c_int, i64p, dp, vp, vp, vp, C.c_int]
+    L.aran_gpu_solver2d_solve.restype = C.c_int
+    for f in (L.aran_gpu_solver2d_get_stats, L.aran_gpu_solver2d_tree_info):
+        f.argtypes = [vp, i64p]
+        f.restype = C.c_int
+    L.aran_gpu_solver2d_timings.argtypes = [vp, dp]
+    L.aran_gpu_solver2d_timings.restype = C.c_int
+    L.aran_gpu_solver2d_launches.argtypes = [vp]
+    L.aran_gpu_solver2d_launches.restype = C.c_int64
     L.aran_gpu_last_error.restype = C.c_char_p
     L.aran_gpu_version.restype = C.c_char_p
     _lib = L
@@ -314,6 +334,93 @@ class Solver3d:
 
     def launches(self) -> int:
         return int(load().aran_gpu_solver3d_launches(self._h))
+
+
+class Solver2d:
+    """GPU counterpart of ``AranSolver2d`` with the Cauchy kernel of
+    tests/dummypot.c (acc_i = sum_{j != i} q_j / (z_i - z_j)), solving a
+    batch of independent systems per call.
+
+    ``order`` is p of ``aran_development2d_new (0, p)``, ``maxbox`` the leaf
+    capacity of ``vsg_prtree2d_new_full``.  FP64 throughout."""
+
+    def __init__(self, *, maxbox=32, order=20, max_depth=21):
+        cfg = Config2d(int(maxbox), int(order), int(max_depth))
+        h = C.c_void_p()
+        _check(load().aran_gpu_solver2d_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.cfg = cfg
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().aran_gpu_solver2d_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @staticmethod
+    def _meta(n, offsets, boxes):
+        offs = np.ascontiguousarray([0, n] if offsets is None else offsets, dtype=np.int64)
+        nsys = len(offs) - 1
+        if nsys < 1 or offs[-1] != n:
+            # the library trusts offs[nsys] as the particle count
+            raise AranError(-1, "offsets must have nsys + 1 entries ending at n")
+        if boxes is None:
+            boxes = np.tile([-1.0, -1.0, 1.0, 1.0], (nsys, 1))
+        boxes = np.ascontiguousarray(np.broadcast_to(np.asarray(boxes, np.float64), (nsys, 4)))
+        return offs, boxes
+
+    def solve(self, xy, q, offsets=None, boxes=None):
+        """Host arrays: xy (n, 2), q (n,); offsets (nsys + 1,) split the
+        particles into systems with boxes (nsys, 4) = lbx, lby, ubx, uby
+        (default one system in [-1, 1]^2).  Returns complex acc (n,)."""
+        xy = np.ascontiguousarray(xy, dtype=np.float64)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        n = len(q)
+        if xy.shape != (n, 2):
+            raise ValueError("xy must be (n, 2)")
+        offs, boxes = self._meta(n, offsets, boxes)
+        acc = np.empty(n, np.complex128)
+        _check(load().aran_gpu_solver2d_solve(
+            self._h, len(offs) - 1, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+            boxes.ctypes.data_as(C.POINTER(C.c_double)), _ptr(xy), _ptr(q), _ptr(acc), MEM_HOST))
+        return acc
+
+    def solve_device(self, n, xy_ptr, q_ptr, acc_ptr, offsets=None, boxes=None):
+        """Device pointers for xy, q and acc (2n doubles); host metadata."""
+        offs, boxes = self._meta(n, offsets, boxes)
+        _check(load().aran_gpu_solver2d_solve(
+            self._h, len(offs) - 1, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+            boxes.ctypes.data_as(C.POINTER(C.c_double)), C.c_void_p(xy_ptr), C.c_void_p(q_ptr),
+            C.c_void_p(acc_ptr), MEM_DEVICE))
+
+    def get_stats(self) -> dict:
+        st = np.zeros(11, np.int64)
+        _check(load().aran_gpu_solver2d_get_stats(self._h, st.ctypes.data_as(C.POINTER(C.c_int64))))
+        return dict(zip(STAT_NAMES, st.tolist()))
+
+    def tree_info(self) -> dict:
+        info = np.zeros(5, np.int64)
+        _check(load().aran_gpu_solver2d_tree_info(self._h, info.ctypes.data_as(C.POINTER(C.c_int64))))
+        return dict(zip(("nodes", "far", "near", "leaves", "depth"), info.tolist()))
+
+    def timings(self) -> dict:
+        ms = np.zeros(16)
+        _check(load().aran_gpu_solver2d_timings(self._h, ms.ctypes.data_as(C.POINTER(C.c_double))))
+        return dict(zip(STAGE_NAMES, ms[:len(STAGE_NAMES)].tolist()))
+
+    def launches(self) -> int:
+        return int(load().aran_gpu_solver2d_launches(self._h))
 
 
 NOALLOC_MAX = 131072

@@ -206,6 +206,9 @@ def cpu_baseline(name: str, n_sample: int, procs: int, rounds: int = 1) -> dict:
 
 
 # ----------------------------------------------------------------- GPU arm
+M2L_DRAM_BYTES_PER_NODE = (28.17408e6 + 0.37632e6) / 37449
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -352,7 +355,7 @@ def run_gpu(args):
     # written local once (FP32 complex), at the HBM roofline
     alg_bytes = (info["far"] * (p * (p + 1) // 2) + info["nodes"] * ((p + 1) * (p + 2) // 2)) * 8
     roof = {
-        "kernel": "k_m2l_rotate<float>",
+        "kernel": "k_m2l_sibling<float> (rotate M2L, all levels, one launch)",
         "bound": "fp32",
         "achieved": round(achieved, 3), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
         "frac": round(achieved / fp32_peak, 4),
@@ -365,7 +368,14 @@ def run_gpu(args):
                      "achieved_gbs": round(alg_bytes / m2l_s / 1e9, 1),
                      "peak_gbs": peaks.get("hbm_gbs", 6803.8),
                      "frac": round(alg_bytes / m2l_s / 1e9 / peaks.get("hbm_gbs", 6803.8), 4)},
-        "traffic": args.m2l_traffic,
+        # DRAM bytes per launch: ncu capture of this kernel on uniform1m
+        # (profiles/m2l_sibling_uniform1m_p12_mixed.md), 762 B per tree node,
+        # scaled by this tree's node count
+        "traffic": (args.m2l_traffic if args.m2l_traffic is not None
+                    else round(M2L_DRAM_BYTES_PER_NODE * info["nodes"])),
+        "traffic_source": ("--m2l-traffic" if args.m2l_traffic is not None else
+                           "ncu dram__bytes_read.sum+write.sum of the uniform1m launch, "
+                           "scaled by node count"),
         "bf16_tensor_peak_tflops": peaks.get("bf16_tflops"),
     }
     line = {

@@ -171,6 +171,44 @@ int aran_gpu_server_cancel (AranGpuServer *sv, int64_t ticket);
 /* Finishes running requests, cancels queued ones, frees everything. */
 void aran_gpu_server_destroy (AranGpuServer *sv);
 
+/* ---- 2D: Cauchy-kernel FMM over a batch of independent systems --------
+ * Replaces aran_solver2d_solve (aran/aransolver2d.c:1137-1204) with the
+ * operators aran_development2d_{p2m,m2m,m2l,l2l,local_evaluate}
+ * (aran/arandevelopment2d.c:167-346: Laurent multipole laurent(0, p), Taylor
+ * local laurent(p, 0)) and the P2P kernel of tests/dummypot.c:62-76:
+ * acc_i = sum_{j != i} q_j / (z_i - z_j), complex, FP64.  One call solves
+ * nsys systems at once (a forest: one quadtree per system). */
+
+typedef struct
+{
+  int maxbox;          /* leaf capacity (vsg_prtree2d_new_full maxbox) */
+  int order;           /* p of aran_development2d_new (0, p), 1..64 */
+  int max_depth;       /* quadtree depth limit, 1..21 (0 = 21) */
+} AranGpuConfig2d;
+
+typedef struct AranGpuSolver2d AranGpuSolver2d;
+
+int aran_gpu_solver2d_create (const AranGpuConfig2d *cfg, AranGpuSolver2d **out);
+void aran_gpu_solver2d_destroy (AranGpuSolver2d *s);
+
+/* System s holds particles offs[s] .. offs[s+1]-1 (offs: nsys+1 host
+ * int64, offs[0] = 0, non-decreasing) in the box box[4s .. 4s+3] = (lbx,
+ * lby, ubx, uby) (host).  xy is 2n doubles (AoS), q n doubles, acc receives
+ * 2n doubles (re, im per particle).  mem selects host or device pointers for
+ * xy, q and acc. */
+int aran_gpu_solver2d_solve (AranGpuSolver2d *s, int nsys, const int64_t *offs,
+                             const double *box, const double *xy, const double *q,
+                             double *acc, int mem);
+/* Call counters of the last solve, summed over its systems, in the order
+ * of aran_solver2d_get_stats (aran/aransolver2d.c:868-896). */
+int aran_gpu_solver2d_get_stats (AranGpuSolver2d *s, int64_t stats[11]);
+/* Stage times of the last solve in ms, same slots as the 3D solver. */
+int aran_gpu_solver2d_timings (AranGpuSolver2d *s, double ms[16]);
+/* Sizes of the last forest: nodes, directed far entries, near ranges,
+ * non-empty leaves, depth. */
+int aran_gpu_solver2d_tree_info (AranGpuSolver2d *s, int64_t info[5]);
+int64_t aran_gpu_solver2d_launches (AranGpuSolver2d *s);
+
 /* Last error message of the calling thread. */
 const char *aran_gpu_last_error (void);
 

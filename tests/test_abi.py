@@ -87,3 +87,7 @@ def test_invalid_configs_rejected_before_device_use():
     with pytest.raises(aran_gb300.AranError) as ei:
         aran_gb300.Solver3d((0, 0, 0), (0, 1, 1))
     assert ei.value.code == -1
+    for kw in (dict(order=0), dict(order=65), dict(maxbox=0), dict(max_depth=22)):
+        with pytest.raises(aran_gb300.AranError) as ei:
+            aran_gb300.Solver2d(**kw)
+        assert ei.value.code == -1, kw
