@@ -385,7 +385,6 @@ int aran_solver3d_solve_try(AranSolver3d *solver) {
     for (int k = 0; k < 11; ++k) solver->stats[k] += st[k];
   int64_t info[5];
   if (aran_gpu_solver3d_tree_info(solver->gpu, info) == ARAN_OK) solver->depth = (guint)info[4];
-  if (solver->zero && solver->devel) solver->zero(solver->devel);
   return ARAN_OK;
 }
 

@@ -14,6 +14,10 @@ These generators reproduce those distributions (numpy PCG64, fixed seeds):
 * blobs(n, seed)       -- 1-8 Gaussian blobs, sigma U[0.02,0.2], centres
                           U[0.2,0.8]^3, clipped to [0,1]^3 (config 4)
 * circle(n)            -- tests/newtonfield3.c:472-493
+* batch2d(nsys, seed)  -- config 4, 2D part: nsys systems, N log-uniform in
+                          [1e3, 1e5], uniform in [-1,1]^2, charges U[-1,1]
+* batch3d(nsys, seed)  -- config 4, 3D part: nsys systems, N log-uniform in
+                          [1e3, 2e5], uniform in [0,1]^3 or blobs, p in {4,8,12}
 """
 from __future__ import annotations
 
@@ -69,3 +73,31 @@ def circle(n: int):
     a = 2 * math.pi * np.arange(n) / n
     x = np.stack([R * np.cos(a), R * np.sin(a), np.zeros(n)], axis=1)
     return x, np.full(n, 1.0 / n)
+
+
+def batch2d(nsys: int = 512, seed: int = 4, nlo: float = 1e3, nhi: float = 1e5):
+    """xy (n, 2), q (n,), offsets (nsys + 1,), boxes (nsys, 4) of a batch of
+    independent 2D systems."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(nlo), np.log(nhi), nsys)).astype(np.int64)
+    n = int(sizes.sum())
+    xy = rng.uniform(-1.0, 1.0, (n, 2))
+    q = rng.uniform(-1.0, 1.0, n)
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    boxes = np.tile([-1.0, -1.0, 1.0, 1.0], (nsys, 1))
+    return xy, q, offs, boxes
+
+
+def batch3d(nsys: int = 2048, seed: int = 4, nlo: float = 1e3, nhi: float = 2e5):
+    """List of (x, q, order) of independent 3D systems in [0,1]^3."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(nsys):
+        n = int(np.exp(rng.uniform(np.log(nlo), np.log(nhi))))
+        p = (4, 8, 12)[int(rng.integers(0, 3))]
+        if rng.uniform() < 0.5:
+            x, q = uniform(n, 10_000 + i)
+        else:
+            x, q = blobs(n, 10_000 + i)
+        out.append((x, q, p))
+    return out

@@ -173,6 +173,106 @@ def run_serving(reqs, precision: str, nslots: int = 4, budget: float = 150e9) ->
             "mean_queue_ms": float(np.mean([i["start_s"] - i["submit_s"] for i in infos]) * 1e3)}
 
 
+# ------------------------------------------------------------------ batched
+def _cpu_job2d(args):
+    xy, q, order, maxbox = args
+    import oracle
+    t0 = time.perf_counter()
+    oracle.solve2d(xy, q, [0, len(q)], [[-1.0, -1.0, 1.0, 1.0]], maxbox, order)
+    return len(q), time.perf_counter() - t0
+
+
+def run_batched_2d(nsys: int, steps: int, order: int = 20, maxbox: int = 32) -> dict:
+    """Config 4, 2D part: one forest solve of nsys systems per step."""
+    import numpy as np
+    import torch
+    import aran_gb300 as A
+    from aran_gb300 import workloads as W
+    xy, q, offs, boxes = W.batch2d(nsys)
+    n = len(q)
+    dxy = torch.from_numpy(xy).cuda()
+    dq = torch.from_numpy(q).cuda()
+    dacc = torch.empty(2 * n, dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out = {"systems": nsys, "particles": n, "order": order, "maxbox": maxbox,
+           "description": "N log-uniform in [1e3, 1e5], uniform in [-1,1]^2, q~U[-1,1], "
+                          "sum_j q_j/(z_i - z_j) (tests/dummypot.c kernel), FP64"}
+    with A.Solver2d(maxbox=maxbox, order=order) as s:
+        for _ in range(2):
+            s.solve_device(n, dxy.data_ptr(), dq.data_ptr(), dacc.data_ptr(), offs, boxes)
+        dev_ms, stages = 0.0, []
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            s.solve_device(n, dxy.data_ptr(), dq.data_ptr(), dacc.data_ptr(), offs, boxes)
+            st = s.timings()
+            stages.append(st)
+            dev_ms += st["total"]
+        out["value"] = n * steps / (dev_ms * 1e-3)
+        out["unit"] = UNIT
+        out["ms_per_step"] = dev_ms / steps
+        out["stage_ms"] = {k: round(statistics.mean(d[k] for d in stages), 3) for k in stages[0]}
+        out["tree"] = s.tree_info()
+        out["gpu_launches_per_step"] = s.launches()
+        # end to end from pageable host arrays through the public call
+        e2e_ms = 0.0
+        for _ in range(steps):
+            acc = s.solve(xy, q, offs, boxes)
+            e2e_ms += s.timings()["total"]
+        out["e2e"] = {"value": n * steps / (e2e_ms * 1e-3), "unit": UNIT,
+                      "h2d_bytes_per_step": n * 24, "d2h_bytes_per_step": n * 16}
+    # accuracy on two systems against the FP64 direct sum (500 targets each)
+    import oracle
+    rng = np.random.default_rng(9)
+    worst, rl2 = 0.0, 0.0
+    for i in rng.choice(nsys, 2, replace=False):
+        a, b = int(offs[i]), int(offs[i + 1])
+        tgt = rng.choice(b - a, min(500, b - a), replace=False).astype(np.int32)
+        ref = oracle.direct2d(xy[a:b], q[a:b], tgt)
+        got = acc[a:b][tgt]
+        worst = max(worst, float((np.abs(got - ref) / np.maximum(np.abs(got), np.abs(ref))).max()))
+        rl2 = max(rl2, float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+    out["accuracy"] = {"max_rel_vs_direct": worst, "rel_l2_vs_direct": rl2}
+    # CPU: the oracle port on a sample of the systems, one process per core
+    sample = [(xy[offs[i]:offs[i + 1]], q[offs[i]:offs[i + 1]], order, maxbox)
+              for i in range(0, nsys, max(1, nsys // 32))][:32]
+    procs = min(len(sample), os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(procs) as pool:
+        done = sum(k for k, _ in pool.map(_cpu_job2d, sample))
+    el = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": done / el, "unit": UNIT, "cores": procs, "kind": "port",
+                           "sample": f"{len(sample)} of the systems ({done} particles), one "
+                                     f"single-threaded process each; {el:.1f} s wall"}
+    return out
+
+
+def run_batched_3d(nsys: int, precision: str = "mixed", nslots: int = 4) -> dict:
+    """Config 4, 3D part: every system a request of the request loop, all
+    submitted at once; throughput = particles / (last end - first submit)."""
+    import numpy as np
+    import aran_gb300 as A
+    from aran_gb300 import workloads as W
+    systems = W.batch3d(nsys)
+    kw = dict(lbound=(0.0, 0.0, 0.0), ubound=(1.0, 1.0, 1.0), maxbox=64, field=True,
+              precision=precision)
+    with A.Server(nslots=nslots, hbm_budget_bytes=150e9) as sv:
+        for p in (4, 8, 12):   # resident solvers per order in every slot
+            for t in [sv.submit(systems[0][0][:2000], systems[0][1][:2000], order=p, **kw)
+                      for _ in range(nslots)]:
+                sv.wait(t)
+        tickets = [sv.submit(x, q, order=p, **kw) for x, q, p in systems]
+        infos = [sv.wait(t)[2] for t in tickets]
+    span = max(i["end_s"] for i in infos) - min(i["submit_s"] for i in infos)
+    npart = sum(len(s[1]) for s in systems)
+    return {"systems": nsys, "particles": npart, "precision": precision, "slots": nslots,
+            "description": (f"the first {nsys} draws of the config-4 3D stream (2,048 "
+                            "systems): N log-uniform in [1e3, 2e5], uniform in [0,1]^3 or 1-8 "
+                            "Gaussian blobs, p in {4, 8, 12}, leaf 64, potential + field, "
+                            "host arrays in and out"),
+            "value": npart / span, "unit": UNIT, "wall_s": span}
+
+
 # ------------------------------------------------------------- CPU baseline
 def _cpu_job(args):
     name, n_sample, seed = args
@@ -416,6 +516,12 @@ def run_gpu(args):
             "mixed": run_serving(reqs, "mixed"),
             "fp64": run_serving(reqs, "fp64"),
         }
+    if args.batched_2d_systems > 0 or args.batched_3d_systems > 0:
+        line["batched"] = {}
+        if args.batched_2d_systems > 0:
+            line["batched"]["2d"] = run_batched_2d(args.batched_2d_systems, max(3, args.steps // 2))
+        if args.batched_3d_systems > 0:
+            line["batched"]["3d"] = run_batched_3d(args.batched_3d_systems)
     if args.cpu_baseline:
         procs = args.cpu_procs or os.cpu_count() or 1
         line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_sample, procs)
@@ -462,6 +568,8 @@ def main():
     ap.add_argument("--ref-warmup", type=int, default=0)
     ap.add_argument("--serving-requests", type=int, default=48)
     ap.add_argument("--serving-rate", type=float, default=16.0)
+    ap.add_argument("--batched-2d-systems", type=int, default=512)
+    ap.add_argument("--batched-3d-systems", type=int, default=512)
     ap.add_argument("--m2l-traffic", type=float, default=None,
                     help="dram bytes per M2L launch from an ncu capture (profiles/)")
     args = ap.parse_args()

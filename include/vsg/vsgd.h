@@ -60,6 +60,48 @@ void vsg_prtree3d_free (VsgPRTree3d *prtree);
 gint vsg_vector3d_vector3d_locfunc (const VsgVector3d *candidate, const VsgVector3d *center);
 gdouble vsg_vector3d_dist (const VsgVector3d *one, const VsgVector3d *other);
 
+/* ---- 2D (the quadtree of aran/aransolver2d.c) ---- */
+typedef struct _VsgVector2d VsgVector2d;
+struct _VsgVector2d
+{
+  gdouble x, y;
+};
+
+typedef gpointer VsgPoint2;
+typedef gpointer VsgRegion2;
+typedef struct _VsgPRTree2d VsgPRTree2d;
+
+typedef struct _VsgPRTree2dNodeInfo VsgPRTree2dNodeInfo;
+struct _VsgPRTree2dNodeInfo
+{
+  VsgVector2d center;
+  VsgVector2d lbound;
+  VsgVector2d ubound;
+  GSList *point_list;
+  guint point_count;
+  gboolean isleaf;
+  guint depth;
+  gpointer user_data;
+  VsgPRTree2dNodeInfo *father_info;
+  guint id;
+};
+
+typedef gint (*VsgPoint2dLocFunc) (const VsgPoint2 candidate, const VsgVector2d *center);
+typedef gdouble (*VsgPoint2dDistFunc) (const VsgPoint2 one, const VsgPoint2 other);
+typedef gint (*VsgRegion2dLocFunc) (const VsgRegion2 region, const VsgVector2d *center);
+
+/* The 2D tree description (bounding box and leaf capacity) the solver
+ * builds on the GPU (tests/dummypot.c:420-424). */
+VsgPRTree2d *vsg_prtree2d_new_full (const VsgVector2d *lbound,
+                                    const VsgVector2d *ubound,
+                                    VsgPoint2dLocFunc locfunc,
+                                    VsgPoint2dDistFunc dist,
+                                    VsgRegion2dLocFunc region_locfunc,
+                                    guint maxbox);
+void vsg_prtree2d_free (VsgPRTree2d *prtree);
+gint vsg_vector2d_vector2d_locfunc (const VsgVector2d *candidate, const VsgVector2d *center);
+gdouble vsg_vector2d_dist (const VsgVector2d *one, const VsgVector2d *other);
+
 G_END_DECLS
 
 #endif

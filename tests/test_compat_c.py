@@ -26,19 +26,29 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "c", "newton_compat.c")
 
 
-@pytest.fixture(scope="module")
-def exe(tmp_path_factory):
+def compile_c(tmp_path_factory, src, name):
     if shutil.which("gcc") is None:
         pytest.skip("gcc not available")
     import aran_gb300
     aran_gb300.load()
     libdir = os.path.dirname(aran_gb300.LIB_PATH)
-    out = str(tmp_path_factory.mktemp("compat") / "newton_compat")
-    cmd = ["gcc", "-std=c11", "-O2", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"),
-           SRC, "-L" + libdir, "-laran_gpu", "-Wl,-rpath," + libdir, "-lm", "-o", out]
+    out = str(tmp_path_factory.mktemp("compat") / name)
+    cmd = ["gcc", "-std=gnu11", "-O2", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"),
+           src, "-L" + libdir, "-laran_gpu", "-Wl,-rpath," + libdir, "-lm", "-o", out]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     return out
+
+
+@pytest.fixture(scope="module")
+def exe(tmp_path_factory):
+    return compile_c(tmp_path_factory, SRC, "newton_compat")
+
+
+@pytest.fixture(scope="module")
+def exe2d(tmp_path_factory):
+    return compile_c(tmp_path_factory, os.path.join(ROOT, "tests", "c", "cauchy_compat.c"),
+                     "cauchy_compat")
 
 
 def run(exe, *args):
@@ -59,6 +69,18 @@ def test_no_device_refuses(exe):
     except ImportError:
         pass
     rc, out = run(exe, 1000, 8, "rotate", "field", "fp64")
+    assert rc == 2, out
+    assert "error:" in out and "CUDA" in out
+
+
+def test_no_device_refuses_2d(exe2d):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    rc, out = run(exe2d, 240, 20, 1, "circle")
     assert rc == 2, out
     assert "error:" in out and "CUDA" in out
 
@@ -106,3 +128,28 @@ def test_refused_solves_leave_points_untouched(exe, args, msg):
     rc, out = run(exe, *args)
     assert rc == 2, out
     assert msg in out
+
+
+# tests/dummypot.at (np, order, maxbox, distribution, error limit) through the
+# LibAran 2D API, plus the series checks of tests/laurent.c (1e-7) and
+# tests/p2l2.c (1e-9) run through aran_laurent_seriesd_* on the GPU
+DUMMYPOT_AT = [
+    (2400, 20, 1, "circle", 1e-6),
+    (240, 40, 1, "circle", 1e-8),
+    (240, 20, 1, "random", 1e-6),
+    (240, 20, 10, "circle", 1e-8),
+    (2400, 20, 10, "circle", 1e-6),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,order,maxbox,dist,tol", DUMMYPOT_AT)
+def test_cauchy_program(exe2d, n, order, maxbox, dist, tol):
+    rc, out = run(exe2d, n, order, maxbox, dist)
+    assert rc == 0, out
+    v = parse(out)
+    assert v["maxerr"] < tol, out
+    assert v["laurent"] < 1e-7 and v["translate"] < 1e-7 and v["taylor"] < 1e-7, out
+    assert v["p2l"] < 1e-9, out
+    assert v["host_calls"] == 0
+    assert v["p2m"] == n and v["l2p"] == n and v["p2p"] > 0
