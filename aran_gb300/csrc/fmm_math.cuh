@@ -32,7 +32,7 @@
 namespace aran {
 
 constexpr int kKeyBits = 21;     // quantisation bits per axis (63-bit keys)
-constexpr int kMaxOrder = 20;    // largest supported p
+constexpr int kMaxOrder = 30;    // largest supported p
 constexpr double kPi = 3.1415926535897932384626433832795028841971693993751;
 
 FMM_HD int tri(int l) { return (l * (l + 1)) / 2; }

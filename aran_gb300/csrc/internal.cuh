@@ -206,4 +206,11 @@ void copy_expansions(AranGpuSolver3d *s, double *mult, double *local);
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
+// lets a kernel use more than the default 48 KB of dynamic shared memory
+template <typename K>
+void smem_opt_in(K kernel, size_t bytes) {
+  if (bytes > 48 * 1024)
+    ACHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
 }  // namespace aran

@@ -16,7 +16,9 @@
 // source at that offset.  The copies are double-buffered (mbarrier
 // completion), so the next offset's table streams in while the current one
 // is applied.  Every mbarrier wait is bounded; a wait that gives up sets
-// the error word and the CTA stops issuing copies.
+// the error word and the CTA stops issuing copies.  At orders whose tables
+// do not fit in shared memory (NST = 0) the warps read the offset tables
+// and vertical factors straight from global memory (L2-resident).
 #include "internal.cuh"
 
 namespace aran {
@@ -108,6 +110,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   // shared layout: NST tables | full[NST] | empty[NST] | vertical factors
   // (m-major) | per-warp buffers | 6x6x6 source grid | offset mask | active list
+  // (NST = 0: no tables, barriers or vertical factors in shared memory)
   size_t off = 0;
   T *tab = reinterpret_cast<T *>(smem_raw);
   off += (size_t)NST * D.stride * sizeof(T);
@@ -116,7 +119,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
   uint64_t *empty = full + NST;
   off += 2 * NST * sizeof(uint64_t);
   T *vtm = reinterpret_cast<T *>(smem_raw + off);
-  off += (size_t)nl * p * sizeof(T);
+  if (NST > 0) off += (size_t)nl * p * sizeof(T);
   off = (off + 15) & ~(size_t)15;
   cplx<T> *wbuf = reinterpret_cast<cplx<T> *>(smem_raw + off);
   off += (size_t)kSibWarps * (nm + nl) * sizeof(cplx<T>);
@@ -136,11 +139,12 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
   for (int i = threadIdx.x; i < 216; i += blockDim.x) grid[i] = -1;
   if (threadIdx.x < 10) mask[threadIdx.x] = 0u;
   // vertical factors, m-major slot k: vtm[n * nl + k]
-  for (int i = threadIdx.x; i < nl * p; i += blockDim.x) {
-    int k = i % nl, n = i / nl, l, m;
-    mmajor_lm(k, p, l, m);
-    vtm[i] = vt_g[tri(l, m) * p + n];
-  }
+  if (NST > 0)
+    for (int i = threadIdx.x; i < nl * p; i += blockDim.x) {
+      int k = i % nl, n = i / nl, l, m;
+      mmajor_lm(k, p, l, m);
+      vtm[i] = vt_g[tri(l, m) * p + n];
+    }
   for (int k = threadIdx.x; k < nl; k += blockDim.x) {
     int l, m;
     mmajor_lm(k, p, l, m);
@@ -149,7 +153,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
     lm[2 * k] = lm_g[2 * k];
     lm[2 * k + 1] = lm_g[2 * k + 1];
   }
-  if (threadIdx.x == 0) {
+  if (NST > 0 && threadIdx.x == 0) {
     for (int b = 0; b < NST; ++b) {
       mbar_init(&full[b], 1);
       mbar_init(&empty[b], kSibWarps);
@@ -203,10 +207,10 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
 
   if (w == kSibWarps) {
     // producer warp: stream the offset tables through the NST-slot ring
-    if (lane == 0)
+    if (NST > 0 && lane == 0)
       for (int i = 0; i < nact; ++i) {
-        const int b = i % NST;
-        if (i >= NST && !mbar_wait(&empty[b], ((i / NST) - 1) & 1)) {
+        const int b = i % (NST > 0 ? NST : 1);
+        if (i >= NST && !mbar_wait(&empty[b], ((i / (NST > 0 ? NST : 1)) - 1) & 1)) {
           atomicExch(err, 1);
           break;
         }
@@ -246,8 +250,8 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
   prefetch();
 
   for (int i = 0; i < nact; ++i) {
-    const int b = i % NST;
-    if (!mbar_wait(&full[b], (i / NST) & 1)) {
+    const int b = i % (NST > 0 ? NST : 1);
+    if (NST > 0 && !mbar_wait(&full[b], (i / (NST > 0 ? NST : 1)) & 1)) {
       atomicExch(err, 1);
       break;
     }
@@ -258,7 +262,8 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
       for (int r = 0; r < R; ++r) cur[r] = pre[r];
       find_next(i + 1);
       prefetch();
-      const T *tb = tab + (size_t)b * D.stride;
+      const T *tb = NST > 0 ? tab + (size_t)b * D.stride
+                            : dirs + (size_t)c_dir_codes[active[i]] * D.stride;
       const T *ph = tb + D.ph;
       const T *EOf = tb + D.ef;
       const T *EOi = tb + D.ei;
@@ -310,13 +315,15 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
         int k = lane + 32 * r;
         if (k < nl) {
           const int l = vmap[2 * k], m = vmap[2 * k + 1];
-          const T *vcol = vtm + k;
+          // factor of source degree n: vcol[n * vs]
+          const T *vcol = NST > 0 ? vtm + k : vt_g + tri(l, m) * p;
+          const int vs = NST > 0 ? nl : 1;
           const cplx<T> *rv = rot;
           T re0 = 0, im0 = 0, re1 = 0, im1 = 0;
           int n = m;
           for (; n + 1 < p; n += 2) {
-            T f0 = vcol[n * nl] * rp[l + n + 1];
-            T f1 = vcol[(n + 1) * nl] * rp[l + n + 2];
+            T f0 = vcol[n * vs] * rp[l + n + 1];
+            T f1 = vcol[(n + 1) * vs] * rp[l + n + 2];
             cplx<T> a0 = rv[tri(n, m)], a1 = rv[tri(n + 1, m)];
             re0 += f0 * a0.re;
             im0 += f0 * a0.im;
@@ -324,7 +331,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
             im1 += f1 * a1.im;
           }
           if (n < p) {
-            T f0 = vcol[n * nl] * rp[l + n + 1];
+            T f0 = vcol[n * vs] * rp[l + n + 1];
             cplx<T> a0 = rv[tri(n, m)];
             re0 += f0 * a0.re;
             im0 += f0 * a0.im;
@@ -368,7 +375,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
       }
     }
     __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[b]);
+    if (NST > 0 && lane == 0) mbar_arrive(&empty[b]);
   }
   if (tvalid && nact > 0) {
     const T ih = (T)(ldexp(1.0, depth[t]) / scale_e);
@@ -408,7 +415,7 @@ size_t m2l_smem(int p, int stride) {
   size_t off = (size_t)NST * stride * sizeof(T);
   off = (off + 15) & ~(size_t)15;
   off += 2 * NST * sizeof(uint64_t);
-  off += (size_t)nl * p * sizeof(T);
+  if (NST > 0) off += (size_t)nl * p * sizeof(T);
   off = (off + 15) & ~(size_t)15;
   off += (size_t)kSibWarps * (nm + nl) * sizeof(cplx<T>);
   off += 216 * sizeof(int) + 10 * sizeof(unsigned) + 320 * sizeof(uint16_t) + 4 * nl;
@@ -456,9 +463,13 @@ void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const cplx<T> *mult, cplx<T> 
   } else if (nl <= 160) {
     if (try_launch<T, 3, 5>(s, tb, D, mult, loc, st, dev_smem)) return;
     if (try_launch<T, 1, 5>(s, tb, D, mult, loc, st, dev_smem)) return;
+  } else if (nl <= 256) {
+    if (try_launch<T, 3, 8>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 8>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 0, 8>(s, tb, D, mult, loc, st, dev_smem)) return;
   } else {
-    if (try_launch<T, 3, kMaxRounds>(s, tb, D, mult, loc, st, dev_smem)) return;
     if (try_launch<T, 1, kMaxRounds>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 0, kMaxRounds>(s, tb, D, mult, loc, st, dev_smem)) return;
   }
   throw CudaError{cudaErrorInvalidConfiguration, "M2L shared memory exceeds the device limit"};
 }

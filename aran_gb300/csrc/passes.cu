@@ -450,6 +450,7 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   {
     const int WPB = 4;
     size_t sm = (2 * nl + p + 2) * sizeof(T) + (size_t)WPB * nm * sizeof(cplx<T>) + 64;
+    smem_opt_in(k_p2m<T>, sm);
     k_p2m<T><<<ceil_div(t.nleaves, WPB), WPB * 32, sm, st>>>(
         t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr, t.depth.ptr, rel, p, tb.rec.ptr,
         tb.p2mf.ptr, s->scale_e, mult);
@@ -465,6 +466,7 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
     DirOffsets D = offsets<T>(p, 1);
     const int WPB = 4;
     size_t sm = ((2 * nl + 15) & ~15) + (size_t)WPB * 2 * nm * sizeof(cplx<T>) + 64;
+    smem_opt_in(k_m2m_rotate<T>, sm);
     for (int d = t.nlevels - 2; d >= 0; --d) {
       if (t.level_internal[d] == 0) continue;
       int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
@@ -488,6 +490,7 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
     DirOffsets D = offsets<T>(p, 2);
     const int WPB = 4;
     size_t sm = ((2 * nl + 15) & ~15) + (size_t)WPB * 2 * nl * sizeof(cplx<T>) + 64;
+    smem_opt_in(k_l2l_rotate<T>, sm);
     for (int d = 3; d < t.nlevels; ++d) {
       int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
       k_l2l_rotate<T><<<ceil_div(cnt, WPB), WPB * 32, sm, st>>>(
@@ -503,6 +506,8 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   ACHECK(cudaEventRecord(s->ev[2 * Stage::L2P], st));
   {
     size_t sm = ((2 * nl + 1) & ~1) * sizeof(T) + (size_t)(nl + nm + p * p) * sizeof(cplx<T>) + 64;
+    smem_opt_in(k_l2p<T, true>, sm);
+    smem_opt_in(k_l2p<T, false>, sm);
     if (field)
       k_l2p<T, true><<<t.nleaves, 64, sm, st>>>(t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
                                                  t.depth.ptr, rel, p, tb.rec.ptr, tb.gz.ptr,

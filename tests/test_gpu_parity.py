@@ -214,3 +214,55 @@ def test_1m_uniform_subset_vs_direct(aran, uniform_1m, precision, tol):
         pot, fld = s.solve(x, q)
     assert rel_l2(pot[tgt], rp) < tol
     assert rel_l2(fld[tgt], rf) < tol
+
+
+# tests/newtonpot3.at and tests/newtonfield3.at: (np, order, maxbox,
+# distribution) with every flavour that runs on the GPU, FP64, per-particle
+# error |acc - sum| / max(|acc|, |sum|) <= 1e-3 against the direct sum
+# (tests/newtonpot3.c:680-705).  The circle has radius 0.999 in z = 0 with
+# densities 1/np; "random" is uniform in [-0.999, 0.999]^3 with densities
+# U[0, 2/np]; the box is [-1, 1]^3.
+NEWTON_AT = [
+    (12, 20, 1, "circle"),
+    (24, 24, 1, "circle"),
+    (24, 24, 1, "random"),
+    (240, 24, 10, "circle"),
+    (2400, 24, 100, "circle"),
+]
+
+
+def newton_points(n, dist):
+    if dist == "circle":
+        return W.circle(n)
+    rng = np.random.default_rng(n)
+    return rng.uniform(-0.999, 0.999, (n, 3)), rng.uniform(0.0, 2.0 / n, n)
+
+
+@pytest.mark.parametrize("flavour", ["rotate", "kkylin"])
+@pytest.mark.parametrize("n,order,maxbox,dist", NEWTON_AT)
+def test_newton_at_cases(aran, oracle, flavour, n, order, maxbox, dist):
+    x, q = newton_points(n, dist)
+    lb, ub = (-1, -1, -1), (1, 1, 1)
+    with aran.Solver3d(lb, ub, maxbox=maxbox, order=order, flavour=flavour, field=True,
+                       precision="fp64") as s:
+        pot, fld = s.solve(x, q)
+        st = s.get_stats()
+    rp, rf = oracle.direct(x, q)
+    ep = np.abs(pot - rp) / np.maximum(np.abs(pot), np.abs(rp))
+    nf, nr = np.linalg.norm(fld, axis=1), np.linalg.norm(rf, axis=1)
+    ef = np.linalg.norm(fld - rf, axis=1) / np.maximum(np.maximum(nf, nr), 1e-300)
+    assert ep.max() < 1e-3
+    assert ef.max() < 1e-3
+    opot, ost = oracle.solve(x, q, order=order, maxbox=maxbox, flavour=flavour, field=False,
+                             lb=lb, ub=ub)
+    assert rel_l2(pot, opot) < FP64_TOL
+    assert st == ost
+
+
+def test_order_30_mixed(aran, oracle):
+    x, q = W.uniform(6000, 31)
+    with aran.Solver3d((0, 0, 0), (1, 1, 1), maxbox=16, order=30, field=True,
+                       precision="mixed") as s:
+        pot, fld = s.solve(x, q)
+    opot, _ = oracle.solve(x, q, order=30, maxbox=16, field=False, lb=(0, 0, 0), ub=(1, 1, 1))
+    assert rel_l2(pot, opot) < MIXED_TOL
