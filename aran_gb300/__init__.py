@@ -50,7 +50,7 @@ class AranError(RuntimeError):
 class Config3d(C.Structure):
     _fields_ = [("lb", C.c_double * 3), ("ub", C.c_double * 3), ("maxbox", C.c_int),
                 ("order", C.c_int), ("flavour", C.c_int), ("field", C.c_int),
-                ("precision", C.c_int), ("max_depth", C.c_int)]
+                ("precision", C.c_int), ("max_depth", C.c_int), ("semifar_threshold", C.c_int)]
 
 
 class Config2d(C.Structure):
@@ -145,7 +145,8 @@ def _ptr(a):
 
 
 def make_config(lbound=(0.0, 0.0, 0.0), ubound=(1.0, 1.0, 1.0), *, maxbox=64, order=12,
-                flavour="rotate", field=True, precision="fp64", max_depth=21) -> Config3d:
+                flavour="rotate", field=True, precision="fp64", max_depth=21,
+                semifar_threshold=0) -> Config3d:
     cfg = Config3d()
     for k in range(3):
         cfg.lb[k], cfg.ub[k] = float(lbound[k]), float(ubound[k])
@@ -154,6 +155,7 @@ def make_config(lbound=(0.0, 0.0, 0.0), ubound=(1.0, 1.0, 1.0), *, maxbox=64, or
     cfg.field = int(bool(field))
     cfg.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     cfg.max_depth = int(max_depth)
+    cfg.semifar_threshold = int(semifar_threshold)
     return cfg
 
 
@@ -230,20 +232,18 @@ class Solver3d:
     ``vsg_prtree3d_new_full``; ``order`` is p of
     ``aran_development3d_new (0, p)``; ``flavour`` picks the M2M/M2L/L2L
     family; ``field`` selects newtonfield3 (potential + field) over newtonpot3
-    (potential only); ``precision`` is "fp64" (plain path) or "mixed".
+    (potential only); ``precision`` is "fp64" (plain path) or "mixed";
+    ``semifar_threshold`` > 0 turns on the semifar P2L/M2P interactions of
+    ``aran_solver3d_set_functions_full`` for nodes holding more points.
     """
 
     def __init__(self, lbound=(0.0, 0.0, 0.0), ubound=(1.0, 1.0, 1.0), *, maxbox=64, order=12,
-                 flavour="rotate", field=True, precision="fp64", max_depth=21):
+                 flavour="rotate", field=True, precision="fp64", max_depth=21,
+                 semifar_threshold=0):
         L = load()
-        cfg = Config3d()
-        for k in range(3):
-            cfg.lb[k], cfg.ub[k] = float(lbound[k]), float(ubound[k])
-        cfg.maxbox, cfg.order = int(maxbox), int(order)
-        cfg.flavour = FLAVOURS[flavour] if isinstance(flavour, str) else int(flavour)
-        cfg.field = int(bool(field))
-        cfg.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
-        cfg.max_depth = int(max_depth)
+        cfg = make_config(lbound, ubound, maxbox=maxbox, order=order, flavour=flavour,
+                          field=field, precision=precision, max_depth=max_depth,
+                          semifar_threshold=semifar_threshold)
         self.cfg = cfg
         self.order = cfg.order
         self.field = bool(field)

@@ -286,6 +286,15 @@ void aran_solver3d_foreach_point(AranSolver3d *solver, GFunc func, gpointer user
   for (VsgPoint3 p : solver->points) func(p, user_data);
 }
 
+// (p2l + m2p) / p2p cost per point on the GPU kernels, from their flop
+// counts: P2L 8 tri(p+1), M2P with gradient 24 tri(p), P2P 20 per pair (the
+// reference times the three callbacks instead, aransolver3d.c:1090-1127)
+guint aran_solver3d_optimal_semifar_threshold(AranSolver3d *solver) {
+  if (!solver || !solver->devel || !solver->p2l || !solver->m2p) return G_MAXUINT;
+  int p = solver->devel->negdeg;
+  return (guint)((8 * (p + 1) * (p + 2) / 2 + 24 * p * (p + 1) / 2) / 20);
+}
+
 void aran_solver3d_set_newton_layout(AranSolver3d *solver, int kind, size_t pos_offset,
                                      size_t charge_offset, size_t result_offset) {
   if (!solver) return;
@@ -348,6 +357,13 @@ int aran_solver3d_solve_try(AranSolver3d *solver) {
   cfg.field = solver->kind == ARAN_NEWTON_FIELD;
   cfg.precision = solver->precision;
   cfg.max_depth = 0;
+  // semifar only with p2l and m2p (aransolver3d.c:1152-1160): G_MAXUINT
+  // turns it off, 0 asks for the optimal threshold
+  if (solver->p2l && solver->m2p && solver->semifar_threshold != G_MAXUINT) {
+    guint t = solver->semifar_threshold ? solver->semifar_threshold
+                                        : aran_solver3d_optimal_semifar_threshold(solver);
+    cfg.semifar_threshold = t > 0x7fffffffu ? 0 : (int)t;
+  }
   if (!solver->gpu || std::memcmp(&cfg, &solver->gpu_cfg, sizeof(cfg)) != 0) {
     if (solver->gpu) aran_gpu_solver3d_destroy(solver->gpu);
     solver->gpu = nullptr;

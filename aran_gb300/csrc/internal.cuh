@@ -106,6 +106,9 @@ struct DevTree {
   DBuf<int2> leaf_be;                 // particle [begin, end) per leaf ordinal
   DBuf<float4> leaf_chi, leaf_clo;    // FP32 leaf centre split hi + lo; chi.w = close-pair r^2
   DBuf<int4> big_items;               // (leaf, lf_a, lf_b, 0): chunks of heavy near ranges
+  DBuf<int> semi_off;                 // CSR over leaves of semifar nodes (threshold > 0)
+  DBuf<int> semi_node, semi_leaf;     // per semifar pair: deep node, coarse leaf ordinal
+  int n_semi = 0;
   DBuf<int> parents;                  // internal nodes of depth >= 1 (their children take M2L)
   int n_parents = 0;
   int n_big = 0;
@@ -202,6 +205,10 @@ constexpr int kBigRange = 2048;   // near ranges above this many particles are c
 void build_p2p_work(AranGpuSolver3d *s);
 void launch_p2p(AranGpuSolver3d *s, cudaStream_t st);
 void compute_stats(AranGpuSolver3d *s);
+// semifar.cu: P2L of coarse-leaf points into semifar nodes' locals (before
+// L2L) and M2P of those nodes' multipoles to the points (after L2P)
+void launch_semifar_p2l(AranGpuSolver3d *s, cudaStream_t st);
+void launch_semifar_m2p(AranGpuSolver3d *s, cudaStream_t st);
 void copy_expansions(AranGpuSolver3d *s, double *mult, double *local);
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }

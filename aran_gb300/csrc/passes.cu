@@ -388,10 +388,16 @@ __global__ void k_scatter(int64_t n, const int *__restrict__ perm, const double 
 __global__ void k_stats(int nn, int nleaves, const int *__restrict__ begin, const int *__restrict__ end,
                         const int *__restrict__ parent, const int *__restrict__ leaf_node,
                         const int *__restrict__ near_off, const int *__restrict__ near_rng,
+                        int nsemi, const int *__restrict__ semi_leaf,
                         unsigned long long *__restrict__ st) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long m2m = 0, p2p2 = 0;
   if (i < nn && end[i] > begin[i] && parent[i] >= 0) m2m = 1;
+  if (i < nsemi) {
+    // semifar_func counts the coarse leaf's points once for p2l and m2p
+    int a = leaf_node[semi_leaf[i]];
+    atomicAdd(&st[2], (unsigned long long)(end[a] - begin[a]));
+  }
   if (i < nleaves) {
     int node = leaf_node[i];
     long long nt = end[node] - begin[node];
@@ -482,6 +488,7 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L], st));
   if (kk) kkylin_pass(s, 1);
   else launch_m2l(s, st);
+  launch_semifar_p2l(s, st);
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L + 1], st));
   // L2L, from depth 3 (depth 0-1 locals are zero: no far pairs above depth 2)
   ACHECK(cudaEventRecord(s->ev[2 * Stage::L2L], st));
@@ -521,6 +528,7 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
     ACHECK(cudaGetLastError());
     s->launches++;
   }
+  launch_semifar_m2p(s, st);
   ACHECK(cudaEventRecord(s->ev[2 * Stage::L2P + 1], st));
 }
 
@@ -544,14 +552,16 @@ void scatter_outputs(AranGpuSolver3d *s, double *pot, double *fld) {
 
 void compute_stats(AranGpuSolver3d *s) {
   DevTree &t = s->tree;
-  s->stats_dev.reserve(2);
-  ACHECK(cudaMemsetAsync(s->stats_dev.ptr, 0, 2 * sizeof(unsigned long long), s->s0));
+  s->stats_dev.reserve(3);
+  ACHECK(cudaMemsetAsync(s->stats_dev.ptr, 0, 3 * sizeof(unsigned long long), s->s0));
   int nmax = t.nnodes > t.nleaves ? t.nnodes : t.nleaves;
+  if (t.n_semi > nmax) nmax = t.n_semi;
   k_stats<<<ceil_div(nmax, 256), 256, 0, s->s0>>>(t.nnodes, t.nleaves, t.begin.ptr, t.end.ptr,
                                                   t.parent.ptr, t.leaf_node.ptr, t.near_off.ptr,
-                                                  t.near_rng.ptr, s->stats_dev.ptr);
+                                                  t.near_rng.ptr, t.n_semi, t.semi_leaf.ptr,
+                                                  s->stats_dev.ptr);
   ACHECK(cudaGetLastError());
-  unsigned long long h[2];
+  unsigned long long h[3];
   ACHECK(cudaMemcpyAsync(h, s->stats_dev.ptr, sizeof(h), cudaMemcpyDeviceToHost, s->s0));
   ACHECK(cudaStreamSynchronize(s->s0));
   int64_t *st = s->stats;
@@ -563,6 +573,8 @@ void compute_stats(AranGpuSolver3d *s) {
   st[4] = t.n_far;           // m2l
   st[5] = (int64_t)h[0];     // l2l
   st[6] = t.n;               // l2p
+  st[7] = (int64_t)h[2];     // p2l (semifar)
+  st[8] = (int64_t)h[2];     // m2p (semifar)
 }
 
 namespace {

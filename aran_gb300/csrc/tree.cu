@@ -228,40 +228,95 @@ __global__ void k_leaf_ranges(int nn, const int *__restrict__ begin, const int *
   }
 }
 
-// near ranges of leaf ordinal L; mode 0 counts, mode 1 writes
+// box of node y (depth >= depth of a) touches the box of node a
+__device__ __forceinline__ bool adjacent_ml(const int *ijk, const uint8_t *depth, int a, int y) {
+  const int sh = depth[y] - depth[a];
+  for (int k = 0; k < 3; ++k) {
+    long long lo = ((long long)ijk[3 * a + k] << sh) - 1;
+    long long hi = (long long)(ijk[3 * a + k] + 1) << sh;
+    long long v = ijk[3 * y + k];
+    if (v < lo || v > hi) return false;
+  }
+  return true;
+}
+
+// Near ranges (and semifar nodes) of leaf ordinal L; mode 0 counts, mode 1
+// writes.  With a semifar threshold T > 0 an internal colleague's subtree is
+// walked: descendants touching the leaf are walked further (near when they
+// are leaves), a descendant that does not touch it is a semifar node of the
+// leaf when it holds more than T points and a near range otherwise; a
+// coarser leaf colleague of an ancestor is near unless the shallowest node
+// between that ancestor and L that does not touch it holds more than T
+// points (it then reaches L through its own semifar P2L/M2P).
 __global__ void k_near(int nleaves, const int *__restrict__ leaf_node, const int *__restrict__ begin,
                        const int *__restrict__ end, const int *__restrict__ child,
                        const int *__restrict__ parent, const int *__restrict__ col,
                        const int *__restrict__ ncol, const int *__restrict__ lf_begin,
-                       const int *__restrict__ lf_end, int *__restrict__ near_cnt,
-                       const int *__restrict__ near_off, int *__restrict__ near_rng, int mode) {
+                       const int *__restrict__ lf_end, const int *__restrict__ ijk,
+                       const uint8_t *__restrict__ depth, int T, int *__restrict__ near_cnt,
+                       const int *__restrict__ near_off, int *__restrict__ near_rng,
+                       int *__restrict__ semi_cnt, const int *__restrict__ semi_off,
+                       int *__restrict__ semi_node, int *__restrict__ semi_leaf, int mode) {
   int L = blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= nleaves) return;
   int node = leaf_node[L];
-  int k = 0;
+  int k = 0, ks = 0;
   int w = mode ? near_off[L] : 0;
-  int nc = ncol[node];
-  for (int j = 0; j < nc; ++j) {
-    int q = col[27 * node + j];
+  int ws = (mode && T > 0) ? semi_off[L] : 0;
+  auto emit = [&](int q) {
     if (mode) {
       near_rng[2 * (w + k)] = lf_begin[q];
       near_rng[2 * (w + k) + 1] = lf_end[q];
     }
     ++k;
+  };
+  int nc = ncol[node];
+  for (int j = 0; j < nc; ++j) {
+    int q = col[27 * node + j];
+    if (T <= 0 || child[q] < 0) {
+      emit(q);
+      continue;
+    }
+    // depth-first walk of q's subtree (at most 7 pending siblings per level)
+    int stk[8 * 22];
+    int sp = 0;
+    for (int o = 7; o >= 0; --o) stk[sp++] = child[q] + o;
+    while (sp > 0) {
+      int d = stk[--sp];
+      if (end[d] == begin[d]) continue;
+      if (adjacent_ml(ijk, depth, node, d)) {
+        if (child[d] < 0) emit(d);
+        else
+          for (int o = 7; o >= 0; --o) stk[sp++] = child[d] + o;
+      } else if (end[d] - begin[d] > T) {
+        if (mode) {
+          semi_node[ws + ks] = d;
+          semi_leaf[ws + ks] = L;
+        }
+        ++ks;
+      } else {
+        emit(d);
+      }
+    }
   }
   for (int a = parent[node]; a >= 0; a = parent[a]) {
     int na = ncol[a];
     for (int j = 0; j < na; ++j) {
       int q = col[27 * a + j];
       if (child[q] >= 0 || end[q] == begin[q]) continue;
-      if (mode) {
-        near_rng[2 * (w + k)] = lf_begin[q];
-        near_rng[2 * (w + k) + 1] = lf_end[q];
+      if (T > 0) {
+        int x = -1;
+        for (int y = node; y != a; y = parent[y])
+          if (!adjacent_ml(ijk, depth, q, y)) x = y;
+        if (x >= 0 && end[x] - begin[x] > T) continue;
       }
-      ++k;
+      emit(q);
     }
   }
-  if (!mode) near_cnt[L] = k;
+  if (!mode) {
+    near_cnt[L] = k;
+    if (T > 0) semi_cnt[L] = ks;
+  }
 }
 
 __global__ void k_parent_flags(int nn, const int *__restrict__ child, const uint8_t *__restrict__ depth,
@@ -483,24 +538,44 @@ void build_lists(AranGpuSolver3d *s) {
                                                         s->rel64.ptr);
   }
   s->launches++;
-  // near ranges per leaf
+  // near ranges (and semifar nodes) per leaf
+  const int T = s->cfg.semifar_threshold;
   t.near_off.reserve(nleaves + 1);
+  int *semi_cnt = nullptr;
+  if (T > 0) {
+    t.semi_off.reserve(nleaves + 1);
+    cntbuf.reserve(2 * ((size_t)nleaves + 1) + (size_t)n + 1);
+    semi_cnt = cntbuf.ptr + nleaves + 1;
+  }
   k_near<<<ceil_div(nleaves, TB), TB, 0, st>>>(nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
                                                 t.child.ptr, t.parent.ptr, t.col.ptr, t.ncol.ptr,
-                                                t.lf_begin.ptr, t.lf_end.ptr, cntbuf.ptr, nullptr,
-                                                nullptr, 0);
+                                                t.lf_begin.ptr, t.lf_end.ptr, t.ijk.ptr, t.depth.ptr,
+                                                T, cntbuf.ptr, nullptr, nullptr, semi_cnt, nullptr,
+                                                nullptr, nullptr, 0);
   s->launches++;
   ACHECK(cudaMemsetAsync(cntbuf.ptr + nleaves, 0, sizeof(int), st));
   exclusive_scan(s, cntbuf.ptr, t.near_off.ptr, nleaves + 1, st);
   int nrng = 0;
   ACHECK(cudaMemcpyAsync(&nrng, t.near_off.ptr + nleaves, sizeof(int), cudaMemcpyDeviceToHost, st));
+  int nsemi = 0;
+  if (T > 0) {
+    ACHECK(cudaMemsetAsync(semi_cnt + nleaves, 0, sizeof(int), st));
+    exclusive_scan(s, semi_cnt, t.semi_off.ptr, nleaves + 1, st);
+    ACHECK(cudaMemcpyAsync(&nsemi, t.semi_off.ptr + nleaves, sizeof(int), cudaMemcpyDeviceToHost, st));
+  }
   ACHECK(cudaStreamSynchronize(st));
   t.n_near_rng = nrng;
+  t.n_semi = nsemi;
   t.near_rng.reserve(2 * (size_t)nrng + 2);
+  if (T > 0) {
+    t.semi_node.reserve(nsemi + 1);
+    t.semi_leaf.reserve(nsemi + 1);
+  }
   k_near<<<ceil_div(nleaves, TB), TB, 0, st>>>(nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
                                                 t.child.ptr, t.parent.ptr, t.col.ptr, t.ncol.ptr,
-                                                t.lf_begin.ptr, t.lf_end.ptr, nullptr,
-                                                t.near_off.ptr, t.near_rng.ptr, 1);
+                                                t.lf_begin.ptr, t.lf_end.ptr, t.ijk.ptr, t.depth.ptr,
+                                                T, nullptr, t.near_off.ptr, t.near_rng.ptr, nullptr,
+                                                t.semi_off.ptr, t.semi_node.ptr, t.semi_leaf.ptr, 1);
   s->launches++;
   // internal nodes of depth >= 1: one M2L block each (their children)
   {

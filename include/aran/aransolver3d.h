@@ -78,6 +78,9 @@ void aran_solver3d_insert_point (AranSolver3d *solver, VsgPoint3 point);
 gboolean aran_solver3d_remove_point (AranSolver3d *solver, VsgPoint3 point);
 void aran_solver3d_foreach_point (AranSolver3d *solver, GFunc func, gpointer user_data);
 void aran_solver3d_solve (AranSolver3d *solver);
+/* the semifar threshold used when set_functions_full was given 0
+ * (aran/aransolver3d.c:1090-1127); G_MAXUINT without p2l/m2p */
+guint aran_solver3d_optimal_semifar_threshold (AranSolver3d *solver);
 
 /* Additive: where the Newton data sits in the caller's point struct
  * (position: VsgVector3d at pos_offset, charge: gdouble at charge_offset,

@@ -57,6 +57,9 @@ typedef struct
   int field;           /* 0: potential only (newtonpot3); 1: potential + field (newtonfield3) */
   int precision;       /* ARAN_PRECISION_* */
   int max_depth;       /* tree depth limit, 1..21 (0 = 21) */
+  int semifar_threshold; /* <= 0: off; > 0: a coarse leaf against a deeper,
+                            non-touching node holding more points takes P2L/M2P
+                            instead of P2P (aran/aransolver3d.c:357-396) */
 } AranGpuConfig3d;
 
 typedef struct AranGpuSolver3d AranGpuSolver3d;

@@ -105,14 +105,15 @@ def lib():
 class SolveConfig(C.Structure):
     _fields_ = [("n", C.c_int), ("maxbox", C.c_int), ("order", C.c_int),
                 ("flavour", C.c_int), ("field", C.c_int), ("max_depth", C.c_int),
-                ("lb", C.c_double * 3), ("ub", C.c_double * 3)]
+                ("lb", C.c_double * 3), ("ub", C.c_double * 3),
+                ("semifar_threshold", C.c_int)]
 
 
 def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
-def _cfg(n, maxbox, order, flavour, field, lb, ub, max_depth=21):
+def _cfg(n, maxbox, order, flavour, field, lb, ub, max_depth=21, semifar_threshold=0):
     if isinstance(flavour, str):
         flavour = FLAVOURS[flavour]
     c = SolveConfig()
@@ -120,6 +121,7 @@ def _cfg(n, maxbox, order, flavour, field, lb, ub, max_depth=21):
     c.field, c.max_depth = int(field), max_depth
     for k in range(3):
         c.lb[k], c.ub[k] = lb[k], ub[k]
+    c.semifar_threshold = int(semifar_threshold)
     return c
 
 
@@ -214,12 +216,13 @@ def harmonics(l, theta, phi):
 
 # ------------------------------------------------------------------- solver
 def solve(xyz, q, *, order, maxbox, flavour="rotate", field=False,
-          lb=(0.0, 0.0, 0.0), ub=(1.0, 1.0, 1.0), max_depth=21):
-    """Full CPU FMM solve; returns (potential or field, stats dict)."""
+          lb=(0.0, 0.0, 0.0), ub=(1.0, 1.0, 1.0), max_depth=21, semifar_threshold=0):
+    """Full CPU FMM solve; returns (potential or field, stats dict).
+    semifar_threshold > 0 turns on P2L/M2P for nodes holding more points."""
     xyz = np.ascontiguousarray(xyz, np.float64)
     q = np.ascontiguousarray(q, np.float64)
     n = len(q)
-    cfg = _cfg(n, maxbox, order, flavour, field, lb, ub, max_depth)
+    cfg = _cfg(n, maxbox, order, flavour, field, lb, ub, max_depth, semifar_threshold)
     pot = np.zeros(n)
     fld = np.zeros((n, 3))
     st = np.zeros(NSTATS, dtype=np.int64)

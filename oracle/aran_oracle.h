@@ -81,6 +81,8 @@ typedef struct
   int field;          /* 0: potential (newtonpot3), 1: field (newtonfield3) */
   int max_depth;      /* <= 21 */
   double lb[3], ub[3];
+  int semifar_threshold;  /* <= 0: off; > 0: semifar P2L/M2P for nodes
+                             holding more points (aransolver3d.c:357-396) */
 } OrSolveConfig;
 
 /* Counters in the order of aran_solver3d_get_stats

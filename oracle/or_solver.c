@@ -15,6 +15,14 @@
  *    are FAR (2 M2L, aran/aransolver3d.c:333-354); adjacent leaves are NEAR
  *    (P2P, :254-324); a leaf against an adjacent internal node is NEAR with
  *    every non-empty leaf below that node; empty nodes take no part.
+ *  - semifar (only with p2l/m2p and a threshold T > 0): a leaf A against an
+ *    adjacent internal node walks that node's subtree instead; a descendant
+ *    D adjacent to A (touching A's box) is walked further (near if it is a
+ *    leaf), a descendant D not adjacent to A takes P2L of A's points into
+ *    D's local and M2P of D's multipole to A's points when D holds more than
+ *    T points (semifar_func, aran/aransolver3d.c:357-396; "beyond this
+ *    number of particles", :622-623), and is near with every leaf below it
+ *    otherwise.
  */
 #include "or_internal.h"
 
@@ -243,6 +251,8 @@ typedef struct
 {
   void (*far) (void *ctx, int a, int b);
   void (*near) (void *ctx, int a, int b);
+  void (*semifar) (void *ctx, int leaf, int node);   /* may be NULL */
+  int threshold;                                     /* semifar: > 0 */
   void *ctx;
   const OrTree *t;
 } Traversal;
@@ -265,6 +275,53 @@ static void near_leaves_below (const Traversal *tv, int leaf, int node)
     }
   for (c = 0; c < 8; c++)
     near_leaves_below (tv, leaf, nd->child[c]);
+}
+
+/* box of node b (depth >= depth of a) touches box of a */
+static int adjacent_ml (const OrNode *a, const OrNode *b)
+{
+  int k, sh = b->depth - a->depth;
+  for (k = 0; k < 3; k++)
+    {
+      int64_t lo = ((int64_t) a->ijk[k] << sh) - 1;
+      int64_t hi = ((int64_t) (a->ijk[k] + 1) << sh);
+      if (b->ijk[k] < lo || b->ijk[k] > hi)
+        return 0;
+    }
+  return 1;
+}
+
+/* leaf against the subtree of an adjacent internal node, semifar on */
+static void semifar_walk (const Traversal *tv, int leaf, int node)
+{
+  const OrNode *A = &tv->t->nodes[leaf], *C = &tv->t->nodes[node];
+  int c;
+  for (c = 0; c < 8; c++)
+    {
+      int d = C->child[c];
+      const OrNode *D = &tv->t->nodes[d];
+      if (cnt (D) == 0)
+        continue;
+      if (adjacent_ml (A, D))
+        {
+          if (D->leaf)
+            tv->near (tv->ctx, leaf, d);
+          else
+            semifar_walk (tv, leaf, d);
+        }
+      else if (cnt (D) > tv->threshold)
+        tv->semifar (tv->ctx, leaf, d);
+      else
+        near_leaves_below (tv, leaf, d);
+    }
+}
+
+static void leaf_vs_node (const Traversal *tv, int leaf, int node)
+{
+  if (tv->semifar && tv->threshold > 0)
+    semifar_walk (tv, leaf, node);
+  else
+    near_leaves_below (tv, leaf, node);
 }
 
 static void pair_traverse (const Traversal *tv, int a, int b)
@@ -292,12 +349,12 @@ static void pair_traverse (const Traversal *tv, int a, int b)
     }
   if (A->leaf)
     {
-      near_leaves_below (tv, a, b);
+      leaf_vs_node (tv, a, b);
       return;
     }
   if (B->leaf)
     {
-      near_leaves_below (tv, b, a);
+      leaf_vs_node (tv, b, a);
       return;
     }
   for (i = 0; i < 8; i++)
@@ -383,6 +440,41 @@ static void cb_far (void *ctx, int a, int b)
   or_to_local_series (s->cfg->flavour, &s->mult[b], B->center, &s->loc[a],
                       A->center);
   s->stats[4] += 2;
+}
+
+/* semifar_func (aran/aransolver3d.c:357-396): every point of the coarse
+ * leaf goes into the deep node's local (p2l, tests/newtonpot3.c:93-97) and
+ * takes the deep node's multipole (m2p: potential tests/newtonpot3.c:99-104,
+ * field = multipole gradient tests/newtonfield3.c:145-151) */
+static void cb_semifar (void *ctx, int leaf, int node)
+{
+  SolveCtx *s = (SolveCtx *) ctx;
+  const OrNode *A = &s->t->nodes[leaf], *D = &s->t->nodes[node];
+  int i;
+  for (i = A->begin; i < A->end; i++)
+    {
+      int o = s->t->perm[i];
+      const double *x = s->xyz + 3 * o;
+      double rel[3] = { x[0] - D->center[0], x[1] - D->center[1], x[2] - D->center[2] };
+      or_p2l_series (x, s->q[o], D->center, &s->loc[node]);
+      if (s->cfg->field)
+        {
+          double g[3];
+          or_gradient_xyz (&s->mult[node], rel, g);
+          s->fld[3 * i] += g[0];
+          s->fld[3 * i + 1] += g[1];
+          s->fld[3 * i + 2] += g[2];
+        }
+      else
+        {
+          double r, cost, sint, cosp, sinp;
+          or_to_spherical_internal (rel, &r, &cost, &sint, &cosp, &sinp);
+          s->acc[i] += creal (or_evaluate_internal (&s->mult[node], r, cost, sint, cosp,
+                                                    sinp));
+        }
+    }
+  s->stats[7] += cnt (A);
+  s->stats[8] += cnt (A);
 }
 
 /* up pass, post order: aran/aransolver3d.c:412-450 */
@@ -493,6 +585,8 @@ int or_solve (const OrSolveConfig *cfg, const double *xyz, const double *q,
   up (&s, 0);
   tv.far = cb_far;
   tv.near = cb_near;
+  tv.semifar = cb_semifar;
+  tv.threshold = cfg->semifar_threshold;
   tv.ctx = &s;
   tv.t = &t;
   pair_traverse (&tv, 0, 0);
@@ -581,6 +675,8 @@ int or_tree_lists (const OrSolveConfig *cfg, const double *xyz,
   lc.t = &t;
   tv.far = lc_far;
   tv.near = lc_near;
+  tv.semifar = NULL;
+  tv.threshold = 0;
   tv.ctx = &lc;
   tv.t = &t;
   pair_traverse (&tv, 0, 0);

@@ -266,3 +266,28 @@ def test_order_30_mixed(aran, oracle):
         pot, fld = s.solve(x, q)
     opot, _ = oracle.solve(x, q, order=30, maxbox=16, field=False, lb=(0, 0, 0), ub=(1, 1, 1))
     assert rel_l2(pot, opot) < MIXED_TOL
+
+
+# semifar P2L/M2P (aran/aransolver3d.c:357-396): on a Plummer tree (coarse
+# leaves next to deep subtrees) the GPU lists reproduce the oracle's counts
+# exactly (fewer P2P pairs, p2l = m2p points), and the results match the
+# oracle's semifar solve
+@pytest.mark.parametrize("threshold", [1, 8, 64])
+@pytest.mark.parametrize("field", [False, True])
+def test_semifar_matches_oracle(aran, oracle, threshold, field):
+    x, q = W.plummer(20000, 13)
+    lb, ub = (-1, -1, -1), (1, 1, 1)
+    kw = dict(maxbox=32, order=10, field=field)
+    with aran.Solver3d(lb, ub, precision="fp64", semifar_threshold=threshold, **kw) as s:
+        pot, fld = s.solve(x, q)
+        st = s.get_stats()
+    ref, ost = oracle.solve(x, q, order=10, maxbox=32, field=field, lb=lb, ub=ub,
+                            semifar_threshold=threshold)
+    got = fld if field else pot
+    assert ost["p2l"] > 0
+    for k in ("p2p", "p2l", "m2p", "m2l", "m2m", "l2l", "zero"):
+        assert st[k] == ost[k], k
+    assert rel_l2(got, ref) < FP64_TOL
+    with aran.Solver3d(lb, ub, precision="mixed", semifar_threshold=threshold, **kw) as s:
+        potm, fldm = s.solve(x, q)
+    assert rel_l2(fldm if field else potm, ref) < MIXED_TOL

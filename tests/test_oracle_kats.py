@@ -449,3 +449,20 @@ def test_solve2d_systems_are_independent(oracle):
         if b > a:
             one, _ = oracle.solve2d(xy[a:b], q[a:b], [0, b - a], boxes[s:s + 1], 16, 20)
             np.testing.assert_array_equal(acc[a:b], one)
+
+
+def test_semifar_keeps_the_accuracy(oracle):
+    # semifar P2L/M2P replaces P2P between a coarse leaf and deep nodes that
+    # do not touch it; the error against the direct sum stays that of the FMM
+    from aran_gb300 import workloads as W
+    x, q = W.plummer(6000, 21)
+    lb, ub = (-1, -1, -1), (1, 1, 1)
+    rp, rf = oracle.direct(x, q)
+    base, st0 = oracle.solve(x, q, order=10, maxbox=16, field=True, lb=lb, ub=ub)
+    semi, st1 = oracle.solve(x, q, order=10, maxbox=16, field=True, lb=lb, ub=ub,
+                             semifar_threshold=4)
+    e0 = np.linalg.norm(base - rf) / np.linalg.norm(rf)
+    e1 = np.linalg.norm(semi - rf) / np.linalg.norm(rf)
+    assert st1["p2l"] > 0 and st1["p2l"] == st1["m2p"] and st0["p2l"] == 0
+    assert st1["p2p"] < st0["p2p"]
+    assert e1 < 2 * e0 + 1e-9
