@@ -97,20 +97,22 @@ __device__ __forceinline__ void mmajor_lm(int k, int p, int &l, int &m) {
 constexpr int kSibWarps = 8;   // consumers: one per child of the parent
 constexpr int kMaxRounds = ((kMaxOrder + 1) * (kMaxOrder + 2) / 2 + 31) / 32;
 
-template <typename T, int NST, int R>
-__global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) k_m2l_sibling(
-    int nparents, const int *__restrict__ parents, const int *__restrict__ child,
-    const int *__restrict__ begin, const int *__restrict__ end, const int *__restrict__ col,
-    const int *__restrict__ ncol, const int *__restrict__ ijk, const uint8_t *__restrict__ depth,
-    int p, const T *__restrict__ dirs, M2LOffsets D, const T *__restrict__ vt_g,
-    const uint8_t *__restrict__ lm_g, double scale_e, const cplx<T> *__restrict__ mult,
-    cplx<T> *__restrict__ loc, int *__restrict__ err) {
+template <typename T, int NST, int R, int G>
+__global__ void __launch_bounds__(32 * (kSibWarps + 1), (sizeof(T) == 4 && G == 1) ? 3 : 2)
+    k_m2l_sibling(int nparents, const int *__restrict__ parents, const int *__restrict__ child,
+                  const int *__restrict__ begin, const int *__restrict__ end,
+                  const int *__restrict__ col, const int *__restrict__ ncol,
+                  const int *__restrict__ ijk, const uint8_t *__restrict__ depth, int p,
+                  const T *__restrict__ dirs, M2LOffsets D, const T *__restrict__ vt_g,
+                  const uint8_t *__restrict__ lm_g, double scale_e,
+                  const cplx<T> *__restrict__ mult, cplx<T> *__restrict__ loc,
+                  int *__restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int nm = tri(p), nl = tri(p + 1);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   // shared layout: NST tables | full[NST] | empty[NST] | vertical factors
-  // (m-major) | per-warp buffers | 6x6x6 source grid | offset mask | active list
-  // (NST = 0: no tables, barriers or vertical factors in shared memory)
+  // (m-major) | per-warp buffers (G columns) | G 6x6x6 source grids | offset
+  // mask | active list (NST = 0: no tables, barriers or vertical factors)
   size_t off = 0;
   T *tab = reinterpret_cast<T *>(smem_raw);
   off += (size_t)NST * D.stride * sizeof(T);
@@ -122,9 +124,9 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
   if (NST > 0) off += (size_t)nl * p * sizeof(T);
   off = (off + 15) & ~(size_t)15;
   cplx<T> *wbuf = reinterpret_cast<cplx<T> *>(smem_raw + off);
-  off += (size_t)kSibWarps * (nm + nl) * sizeof(cplx<T>);
+  off += (size_t)kSibWarps * G * (nm + nl) * sizeof(cplx<T>);
   int *grid = reinterpret_cast<int *>(smem_raw + off);
-  off += 216 * sizeof(int);
+  off += (size_t)G * 216 * sizeof(int);
   unsigned *mask = reinterpret_cast<unsigned *>(smem_raw + off);
   off += 10 * sizeof(unsigned);
   uint16_t *active = reinterpret_cast<uint16_t *>(smem_raw + off);
@@ -134,9 +136,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
   uint8_t *vmap = smem_raw + off;         // (l, m) of m-major slot k
   __shared__ int s_nact;
 
-  const int P = parents[blockIdx.x];
-  const int c0 = child[P];
-  for (int i = threadIdx.x; i < 216; i += blockDim.x) grid[i] = -1;
+  for (int i = threadIdx.x; i < G * 216; i += blockDim.x) grid[i] = -1;
   if (threadIdx.x < 10) mask[threadIdx.x] = 0u;
   // vertical factors, m-major slot k: vtm[n * nl + k]
   if (NST > 0)
@@ -161,32 +161,52 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
     fence_mbar_init();
   }
   __syncthreads();
-  const int pi = ijk[3 * P], pj = ijk[3 * P + 1], pk = ijk[3 * P + 2];
-  const int nc = ncol[P];
-  for (int e = threadIdx.x; e < nc * 8; e += blockDim.x) {
-    int q = col[27 * P + e / 8];
-    int qc = child[q];
-    if (qc < 0) continue;
-    int o = e & 7;
-    int s = qc + o;
-    if (end[s] == begin[s]) continue;
-    int gx = 2 * (ijk[3 * q] - pi + 1) + (o & 1);
-    int gy = 2 * (ijk[3 * q + 1] - pj + 1) + ((o >> 1) & 1);
-    int gz = 2 * (ijk[3 * q + 2] - pk + 1) + ((o >> 2) & 1);
-    grid[gx + 6 * (gy + 6 * gz)] = s;
+  // the G parents of this CTA: their colleagues' children fill the grids
+  for (int g = 0; g < G; ++g) {
+    const int pidx = blockIdx.x * G + g;
+    if (pidx >= nparents) break;
+    const int P = parents[pidx];
+    const int pi = ijk[3 * P], pj = ijk[3 * P + 1], pk = ijk[3 * P + 2];
+    const int nc = ncol[P];
+    for (int e = threadIdx.x; e < nc * 8; e += blockDim.x) {
+      int q = col[27 * P + e / 8];
+      int qc = child[q];
+      if (qc < 0) continue;
+      int o = e & 7;
+      int s = qc + o;
+      if (end[s] == begin[s]) continue;
+      int gx = 2 * (ijk[3 * q] - pi + 1) + (o & 1);
+      int gy = 2 * (ijk[3 * q + 1] - pj + 1) + ((o >> 1) & 1);
+      int gz = 2 * (ijk[3 * q + 2] - pk + 1) + ((o >> 2) & 1);
+      grid[g * 216 + gx + 6 * (gy + 6 * gz)] = s;
+    }
   }
   __syncthreads();
-  const int t = c0 + (w < kSibWarps ? w : 0);
-  const bool tvalid = w < kSibWarps && end[t] > begin[t];
+  // consumer warp w <-> child w of each of the G parents (column g)
+  int tg[G];
+  bool tvalid[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    const int pidx = blockIdx.x * G + g;
+    tvalid[g] = false;
+    tg[g] = 0;
+    if (w < kSibWarps && pidx < nparents) {
+      tg[g] = child[parents[pidx]] + w;
+      tvalid[g] = end[tg[g]] > begin[tg[g]];
+    }
+  }
   const int tx = 2 + (w & 1), ty = 2 + ((w >> 1) & 1), tz = 2 + ((w >> 2) & 1);
-  auto source_of = [&](int di) -> int {
+  auto source_of = [&](int g, int di) -> int {
+    if (!tvalid[g]) return -1;
     int cx = tx - c_dir_vec[3 * di], cy = ty - c_dir_vec[3 * di + 1], cz = tz - c_dir_vec[3 * di + 2];
     if (cx < 0 || cx > 5 || cy < 0 || cy > 5 || cz < 0 || cz > 5) return -1;
-    return grid[cx + 6 * (cy + 6 * cz)];
+    return grid[g * 216 + cx + 6 * (cy + 6 * cz)];
   };
-  if (tvalid)
-    for (int di = lane; di < 316; di += 32)
-      if (source_of(di) >= 0) atomicOr(&mask[di >> 5], 1u << (di & 31));
+#pragma unroll
+  for (int g = 0; g < G; ++g)
+    if (tvalid[g])
+      for (int di = lane; di < 316; di += 32)
+        if (source_of(g, di) >= 0) atomicOr(&mask[di >> 5], 1u << (di & 31));
   __syncthreads();
   for (int di = threadIdx.x; di < 316; di += blockDim.x) {
     unsigned m = mask[di >> 5];
@@ -221,30 +241,38 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
     return;
   }
 
-  // consumer warp w <-> target child w; its local lives in registers
-  cplx<T> acc[R];
+  // accumulated locals of the G targets live in registers
+  cplx<T> acc[G][R];
 #pragma unroll
-  for (int r = 0; r < R; ++r) acc[r] = cmake<T>(0, 0);
-  // src (phased multipole) and tr (translated, m-major slots) share region A
-  cplx<T> *src = wbuf + (size_t)w * (nm + nl);
-  cplx<T> *tr = src;
-  cplx<T> *rot = src + nl;
-  // the next pair's multipole is fetched one offset ahead into registers
-  cplx<T> pre[R];
-  int next_i = 0, next_s = -1;
+  for (int g = 0; g < G; ++g)
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[g][r] = cmake<T>(0, 0);
+  // column g: src (phased multipole) and tr (translated, m-major slots)
+  // share region A, rot follows
+  cplx<T> *cbuf = wbuf + (size_t)w * G * (nm + nl);
+  // the next direction's multipoles are fetched one direction ahead
+  cplx<T> pre[G][R];
+  int next_i = 0, next_s[G];
   auto find_next = [&](int from) {
-    next_s = -1;
     for (next_i = from; next_i < nact; ++next_i) {
-      next_s = tvalid ? source_of(active[next_i]) : -1;
-      if (next_s >= 0) break;
+      bool any = false;
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        next_s[g] = source_of(g, active[next_i]);
+        any |= next_s[g] >= 0;
+      }
+      if (any) break;
     }
   };
   auto prefetch = [&]() {
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      int c = lane + 32 * r;
-      pre[r] = (next_s >= 0 && c < nm) ? mult[(size_t)next_s * nm + c] : cmake<T>(0, 0);
-    }
+    for (int g = 0; g < G; ++g)
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        int c = lane + 32 * r;
+        pre[g][r] = (next_i < nact && next_s[g] >= 0 && c < nm) ? mult[(size_t)next_s[g] * nm + c]
+                                                                : cmake<T>(0, 0);
+      }
   };
   find_next(0);
   prefetch();
@@ -255,30 +283,29 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
       atomicExch(err, 1);
       break;
     }
-    const int s = (i == next_i) ? next_s : -1;
-    if (s >= 0) {
-      cplx<T> cur[R];
-#pragma unroll
-      for (int r = 0; r < R; ++r) cur[r] = pre[r];
-      find_next(i + 1);
-      prefetch();
+    if (i == next_i) {
       const T *tb = NST > 0 ? tab + (size_t)b * D.stride
                             : dirs + (size_t)c_dir_codes[active[i]] * D.stride;
       const T *ph = tb + D.ph;
       const T *EOf = tb + D.ef;
       const T *EOi = tb + D.ei;
       const T *rp = tb + D.rp;
-      // z-phase of the source multipole: e^{i m phi}
+      // z-phase of the source multipoles: e^{i m phi}
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         int c = lane + 32 * r;
         if (c < nm) {
-          cplx<T> v = cur[r];
           const int m = lm[2 * c + 1];
           T cr = ph[2 * m], ci = ph[2 * m + 1];
-          src[c] = cmake<T>(v.re * cr - v.im * ci, v.re * ci + v.im * cr);
+#pragma unroll
+          for (int g = 0; g < G; ++g) {
+            cplx<T> v = pre[g][r];
+            cbuf[g * (nm + nl) + c] = cmake<T>(v.re * cr - v.im * ci, v.re * ci + v.im * cr);
+          }
         }
       }
+      find_next(i + 1);
+      prefetch();
       __syncwarp();
       // rotation to the z axis (degrees < p)
 #pragma unroll
@@ -287,25 +314,22 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
         if (c < nm) {
           const int l = lm[2 * c], mp = lm[2 * c + 1];
           const T *col0 = EOf + 2 * (sq_off(l) + mp);
-          const cplx<T> *sv = src + tri(l);
-          T re0 = 0, im0 = 0, re1 = 0, im1 = 0;
-          int m = 0;
-          for (; m + 1 <= l; m += 2) {
-            cplx<T> x0 = sv[m], x1 = sv[m + 1];
-            const T *e0 = col0 + 2 * m * (l + 1);
-            const T *e1 = e0 + 2 * (l + 1);
-            re0 += e0[0] * x0.re;
-            im0 += e0[1] * x0.im;
-            re1 += e1[0] * x1.re;
-            im1 += e1[1] * x1.im;
+          const int so = tri(l);
+          T re[G], im[G];
+#pragma unroll
+          for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
+          for (int m = 0; m <= l; ++m) {
+            const T *e = col0 + 2 * m * (l + 1);
+            const T ee = e[0], eo = e[1];
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+              cplx<T> x = cbuf[g * (nm + nl) + so + m];
+              re[g] += ee * x.re;
+              im[g] += eo * x.im;
+            }
           }
-          if (m <= l) {
-            cplx<T> x0 = sv[m];
-            const T *e0 = col0 + 2 * m * (l + 1);
-            re0 += e0[0] * x0.re;
-            im0 += e0[1] * x0.im;
-          }
-          rot[c] = cmake<T>(re0 + re1, im0 + im1);
+#pragma unroll
+          for (int g = 0; g < G; ++g) cbuf[g * (nm + nl) + nl + c] = cmake<T>(re[g], im[g]);
         }
       }
       __syncwarp();
@@ -318,25 +342,21 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
           // factor of source degree n: vcol[n * vs]
           const T *vcol = NST > 0 ? vtm + k : vt_g + tri(l, m) * p;
           const int vs = NST > 0 ? nl : 1;
-          const cplx<T> *rv = rot;
-          T re0 = 0, im0 = 0, re1 = 0, im1 = 0;
-          int n = m;
-          for (; n + 1 < p; n += 2) {
-            T f0 = vcol[n * vs] * rp[l + n + 1];
-            T f1 = vcol[(n + 1) * vs] * rp[l + n + 2];
-            cplx<T> a0 = rv[tri(n, m)], a1 = rv[tri(n + 1, m)];
-            re0 += f0 * a0.re;
-            im0 += f0 * a0.im;
-            re1 += f1 * a1.re;
-            im1 += f1 * a1.im;
+          T re[G], im[G];
+#pragma unroll
+          for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
+          for (int n = m; n < p; ++n) {
+            const T f = vcol[n * vs] * rp[l + n + 1];
+            const int sidx = nl + tri(n, m);
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+              cplx<T> a = cbuf[g * (nm + nl) + sidx];
+              re[g] += f * a.re;
+              im[g] += f * a.im;
+            }
           }
-          if (n < p) {
-            T f0 = vcol[n * vs] * rp[l + n + 1];
-            cplx<T> a0 = rv[tri(n, m)];
-            re0 += f0 * a0.re;
-            im0 += f0 * a0.im;
-          }
-          tr[k] = cmake<T>(re0 + re1, im0 + im1);
+#pragma unroll
+          for (int g = 0; g < G; ++g) cbuf[g * (nm + nl) + k] = cmake<T>(re[g], im[g]);
         }
       }
       __syncwarp();
@@ -347,42 +367,44 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2) 
         if (c < nl) {
           const int l = lm[2 * c], mp = lm[2 * c + 1];
           const T *col0 = EOi + 2 * (sq_off(l) + mp);
+          T re[G], im[G];
+#pragma unroll
+          for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
           // slot of (l, m) in m-major order: m(p+1) - m(m-1)/2 + (l - m)
-          T re0 = 0, im0 = 0, re1 = 0, im1 = 0;
-          int m = 0, slot = l;
-          for (; m + 1 <= l; m += 2) {
-            const int slot1 = slot + p - m;  // (l, m+1)
-            cplx<T> x0 = tr[slot], x1 = tr[slot1];
-            const T *e0 = col0 + 2 * m * (l + 1);
-            const T *e1 = e0 + 2 * (l + 1);
-            re0 += e0[0] * x0.re;
-            im0 += e0[1] * x0.im;
-            re1 += e1[0] * x1.re;
-            im1 += e1[1] * x1.im;
-            slot = slot1 + p - m - 1;        // (l, m+2)
+          int slot = l;
+          for (int m = 0; m <= l; ++m) {
+            const T *e = col0 + 2 * m * (l + 1);
+            const T ee = e[0], eo = e[1];
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+              cplx<T> x = cbuf[g * (nm + nl) + slot];
+              re[g] += ee * x.re;
+              im[g] += eo * x.im;
+            }
+            slot += p - m;                   // (l, m+1)
           }
-          if (m <= l) {
-            cplx<T> x0 = tr[slot];
-            const T *e0 = col0 + 2 * m * (l + 1);
-            re0 += e0[0] * x0.re;
-            im0 += e0[1] * x0.im;
-          }
-          T re = re0 + re1, im = im0 + im1;
           T cr = ph[2 * mp], ci = -ph[2 * mp + 1];
-          acc[r].re += re * cr - im * ci;
-          acc[r].im += re * ci + im * cr;
+#pragma unroll
+          for (int g = 0; g < G; ++g) {
+            acc[g][r].re += re[g] * cr - im[g] * ci;
+            acc[g][r].im += re[g] * ci + im[g] * cr;
+          }
         }
       }
     }
     __syncwarp();
     if (NST > 0 && lane == 0) mbar_arrive(&empty[b]);
   }
-  if (tvalid && nact > 0) {
-    const T ih = (T)(ldexp(1.0, depth[t]) / scale_e);
+  if (nact > 0) {
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      int c = lane + 32 * r;
-      if (c < nl) loc[(size_t)t * nl + c] = cmake<T>(acc[r].re * ih, acc[r].im * ih);
+    for (int g = 0; g < G; ++g) {
+      if (!tvalid[g]) continue;
+      const T ih = (T)(ldexp(1.0, depth[tg[g]]) / scale_e);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        int c = lane + 32 * r;
+        if (c < nl) loc[(size_t)tg[g] * nl + c] = cmake<T>(acc[g][r].re * ih, acc[g][r].im * ih);
+      }
     }
   }
 }
@@ -409,7 +431,7 @@ void upload_codes(int device) {
   if (device >= 0 && device < 64) g_codes_ready[device] = true;
 }
 
-template <typename T, int NST>
+template <typename T, int NST, int G>
 size_t m2l_smem(int p, int stride) {
   int nm = tri(p), nl = tri(p + 1);
   size_t off = (size_t)NST * stride * sizeof(T);
@@ -417,21 +439,21 @@ size_t m2l_smem(int p, int stride) {
   off += 2 * NST * sizeof(uint64_t);
   if (NST > 0) off += (size_t)nl * p * sizeof(T);
   off = (off + 15) & ~(size_t)15;
-  off += (size_t)kSibWarps * (nm + nl) * sizeof(cplx<T>);
-  off += 216 * sizeof(int) + 10 * sizeof(unsigned) + 320 * sizeof(uint16_t) + 4 * nl;
+  off += (size_t)kSibWarps * G * (nm + nl) * sizeof(cplx<T>);
+  off += (size_t)G * 216 * sizeof(int) + 10 * sizeof(unsigned) + 320 * sizeof(uint16_t) + 4 * nl;
   return off + 64;
 }
 
-template <typename T, int NST, int R>
+template <typename T, int NST, int R, int G>
 bool try_launch(AranGpuSolver3d *s, OpTables<T> &tb, const M2LOffsets &D, const cplx<T> *mult,
                 cplx<T> *loc, cudaStream_t st, int dev_smem) {
   DevTree &t = s->tree;
   const int p = s->cfg.order;
-  size_t sm = m2l_smem<T, NST>(p, D.stride);
+  size_t sm = m2l_smem<T, NST, G>(p, D.stride);
   if ((int)sm > dev_smem) return false;
-  ACHECK(cudaFuncSetAttribute(k_m2l_sibling<T, NST, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)sm));
-  k_m2l_sibling<T, NST, R><<<t.n_parents, 32 * (kSibWarps + 1), sm, st>>>(
+  ACHECK(cudaFuncSetAttribute(k_m2l_sibling<T, NST, R, G>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_m2l_sibling<T, NST, R, G><<<ceil_div(t.n_parents, G), 32 * (kSibWarps + 1), sm, st>>>(
       t.n_parents, t.parents.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
       t.ijk.ptr, t.depth.ptr, p, tb.dir_m2l.ptr, D, tb.vt.ptr, tb.lm.ptr, s->scale_e, mult, loc,
       s->err_dev.ptr);
@@ -455,21 +477,24 @@ void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const cplx<T> *mult, cplx<T> 
   D.stride = dir_offset(p, 0, 6);
   int dev_smem = 0;
   ACHECK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
-  // R = rounds of 32 lanes over the tri(p+1) local coefficients
+  // R = rounds of 32 lanes over the tri(p+1) local coefficients; G parents
+  // per CTA (each warp takes child w of every one of them)
   const int nl = tri(p + 1);
   if (nl <= 96) {
-    if (try_launch<T, 3, 3>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 1, 3>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 3, 3, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 3, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 3, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
   } else if (nl <= 160) {
-    if (try_launch<T, 3, 5>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 1, 5>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 3, 5, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 5, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 5, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
   } else if (nl <= 256) {
-    if (try_launch<T, 3, 8>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 1, 8>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 0, 8>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 3, 8, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 8, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 0, 8, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
   } else {
-    if (try_launch<T, 1, kMaxRounds>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 0, kMaxRounds>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, kMaxRounds, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 0, kMaxRounds, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
   }
   throw CudaError{cudaErrorInvalidConfiguration, "M2L shared memory exceeds the device limit"};
 }
