@@ -312,14 +312,14 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), (sizeof(T) == 4 && G == 
       for (int r = 0; r < R; ++r) {
         int c = lane + 32 * r;
         if (c < nm) {
-          const int l = lm[2 * c], mp = lm[2 * c + 1];
-          const T *col0 = EOf + 2 * (sq_off(l) + mp);
+          const int l = lm[2 * c];
+          const T *col0 = EOf + 2 * c;     // plane m at col0 + 2 m nm
           const int so = tri(l);
           T re[G], im[G];
 #pragma unroll
           for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
           for (int m = 0; m <= l; ++m) {
-            const T *e = col0 + 2 * m * (l + 1);
+            const T *e = col0 + 2 * m * nm;
             const T ee = e[0], eo = e[1];
 #pragma unroll
             for (int g = 0; g < G; ++g) {
@@ -366,14 +366,14 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), (sizeof(T) == 4 && G == 
         int c = lane + 32 * r;
         if (c < nl) {
           const int l = lm[2 * c], mp = lm[2 * c + 1];
-          const T *col0 = EOi + 2 * (sq_off(l) + mp);
+          const T *col0 = EOi + 2 * c;     // plane m at col0 + 2 m nl
           T re[G], im[G];
 #pragma unroll
           for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
           // slot of (l, m) in m-major order: m(p+1) - m(m-1)/2 + (l - m)
           int slot = l;
           for (int m = 0; m <= l; ++m) {
-            const T *e = col0 + 2 * m * (l + 1);
+            const T *e = col0 + 2 * m * nl;
             const T ee = e[0], eo = e[1];
 #pragma unroll
             for (int g = 0; g < G; ++g) {

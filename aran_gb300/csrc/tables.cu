@@ -25,13 +25,13 @@ struct DirLayout {
 
 __host__ __device__ DirLayout dir_layout(int p, int kind) {
   DirLayout d;
-  if (kind == 0) {  // M2L: (E, O) interleaved, column-major blocks
+  if (kind == 0) {  // M2L: (E, O) interleaved, [m][coefficient] planes
     d.Lf = p; d.Li = p + 1; d.nrp = 2 * p + 2;
     d.ef = 0;
     d.of = -1;
-    d.ei = 2 * sq_size(d.Lf);
+    d.ei = 2 * d.Lf * tri(d.Lf);
     d.oi = -1;
-    d.ph = d.ei + 2 * sq_size(d.Li);
+    d.ph = d.ei + 2 * d.Li * tri(d.Li);
     d.rp = d.ph + 2 * (p + 1);
     d.stride = ((d.rp + d.nrp) + 3) & ~3;
     return d;
@@ -137,14 +137,18 @@ __global__ void k_dir_tables(int p, int kind, int ndir, double ex, double ey, do
   double *eo = wm + wig_size(Lmax);
   gen_wigner_d(Lmax, theta, w);
   gen_wigner_d(Lmax, -theta, wm);
-  // M2L blocks go column-major ([l][m][m'], (E, O) interleaved) so the lanes
-  // of a warp, one output order m' each, read consecutive words
+  // M2L blocks go in planes of the source order m: plane m holds, for every
+  // output coefficient c = (l, m') in tri order, the (E, O) pair that
+  // multiplies source (l, m) (zero when m > l), so the lanes of a warp, one
+  // output coefficient each, read consecutive words at every step m
   auto put_cm = [&](int Lb, int base) {
+    const int nc = tri(Lb);
+    for (int i = 0; i < 2 * Lb * nc; ++i) o[base + i] = (T)0;
     for (int l = 0; l < Lb; ++l)
       for (int mp = 0; mp <= l; ++mp)
         for (int m = 0; m <= l; ++m) {
           int src = sq_off(l) + mp * (l + 1) + m;
-          int dst = sq_off(l) + m * (l + 1) + mp;
+          int dst = m * nc + tri(l, mp);
           o[base + 2 * dst] = (T)eo[src];
           o[base + 2 * dst + 1] = (T)eo[sq_size(Lb) + src];
         }
