@@ -98,7 +98,7 @@ constexpr int kSibWarps = 8;   // consumers: one per child of the parent
 constexpr int kMaxRounds = ((kMaxOrder + 1) * (kMaxOrder + 2) / 2 + 31) / 32;
 
 template <typename T, int NST, int R, int G>
-__global__ void __launch_bounds__(32 * (kSibWarps + 1), (sizeof(T) == 4 && G == 1) ? 3 : 2)
+__global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
     k_m2l_sibling(int nparents, const int *__restrict__ parents, const int *__restrict__ child,
                   const int *__restrict__ begin, const int *__restrict__ end,
                   const int *__restrict__ col, const int *__restrict__ ncol,
@@ -480,12 +480,14 @@ void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const cplx<T> *mult, cplx<T> 
   // R = rounds of 32 lanes over the tri(p+1) local coefficients; G parents
   // per CTA (each warp takes child w of every one of them)
   const int nl = tri(p + 1);
+  // (two table slots keep a p <= 12 FP32 CTA under a third of the shared
+  // memory, so three CTAs share an SM)
   if (nl <= 96) {
-    if (try_launch<T, 3, 3, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (sizeof(T) == 8 && try_launch<T, 3, 3, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 2, 3, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
     if (try_launch<T, 1, 3, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
     if (try_launch<T, 1, 3, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
   } else if (nl <= 160) {
-    if (try_launch<T, 3, 5, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
     if (try_launch<T, 1, 5, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
     if (try_launch<T, 1, 5, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
   } else if (nl <= 256) {
