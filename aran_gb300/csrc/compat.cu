@@ -335,10 +335,14 @@ int aran_solver3d_solve_try(AranSolver3d *solver) {
            is((void *)solver->m2l, (void *)&aran_development3d_m2l_kkylin) &&
            is((void *)solver->l2l, (void *)&aran_development3d_l2l_kkylin))
     flavour = ARAN_FLAVOUR_KKYLIN;
+  else if (is((void *)solver->m2m, (void *)&aran_development3d_m2m) &&
+           is((void *)solver->m2l, (void *)&aran_development3d_m2l) &&
+           is((void *)solver->l2l, (void *)&aran_development3d_l2l))
+    flavour = ARAN_FLAVOUR_NORMAL;
   if (flavour < 0) {
-    aran::set_error("aran_solver3d_solve: m2m/m2l/l2l must be the rotate or the kkylin "
-                    "operators of this library (the normal flavour and user translations do "
-                    "not run on the GPU)");
+    aran::set_error("aran_solver3d_solve: m2m/m2l/l2l must be one flavour of this library's "
+                    "operators (normal, kkylin or rotate); user translations do not run on "
+                    "the GPU");
     return ARAN_ERR_UNSUPPORTED;
   }
   const int64_t n = (int64_t)solver->points.size();

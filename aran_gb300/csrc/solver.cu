@@ -27,10 +27,11 @@ int check_config(const AranGpuConfig3d *c) {
   if (c->maxbox < 1) return fail(ARAN_ERR_INVALID, "maxbox must be >= 1");
   if (c->order < 1 || c->order > kMaxOrder)
     return fail(ARAN_ERR_INVALID, "order must be in [1, " + std::to_string(kMaxOrder) + "]");
-  if (c->flavour == ARAN_FLAVOUR_NORMAL)
-    return fail(ARAN_ERR_UNSUPPORTED, "the normal O(p^4) flavour is not available on the GPU; "
-                                      "use ARAN_FLAVOUR_ROTATE or ARAN_FLAVOUR_KKYLIN");
-  if (c->flavour != ARAN_FLAVOUR_ROTATE && c->flavour != ARAN_FLAVOUR_KKYLIN)
+  // the normal flavour (aransphericalseriesd-translate.c:507-834) applies the
+  // same linear operators as the rotate flavour; it runs the rotation
+  // kernels (O(p^3) per translation instead of O(p^4), equal to FP64 rounding)
+  if (c->flavour != ARAN_FLAVOUR_ROTATE && c->flavour != ARAN_FLAVOUR_KKYLIN &&
+      c->flavour != ARAN_FLAVOUR_NORMAL)
     return fail(ARAN_ERR_INVALID, "unknown flavour");
   if (c->precision != ARAN_PRECISION_FP64 && c->precision != ARAN_PRECISION_MIXED)
     return fail(ARAN_ERR_INVALID, "unknown precision");

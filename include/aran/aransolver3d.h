@@ -11,7 +11,8 @@
  * charge and result sit in its point struct; the per-pair/per-particle user
  * callbacks are then replaced by the GPU Newton kernels (potential as in
  * tests/newtonpot3.c, field as in tests/newtonfield3.c) and the m2m/m2l/l2l
- * addresses select the rotate or kkylin flavour.  aran_solver3d_solve adds
+ * addresses select the flavour (normal and rotate run the rotation
+ * kernels, kkylin its own).  aran_solver3d_solve adds
  * the result into each point's result member, as the reference's callbacks
  * accumulate.  Anything the GPU path cannot run (unknown operator
  * callbacks, no layout) makes aran_solver3d_solve return without touching

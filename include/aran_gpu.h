@@ -34,7 +34,8 @@ extern "C" {
 #define ARAN_ERR_CANCELLED (-7)    /* a queued request was cancelled */
 
 /* M2M/M2L/L2L flavours: aran_development3d_{m2l,m2l_kkylin,m2l_rotate}
- * (aran/arandevelopment3d.c:306-313,362-369,423-430) */
+ * (aran/arandevelopment3d.c:306-313,362-369,423-430).  NORMAL applies the
+ * same operators as ROTATE and runs its kernels. */
 #define ARAN_FLAVOUR_NORMAL 0
 #define ARAN_FLAVOUR_KKYLIN 1
 #define ARAN_FLAVOUR_ROTATE 2

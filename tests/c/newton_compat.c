@@ -10,7 +10,10 @@
  * particle, solve, get_stats, free.  The only added call is
  * aran_solver3d_set_newton_layout.
  *
- *   newton_compat N ORDER rotate|kkylin|normal pot|field fp64|mixed [twice|nolayout]
+ *   newton_compat N ORDER rotate|kkylin|normal|mixops pot|field fp64|mixed [twice|nolayout]
+ *
+ * "mixops" hands m2m/l2l of the rotate flavour with the kkylin m2l, which the
+ * GPU path refuses.
  *
  * Prints one line "maxerr=<max relative error vs direct sum> p2p=... m2l=..."
  * and exits 0, or prints "error: <aran_gpu_last_error()>" and exits 2 when
@@ -74,7 +77,7 @@ int main (int argc, char **argv)
 {
   if (argc < 6)
     {
-      fprintf (stderr, "usage: %s N ORDER rotate|kkylin|normal pot|field fp64|mixed [twice|nolayout]\n",
+      fprintf (stderr, "usage: %s N ORDER rotate|kkylin|normal|mixops pot|field fp64|mixed [twice|nolayout]\n",
                argv[0]);
       return 64;
     }
@@ -104,6 +107,12 @@ int main (int argc, char **argv)
     {
       m2m = (AranMultipole2MultipoleFunc3d) aran_development3d_m2m_rotate;
       m2l = (AranMultipole2LocalFunc3d) aran_development3d_m2l_rotate;
+      l2l = (AranLocal2LocalFunc3d) aran_development3d_l2l_rotate;
+    }
+  else if (strcmp (flavour, "mixops") == 0)
+    {
+      m2m = (AranMultipole2MultipoleFunc3d) aran_development3d_m2m_rotate;
+      m2l = (AranMultipole2LocalFunc3d) aran_development3d_m2l_kkylin;
       l2l = (AranLocal2LocalFunc3d) aran_development3d_l2l_rotate;
     }
   else if (strcmp (flavour, "kkylin") == 0)

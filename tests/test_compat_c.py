@@ -12,8 +12,8 @@ largest relative error.
   potential (gcomplex128 accumulator) and the field (VsgVector3d);
 * results accumulate into the points like the reference callbacks (two
   solves give twice the field);
-* the normal flavour and a missing layout are refused and leave the points
-  untouched.
+* a mixed set of operators and a missing layout are refused and leave the
+  points untouched.
 """
 import os
 import re
@@ -91,6 +91,7 @@ def test_no_device_refuses_2d(exe2d):
 # GB300: 5.2e-5 at p=12 in FP64 and 5.6e-5 mixed, 1.2e-4 kkylin at p=10;
 # potential 8.7e-8 at p=12)
 CASES = [
+    ("normal", "field", "fp64", 12, 2e-4),
     ("rotate", "field", "fp64", 12, 2e-4),
     ("rotate", "pot", "fp64", 12, 5e-7),
     ("rotate", "field", "mixed", 12, 2e-4),
@@ -121,7 +122,7 @@ def test_results_accumulate(exe):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("args,msg", [
-    ((4000, 8, "normal", "field", "fp64"), "rotate or the kkylin"),
+    ((4000, 8, "mixops", "field", "fp64"), "one flavour"),
     ((4000, 8, "rotate", "field", "fp64", "nolayout"), "set_newton_layout"),
 ])
 def test_refused_solves_leave_points_untouched(exe, args, msg):

@@ -154,8 +154,21 @@ def test_error_codes(aran):
             s.solve(np.zeros((0, 3)), np.zeros(0))
         assert ei.value.code == -1
     with pytest.raises(aran.AranError) as ei:
-        aran.Solver3d(flavour="normal")
-    assert ei.value.code == -6
+        aran.Solver3d(flavour=7)
+    assert ei.value.code == -1
+
+
+def test_normal_flavour_matches_oracle(aran, oracle):
+    # the normal flavour runs the rotation kernels: same operators, so the
+    # GPU result equals the oracle's O(p^4) normal flavour to FP64 rounding
+    x, q = W.uniform(6000, 11)
+    with aran.Solver3d((0, 0, 0), (1, 1, 1), maxbox=20, order=8, flavour="normal",
+                       field=True, precision="fp64") as s:
+        pot, fld = s.solve(x, q)
+        st = s.get_stats()
+    ofld, ost = oracle.solve(x, q, order=8, maxbox=20, flavour="normal", field=True)
+    assert rel_l2(fld, ofld) < FP64_TOL
+    assert st == ost
 
 
 KK_CASES = [
@@ -238,7 +251,7 @@ def newton_points(n, dist):
     return rng.uniform(-0.999, 0.999, (n, 3)), rng.uniform(0.0, 2.0 / n, n)
 
 
-@pytest.mark.parametrize("flavour", ["rotate", "kkylin"])
+@pytest.mark.parametrize("flavour", ["normal", "rotate", "kkylin"])
 @pytest.mark.parametrize("n,order,maxbox,dist", NEWTON_AT)
 def test_newton_at_cases(aran, oracle, flavour, n, order, maxbox, dist):
     x, q = newton_points(n, dist)
