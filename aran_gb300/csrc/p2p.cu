@@ -89,7 +89,7 @@ __global__ void k_big_items(int nleaves, const int *__restrict__ near_off,
 }
 
 template <typename T, bool FIELD, bool MIXED, bool BIG>
-__global__ void __launch_bounds__(128) k_p2p(
+__global__ void __launch_bounds__(128, 10) k_p2p(
     const int4 *__restrict__ items, const int *__restrict__ near_off,
     const int *__restrict__ near_rng, const int2 *__restrict__ be, const float4 *__restrict__ chi,
     const float4 *__restrict__ clo, const double *__restrict__ sx, const double *__restrict__ sy,
@@ -141,11 +141,12 @@ __global__ void __launch_bounds__(128) k_p2p(
         const float oz = tz - ((sh.z - tch.z) + (sl.z - tcl.z));
         const float thr2 = tch.w;
         float p0 = 0.f, f0 = 0.f, f1 = 0.f, f2 = 0.f;
+#pragma unroll 4
         for (int j = sbe.x + j0; j < sbe.y; j += js) {
           const real4<float> sj = rel32[j];
           float dx = ox - sj.x, dy = oy - sj.y, dz = oz - sj.z;
           float r2 = dx * dx + dy * dy + dz * dz;
-          if (r2 < thr2) {
+          if (__builtin_expect(r2 < thr2, 0)) {
             if (j == t) {
               r2 = 0.f;
             } else {
