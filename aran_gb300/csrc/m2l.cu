@@ -318,6 +318,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
           T re[G], im[G];
 #pragma unroll
           for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
+#pragma unroll 2
           for (int m = 0; m <= l; ++m) {
             const T *e = col0 + 2 * m * nm;
             const T ee = e[0], eo = e[1];
@@ -345,6 +346,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
           T re[G], im[G];
 #pragma unroll
           for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
+#pragma unroll 2
           for (int n = m; n < p; ++n) {
             const T f = vcol[n * vs] * rp[l + n + 1];
             const int sidx = nl + tri(n, m);
@@ -372,6 +374,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
           for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
           // slot of (l, m) in m-major order: m(p+1) - m(m-1)/2 + (l - m)
           int slot = l;
+#pragma unroll 2
           for (int m = 0; m <= l; ++m) {
             const T *e = col0 + 2 * m * nl;
             const T ee = e[0], eo = e[1];
