@@ -122,6 +122,16 @@ __global__ void __launch_bounds__(128, 10) k_p2p(
     const bool active = ti < nt;
     const int t = b + (active ? ti : 0);
     double pot = 0, fx = 0, fy = 0, fz = 0;
+    // mixed: per-source-leaf FP32 sums are added with Kahan compensation in
+    // FP32 (FP64 adds per leaf would occupy the FP64 pipe, 1/64 of FP32)
+    float ks0 = 0.f, ks1 = 0.f, ks2 = 0.f, ks3 = 0.f;
+    float kc0 = 0.f, kc1 = 0.f, kc2 = 0.f, kc3 = 0.f;
+    auto kahan = [](float &sum, float &comp, float v) {
+      const float y = v - comp;
+      const float t2 = sum + y;
+      comp = (t2 - sum) - y;
+      sum = t2;
+    };
     const double tx64 = sx[t], ty64 = sy[t], tz64 = sz[t];
     float tx = 0.f, ty = 0.f, tz = 0.f;
     if (MIXED) {
@@ -168,11 +178,11 @@ __global__ void __launch_bounds__(128, 10) k_p2p(
             f2 -= q3 * dz;
           }
         }
-        pot += (double)p0;
+        kahan(ks0, kc0, p0);
         if (FIELD) {
-          fx += (double)f0;
-          fy += (double)f1;
-          fz += (double)f2;
+          kahan(ks1, kc1, f0);
+          kahan(ks2, kc2, f1);
+          kahan(ks3, kc3, f2);
         }
       } else {
         for (int j = sbe.x + j0; j < sbe.y; j += js) {
@@ -208,6 +218,12 @@ __global__ void __launch_bounds__(128, 10) k_p2p(
           for (int lf = la; lf < lb; ++lf) do_leaf(lf, sub, tpt);
         }
       }
+    }
+    if (MIXED) {
+      pot = (double)ks0 - (double)kc0;
+      fx = (double)ks1 - (double)kc1;
+      fy = (double)ks2 - (double)kc2;
+      fz = (double)ks3 - (double)kc3;
     }
     for (int o = 1; o < tpt; o <<= 1) {
       pot += __shfl_xor_sync(kFull, pot, o);
