@@ -41,6 +41,18 @@ FMM_HD int tri(int l, int m) { return (l * (l + 1)) / 2 + m; }
 FMM_HD int n_mult(int p) { return tri(p); }           // degrees 0..p-1
 FMM_HD int n_local(int p) { return tri(p + 1); }      // degrees 0..p
 // packed (l+1)x(l+1) block offsets for rotation tables, degrees 0..L-1
+// (l, m) of the k-th coefficient in m-major order (m = 0: l = 0..p, m = 1:
+// l = 1..p, ...): the vertical stage walks coefficients in this order so the
+// 32 lanes of a round share m and hence their trip count
+FMM_HD void mmajor_lm(int k, int p, int &l, int &m) {
+  m = 0;
+  while (k > p - m) {
+    k -= p + 1 - m;
+    ++m;
+  }
+  l = m + k;
+}
+
 FMM_HD int sq_off(int l) { return (l * (l + 1) * (2 * l + 1)) / 6; }  // sum_{i<l} (i+1)^2
 FMM_HD int sq_size(int L) { return sq_off(L); }
 

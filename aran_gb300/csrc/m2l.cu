@@ -75,23 +75,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mb, uint32_t parity) {
 }
 
 struct M2LOffsets {
-  int ef, ei, ph, rp, stride;  // in T units; ef/ei: (E, O) pairs, column-major blocks
+  int ef, ei, ph, rp, vv, stride;  // in T units; ef/ei: (E, O) pairs in source-order planes
 };
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *mb) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mb)) : "memory");
-}
-
-// (l, m) of the k-th coefficient in m-major order (m = 0: l = 0..p, m = 1:
-// l = 1..p, ...): the vertical stage walks coefficients in this order so the
-// 32 lanes of a round share m and hence their trip count
-__device__ __forceinline__ void mmajor_lm(int k, int p, int &l, int &m) {
-  m = 0;
-  while (k > p - m) {
-    k -= p + 1 - m;
-    ++m;
-  }
-  l = m + k;
 }
 
 constexpr int kSibWarps = 8;   // consumers: one per child of the parent
@@ -103,16 +91,16 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
                   const int *__restrict__ begin, const int *__restrict__ end,
                   const int *__restrict__ col, const int *__restrict__ ncol,
                   const int *__restrict__ ijk, const uint8_t *__restrict__ depth, int p,
-                  const T *__restrict__ dirs, M2LOffsets D, const T *__restrict__ vt_g,
+                  const T *__restrict__ dirs, M2LOffsets D,
                   const uint8_t *__restrict__ lm_g, double scale_e,
                   const cplx<T> *__restrict__ mult, cplx<T> *__restrict__ loc,
                   int *__restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int nm = tri(p), nl = tri(p + 1);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  // shared layout: NST tables | full[NST] | empty[NST] | vertical factors
-  // (m-major) | per-warp buffers (G columns) | G 6x6x6 source grids | offset
-  // mask | active list (NST = 0: no tables, barriers or vertical factors)
+  // shared layout: NST tables | full[NST] | empty[NST] | per-warp buffers
+  // (G columns) | G 6x6x6 source grids | offset mask | active list (NST = 0:
+  // no tables or barriers in shared memory)
   size_t off = 0;
   T *tab = reinterpret_cast<T *>(smem_raw);
   off += (size_t)NST * D.stride * sizeof(T);
@@ -120,8 +108,6 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
   uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + off);
   uint64_t *empty = full + NST;
   off += 2 * NST * sizeof(uint64_t);
-  T *vtm = reinterpret_cast<T *>(smem_raw + off);
-  if (NST > 0) off += (size_t)nl * p * sizeof(T);
   off = (off + 15) & ~(size_t)15;
   cplx<T> *wbuf = reinterpret_cast<cplx<T> *>(smem_raw + off);
   off += (size_t)kSibWarps * G * (nm + nl) * sizeof(cplx<T>);
@@ -138,13 +124,6 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
 
   for (int i = threadIdx.x; i < G * 216; i += blockDim.x) grid[i] = -1;
   if (threadIdx.x < 10) mask[threadIdx.x] = 0u;
-  // vertical factors, m-major slot k: vtm[n * nl + k]
-  if (NST > 0)
-    for (int i = threadIdx.x; i < nl * p; i += blockDim.x) {
-      int k = i % nl, n = i / nl, l, m;
-      mmajor_lm(k, p, l, m);
-      vtm[i] = vt_g[tri(l, m) * p + n];
-    }
   for (int k = threadIdx.x; k < nl; k += blockDim.x) {
     int l, m;
     mmajor_lm(k, p, l, m);
@@ -289,7 +268,6 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
       const T *ph = tb + D.ph;
       const T *EOf = tb + D.ef;
       const T *EOi = tb + D.ei;
-      const T *rp = tb + D.rp;
       // z-phase of the source multipoles: e^{i m phi}
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -339,16 +317,15 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
       for (int r = 0; r < R; ++r) {
         int k = lane + 32 * r;
         if (k < nl) {
-          const int l = vmap[2 * k], m = vmap[2 * k + 1];
-          // factor of source degree n: vcol[n * vs]
-          const T *vcol = NST > 0 ? vtm + k : vt_g + tri(l, m) * p;
-          const int vs = NST > 0 ? nl : 1;
+          const int m = vmap[2 * k + 1];
+          // vertical factor times radial power for source degree n: vcol[n * nl]
+          const T *vcol = tb + D.vv + k;
           T re[G], im[G];
 #pragma unroll
           for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
 #pragma unroll 2
           for (int n = m; n < p; ++n) {
-            const T f = vcol[n * vs] * rp[l + n + 1];
+            const T f = vcol[n * nl];
             const int sidx = nl + tri(n, m);
 #pragma unroll
             for (int g = 0; g < G; ++g) {
@@ -440,7 +417,6 @@ size_t m2l_smem(int p, int stride) {
   size_t off = (size_t)NST * stride * sizeof(T);
   off = (off + 15) & ~(size_t)15;
   off += 2 * NST * sizeof(uint64_t);
-  if (NST > 0) off += (size_t)nl * p * sizeof(T);
   off = (off + 15) & ~(size_t)15;
   off += (size_t)kSibWarps * G * (nm + nl) * sizeof(cplx<T>);
   off += (size_t)G * 216 * sizeof(int) + 10 * sizeof(unsigned) + 320 * sizeof(uint16_t) + 4 * nl;
@@ -458,7 +434,7 @@ bool try_launch(AranGpuSolver3d *s, OpTables<T> &tb, const M2LOffsets &D, const 
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   k_m2l_sibling<T, NST, R, G><<<ceil_div(t.n_parents, G), 32 * (kSibWarps + 1), sm, st>>>(
       t.n_parents, t.parents.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
-      t.ijk.ptr, t.depth.ptr, p, tb.dir_m2l.ptr, D, tb.vt.ptr, tb.lm.ptr, s->scale_e, mult, loc,
+      t.ijk.ptr, t.depth.ptr, p, tb.dir_m2l.ptr, D, tb.lm.ptr, s->scale_e, mult, loc,
       s->err_dev.ptr);
   ACHECK(cudaGetLastError());
   s->launches++;
@@ -477,6 +453,7 @@ void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const cplx<T> *mult, cplx<T> 
   D.ei = dir_offset(p, 0, 2);
   D.ph = dir_offset(p, 0, 4);
   D.rp = dir_offset(p, 0, 5);
+  D.vv = dir_offset(p, 0, 7);
   D.stride = dir_offset(p, 0, 6);
   int dev_smem = 0;
   ACHECK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));

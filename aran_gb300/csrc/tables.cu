@@ -20,7 +20,7 @@ namespace {
 
 struct DirLayout {
   int Lf, Li, nrp;
-  int ef, of, ei, oi, ph, rp, stride;
+  int ef, of, ei, oi, ph, rp, vv, stride;
 };
 
 __host__ __device__ DirLayout dir_layout(int p, int kind) {
@@ -33,7 +33,10 @@ __host__ __device__ DirLayout dir_layout(int p, int kind) {
     d.oi = -1;
     d.ph = d.ei + 2 * d.Li * tri(d.Li);
     d.rp = d.ph + 2 * (p + 1);
-    d.stride = ((d.rp + d.nrp) + 3) & ~3;
+    // vertical factors times the radial powers of this offset, m-major
+    // slot k of the local, source degree n: vv[n * tri(p+1) + k]
+    d.vv = ((d.rp + d.nrp) + 3) & ~3;
+    d.stride = ((d.vv + tri(p + 1) * p) + 3) & ~3;
     return d;
   } else if (kind == 1) { d.Lf = p; d.Li = p; d.nrp = p + 1; }          // M2M
   else { d.Lf = p + 1; d.Li = p + 1; d.nrp = p + 2; }                 // L2L
@@ -43,6 +46,7 @@ __host__ __device__ DirLayout dir_layout(int p, int kind) {
   d.oi = d.ei + sq_size(d.Li);
   d.ph = d.oi + sq_size(d.Li);
   d.rp = d.ph + 2 * (p + 1);
+  d.vv = -1;
   d.stride = ((d.rp + d.nrp) + 3) & ~3;
   return d;
 }
@@ -101,6 +105,22 @@ __global__ void k_scalar_tables(int p, double *scratch, T *rec, T *p2mf, T *vt, 
   gen_grad_coefs(p, gz64, gm64);
   for (int i = 0; i < tri(p); ++i) gz[i] = (T)gz64[i];
   for (int i = 0; i < p * p; ++i) gm[i] = (T)gm64[i];
+}
+
+// M2L: the vertical factors (sign folded) times the offset's radial powers,
+// so the translation along z takes one factor per term
+template <typename T>
+__global__ void k_m2l_vertical(int p, int ndir, int stride, int rp_off, int vv_off,
+                               const T *__restrict__ vt, T *__restrict__ dirs) {
+  const int nl = tri(p + 1);
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)ndir * nl * p) return;
+  const int d = (int)(i / (nl * p)), e = (int)(i % (nl * p));
+  const int k = e % nl, n = e / nl;
+  int l, m;
+  mmajor_lm(k, p, l, m);
+  T *tb = dirs + (size_t)d * stride;
+  tb[vv_off + e] = vt[tri(l, m) * p + n] * tb[rp_off + l + n + 1];
 }
 
 // one thread per direction: kind 0 = M2L offset code, 1 = M2M octant, 2 = L2L octant
@@ -220,6 +240,12 @@ void build_tables_t(AranGpuSolver3d *s, OpTables<T> &tb, cudaStream_t st) {
     k_dir_tables<T><<<ceil_div(ndir, 64), 64, 0, st>>>(p, kind, ndir, ex, ey, ez, scratch.ptr,
                                                         dstride, dst.ptr);
     ACHECK(cudaGetLastError());
+    if (kind == 0) {
+      const int64_t ne = (int64_t)ndir * tri(p + 1) * p;
+      k_m2l_vertical<T><<<ceil_div(ne, 256), 256, 0, st>>>(p, ndir, L.stride, L.rp, L.vv,
+                                                            tb.vt.ptr, dst.ptr);
+      ACHECK(cudaGetLastError());
+    }
     ACHECK(cudaStreamSynchronize(st));
   }
   scratch.release();
@@ -236,6 +262,7 @@ int dir_offset(int p, int kind, int what) {
     case 3: return L.oi;
     case 4: return L.ph;
     case 5: return L.rp;
+    case 7: return L.vv;
     default: return L.stride;
   }
 }
