@@ -1,7 +1,8 @@
 // compat.cu -- LibAran's public 3D solver API (aran/aransolver3d.h,
-// aran/arandevelopment3d.h, aran/aran.h and the vsg_prtree3d_new_full tree
-// constructor) implemented on the GPU solver, so a program written against
-// LibAran keeps its calls.  See include/aran/aransolver3d.h for the contract.
+// aran/aran.h and the vsg_prtree3d_new_full tree constructor) implemented on
+// the GPU solver, so a program written against LibAran keeps its calls.  See
+// include/aran/aransolver3d.h for the contract; the development and series
+// operators are in series3d.cu.
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -40,21 +41,6 @@ struct _AranSolver3d {
   guint depth = 0;
 };
 
-namespace {
-
-const GType kDevelopmentType = 0x41524433;  // "ARD3"
-
-size_t series_size(int posdeg, int negdeg) {
-  return ((size_t)(posdeg + 1) * (posdeg + 2) + (size_t)negdeg * (negdeg + 1)) / 2;
-}
-
-void not_on_host(const char *fn) {
-  aran::set_error(std::string(fn) +
-                  ": LibAran operator callbacks run inside aran_solver3d_solve on the GPU; "
-                  "calling them on host developments is not supported");
-}
-
-}  // namespace
 
 extern "C" {
 
@@ -87,91 +73,6 @@ gdouble vsg_vector3d_dist(const VsgVector3d *one, const VsgVector3d *other) {
   return sqrt(dx * dx + dy * dy + dz * dz);
 }
 
-// ---- developments (host containers; aran/arandevelopment3d.c:64-158) ----
-GType aran_development3d_get_type(void) { return kDevelopmentType; }
-
-AranDevelopment3d *aran_development3d_new(guint8 posdeg, guint8 negdeg) {
-  AranDevelopment3d *d = (AranDevelopment3d *)std::calloc(1, sizeof(AranDevelopment3d));
-  d->posdeg = posdeg;
-  d->negdeg = negdeg;
-  int lp = posdeg > negdeg ? posdeg : negdeg;
-  d->multipole = (gcomplex128 *)std::calloc(series_size(posdeg, negdeg), sizeof(gcomplex128));
-  d->local = (gcomplex128 *)std::calloc(series_size(lp, 0), sizeof(gcomplex128));
-  return d;
-}
-
-void aran_development3d_free(AranDevelopment3d *ad) {
-  if (!ad) return;
-  std::free(ad->multipole);
-  std::free(ad->local);
-  std::free(ad);
-}
-
-void aran_development3d_copy(const AranDevelopment3d *src, AranDevelopment3d *dst) {
-  if (!src || !dst || src->posdeg != dst->posdeg || src->negdeg != dst->negdeg) return;
-  int lp = src->posdeg > src->negdeg ? src->posdeg : src->negdeg;
-  std::memcpy(dst->multipole, src->multipole, series_size(src->posdeg, src->negdeg) * sizeof(gcomplex128));
-  std::memcpy(dst->local, src->local, series_size(lp, 0) * sizeof(gcomplex128));
-}
-
-AranDevelopment3d *aran_development3d_clone(AranDevelopment3d *src) {
-  if (!src) return nullptr;
-  AranDevelopment3d *d = aran_development3d_new(src->posdeg, src->negdeg);
-  aran_development3d_copy(src, d);
-  return d;
-}
-
-void aran_development3d_set_zero(AranDevelopment3d *ad) {
-  if (!ad) return;
-  int lp = ad->posdeg > ad->negdeg ? ad->posdeg : ad->negdeg;
-  std::memset(ad->multipole, 0, series_size(ad->posdeg, ad->negdeg) * sizeof(gcomplex128));
-  std::memset(ad->local, 0, series_size(lp, 0) * sizeof(gcomplex128));
-}
-
-void aran_development3d_write(AranDevelopment3d *ad, FILE *file) {
-  if (!ad || !file) return;
-  std::fprintf(file, "{multipole degree %d, local degree %d}", (int)ad->negdeg,
-               (int)(ad->posdeg > ad->negdeg ? ad->posdeg : ad->negdeg));
-}
-
-// operator callbacks: identity tokens for the solver (see the header)
-#define ARAN_TOKEN_OP(name)                                                                  \
-  void name(const VsgPRTree3dNodeInfo *, AranDevelopment3d *, const VsgPRTree3dNodeInfo *, \
-            AranDevelopment3d *) {                                                         \
-    not_on_host(#name);                                                                    \
-  }
-ARAN_TOKEN_OP(aran_development3d_m2m)
-ARAN_TOKEN_OP(aran_development3d_m2l)
-ARAN_TOKEN_OP(aran_development3d_l2l)
-ARAN_TOKEN_OP(aran_development3d_m2m_kkylin)
-ARAN_TOKEN_OP(aran_development3d_m2l_kkylin)
-ARAN_TOKEN_OP(aran_development3d_l2l_kkylin)
-ARAN_TOKEN_OP(aran_development3d_m2m_rotate)
-ARAN_TOKEN_OP(aran_development3d_m2l_rotate)
-ARAN_TOKEN_OP(aran_development3d_l2l_rotate)
-#undef ARAN_TOKEN_OP
-
-void aran_development3d_p2m(const VsgVector3d *, const gdouble, const VsgPRTree3dNodeInfo *,
-                            AranDevelopment3d *) {
-  not_on_host("aran_development3d_p2m");
-}
-
-void aran_development3d_p2l(const VsgVector3d *, const gdouble, const VsgPRTree3dNodeInfo *,
-                            AranDevelopment3d *) {
-  not_on_host("aran_development3d_p2l");
-}
-
-gcomplex128 aran_development3d_local_evaluate(const VsgPRTree3dNodeInfo *, AranDevelopment3d *,
-                                              const VsgVector3d *) {
-  not_on_host("aran_development3d_local_evaluate");
-  return gcomplex128(0.0, 0.0);
-}
-
-void aran_development3d_local_gradient_evaluate(const VsgPRTree3dNodeInfo *, AranDevelopment3d *,
-                                                const VsgVector3d *, VsgVector3d *) {
-  not_on_host("aran_development3d_local_gradient_evaluate");
-}
-
 // ---- solver (aran/aransolver3d.c) ----
 AranSolver3d *aran_solver3d_new(VsgPRTree3d *prtree, GType devel_type, gpointer devel,
                                 AranZeroFunc zero) {
@@ -197,7 +98,7 @@ void aran_solver3d_free(AranSolver3d *solver) {
 void aran_solver3d_set_development(AranSolver3d *solver, GType devel_type, gpointer devel,
                                    AranZeroFunc zero) {
   if (!solver) return;
-  if (devel && devel_type != kDevelopmentType) {
+  if (devel && devel_type != aran_development3d_get_type()) {
     aran::set_error("aran_solver3d_set_development: only ARAN_TYPE_DEVELOPMENT3D is supported");
     return;
   }
@@ -291,7 +192,7 @@ void aran_solver3d_foreach_point(AranSolver3d *solver, GFunc func, gpointer user
 // reference times the three callbacks instead, aransolver3d.c:1090-1127)
 guint aran_solver3d_optimal_semifar_threshold(AranSolver3d *solver) {
   if (!solver || !solver->devel || !solver->p2l || !solver->m2p) return G_MAXUINT;
-  int p = solver->devel->negdeg;
+  int p = aran_spherical_seriesd_get_negdeg(solver->devel->multipole);
   return (guint)((8 * (p + 1) * (p + 2) / 2 + 24 * p * (p + 1) / 2) / 20);
 }
 
@@ -317,7 +218,7 @@ int aran_solver3d_solve_try(AranSolver3d *solver) {
     aran::set_error("aran_solver3d_solve: call aran_solver3d_set_newton_layout first");
     return ARAN_ERR_INVALID;
   }
-  if (!solver->devel || solver->devel->negdeg < 1) {
+  if (!solver->devel || aran_spherical_seriesd_get_negdeg(solver->devel->multipole) < 1) {
     aran::set_error("aran_solver3d_solve: no development (aran_development3d_new (0, p))");
     return ARAN_ERR_INVALID;
   }
@@ -356,7 +257,7 @@ int aran_solver3d_solve_try(AranSolver3d *solver) {
   cfg.ub[1] = solver->tree->ub.y;
   cfg.ub[2] = solver->tree->ub.z;
   cfg.maxbox = (int)solver->tree->maxbox;
-  cfg.order = solver->devel->negdeg;
+  cfg.order = aran_spherical_seriesd_get_negdeg(solver->devel->multipole);
   cfg.flavour = flavour;
   cfg.field = solver->kind == ARAN_NEWTON_FIELD;
   cfg.precision = solver->precision;

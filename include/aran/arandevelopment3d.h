@@ -1,15 +1,14 @@
 /*
  * arandevelopment3d.h -- LibAran's 3D development (multipole + local pair) and
- * its operators, as the GPU library exposes them.
+ * its operators (aran/arandevelopment3d.h:38-150) on the GPU library.
  *
  * The development object is the template a program hands to
  * aran_solver3d_new (aran_development3d_new (0, p) fixes the order p,
- * aran/arandevelopment3d.c:64-73).  The operator functions are the callbacks
- * of the reference (aran/arandevelopment3d.c:169-552); with the GPU library
- * their addresses select what aran_solver3d_solve runs on the device (the
- * rotate or the kkylin flavour of M2M/M2L/L2L, the Newton P2M and L2P).
- * Calling an operator directly on host developments is not supported: it
- * leaves its output untouched and sets aran_gpu_last_error().
+ * aran/arandevelopment3d.c:64-73).  Handed to aran_solver3d_set_functions the
+ * operator addresses select what aran_solver3d_solve runs on the device (the
+ * normal, kkylin or rotate flavour of M2M/M2L/L2L; the Newton P2M and L2P).
+ * Called directly on host developments the operators run on the GPU one
+ * launch per call (see aransphericalseriesd.h).
  */
 #ifndef ARAN_COMPAT_DEVELOPMENT3D_H
 #define ARAN_COMPAT_DEVELOPMENT3D_H
@@ -17,6 +16,7 @@
 #include <stdio.h>
 
 #include <aran/aran.h>
+#include <aran/aransphericalseriesd.h>
 #include <vsg/vsgd.h>
 
 G_BEGIN_DECLS
@@ -26,10 +26,8 @@ G_BEGIN_DECLS
 typedef struct _AranDevelopment3d AranDevelopment3d;
 struct _AranDevelopment3d
 {
-  guint8 posdeg;          /* multipole series: aran_spherical_seriesd_new (posdeg, negdeg) */
-  guint8 negdeg;
-  gcomplex128 *multipole; /* LibAran layout, ((posdeg+1)(posdeg+2)+negdeg(negdeg+1))/2 terms */
-  gcomplex128 *local;     /* degree max (posdeg, negdeg) */
+  AranSphericalSeriesd *multipole;   /* series (posdeg, negdeg) */
+  AranSphericalSeriesd *local;       /* series (max (posdeg, negdeg), 0) */
 };
 
 GType aran_development3d_get_type (void);
@@ -62,11 +60,25 @@ void aran_development3d_m2l_rotate (const VsgPRTree3dNodeInfo *src_node, AranDev
                                     const VsgPRTree3dNodeInfo *dst_node, AranDevelopment3d *dst);
 void aran_development3d_l2l_rotate (const VsgPRTree3dNodeInfo *src_node, AranDevelopment3d *src,
                                     const VsgPRTree3dNodeInfo *dst_node, AranDevelopment3d *dst);
+gcomplex128 aran_development3d_multipole_evaluate (const VsgPRTree3dNodeInfo *devel_node,
+                                                   AranDevelopment3d *devel,
+                                                   const VsgVector3d *pos);
 gcomplex128 aran_development3d_local_evaluate (const VsgPRTree3dNodeInfo *devel_node,
                                                AranDevelopment3d *devel, const VsgVector3d *pos);
+gcomplex128 aran_development3d_m2p (const VsgPRTree3dNodeInfo *devel_node,
+                                    AranDevelopment3d *devel, const VsgVector3d *pos);
+gcomplex128 aran_development3d_l2p (const VsgPRTree3dNodeInfo *devel_node,
+                                    AranDevelopment3d *devel, const VsgVector3d *pos);
+void aran_development3d_multipole_gradient_evaluate (const VsgPRTree3dNodeInfo *devel_node,
+                                                     AranDevelopment3d *devel,
+                                                     const VsgVector3d *pos, VsgVector3d *grad);
 void aran_development3d_local_gradient_evaluate (const VsgPRTree3dNodeInfo *devel_node,
                                                  AranDevelopment3d *devel,
                                                  const VsgVector3d *pos, VsgVector3d *grad);
+void aran_development3d_m2pv (const VsgPRTree3dNodeInfo *devel_node, AranDevelopment3d *devel,
+                              const VsgVector3d *pos, VsgVector3d *grad);
+void aran_development3d_l2pv (const VsgPRTree3dNodeInfo *devel_node, AranDevelopment3d *devel,
+                              const VsgVector3d *pos, VsgVector3d *grad);
 
 G_END_DECLS
 
