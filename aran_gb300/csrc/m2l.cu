@@ -74,6 +74,25 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mb, uint32_t parity) {
   return false;
 }
 
+// 8-byte asynchronous global -> shared copy (one complex FP32 coefficient;
+// FP64 coefficients take two)
+template <typename T>
+__device__ __forceinline__ void cp_async_cplx(cplx<T> *dst, const cplx<T> *src) {
+  if (sizeof(cplx<T>) == 8) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src)
+                 : "memory");
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src)
+                 : "memory");
+  }
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 struct M2LOffsets {
   int ef, ei, ph, rp, vv, stride;  // in T units; ef/ei: (E, O) pairs in source-order planes
 };
@@ -227,10 +246,10 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[g][r] = cmake<T>(0, 0);
   // column g: src (phased multipole) and tr (translated, m-major slots)
-  // share region A, rot follows
+  // share region A, rot follows; between the vertical stage and the next
+  // direction's phase stage the rot region holds the next source multipoles,
+  // copied in asynchronously (cp.async) while the rotation back runs
   cplx<T> *cbuf = wbuf + (size_t)w * G * (nm + nl);
-  // the next direction's multipoles are fetched one direction ahead
-  cplx<T> pre[G][R];
   int next_i = 0, next_s[G];
   auto find_next = [&](int from) {
     for (next_i = from; next_i < nact; ++next_i) {
@@ -249,9 +268,14 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         int c = lane + 32 * r;
-        pre[g][r] = (next_i < nact && next_s[g] >= 0 && c < nm) ? mult[(size_t)next_s[g] * nm + c]
-                                                                : cmake<T>(0, 0);
+        if (c >= nm) continue;
+        cplx<T> *dst = cbuf + g * (nm + nl) + nl + c;
+        if (next_i < nact && next_s[g] >= 0)
+          cp_async_cplx(dst, mult + (size_t)next_s[g] * nm + c);
+        else
+          *dst = cmake<T>(0, 0);
       }
+    cp_async_commit();
   };
   find_next(0);
   prefetch();
@@ -268,6 +292,8 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
       const T *ph = tb + D.ph;
       const T *EOf = tb + D.ef;
       const T *EOi = tb + D.ei;
+      cp_async_wait_all();
+      __syncwarp();
       // z-phase of the source multipoles: e^{i m phi}
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -277,13 +303,12 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
           T cr = ph[2 * m], ci = ph[2 * m + 1];
 #pragma unroll
           for (int g = 0; g < G; ++g) {
-            cplx<T> v = pre[g][r];
+            cplx<T> v = cbuf[g * (nm + nl) + nl + c];
             cbuf[g * (nm + nl) + c] = cmake<T>(v.re * cr - v.im * ci, v.re * ci + v.im * cr);
           }
         }
       }
       find_next(i + 1);
-      prefetch();
       __syncwarp();
       // rotation to the z axis (degrees < p)
 #pragma unroll
@@ -339,6 +364,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
         }
       }
       __syncwarp();
+      prefetch();   // rot region is free until the next phase stage
       // rotation back (degrees <= p), conjugate z-phase, accumulate
 #pragma unroll
       for (int r = 0; r < R; ++r) {
