@@ -53,6 +53,47 @@ FMM_HD void mmajor_lm(int k, int p, int &l, int &m) {
   l = m + k;
 }
 
+// Compact M2L tables.  Rotation planes: plane m (source order) holds the
+// entries of the coefficients c = (l, m'), l >= m, which in tri order are
+// c = tri(m) .. nc-1; plane m starts at m2l_plane_off(nc, m), entry c at
+// m2l_plane_off(nc, m) + c - tri(m).
+FMM_HD int m2l_plane_off(int nc, int m) { return m * nc - ((m - 1) * m * (m + 1)) / 6; }
+// Vertical rows: row n (source degree) holds the m-major slots k with
+// m(k) <= n, i.e. k < (n+1)(p+1) - n(n+1)/2; row n starts at m2l_vrow_off.
+FMM_HD int m2l_vrow_len(int p, int n) { return (n + 1) * (p + 1) - ((n + 1) * n) / 2; }
+FMM_HD int m2l_vrow_off(int p, int n) {
+  return (p + 1) * (n * (n + 1) / 2) - ((n + 1) * n * (n - 1)) / 6;
+}
+
+// Stream layout of the lane-parallel M2L tables (FP32, order p), one block
+// per offset, in the order the kernel consumes it: the z-phases (cos, sin)
+// of m = 0..p; the forward rotation terms (l < p, m' <= l, m <= l) in groups
+// of four, each group four even-part factors then four odd-part factors;
+// the vertical factors times the offset's radial powers, terms
+// (m <= p, j = m..p, n = m..p-1); the backward rotation terms (l <= p),
+// grouped like the forward ones.
+__host__ __device__ constexpr int m2l_lane_nf(int p) { return p * (p + 1) * (2 * p + 1) / 6; }
+__host__ __device__ constexpr int m2l_lane_nv(int p) { return p * (p + 1) * (p + 2) / 3; }
+__host__ __device__ constexpr int m2l_lane_nb(int p) {
+  return (p + 1) * (p + 2) * (2 * p + 3) / 6;
+}
+__host__ __device__ constexpr int m2l_lane_f(int p) { return (2 * (p + 1) + 3) & ~3; }
+__host__ __device__ constexpr int m2l_lane_v(int p) {
+  return m2l_lane_f(p) + 8 * ((m2l_lane_nf(p) + 3) / 4);
+}
+__host__ __device__ constexpr int m2l_lane_b(int p) {
+  return m2l_lane_v(p) + 4 * ((m2l_lane_nv(p) + 3) / 4);
+}
+__host__ __device__ constexpr int m2l_lane_stride(int p) {
+  return m2l_lane_b(p) + 8 * ((m2l_lane_nb(p) + 3) / 4);
+}
+// index of the first vertical term of order m
+__host__ __device__ constexpr int m2l_lane_vpre(int p, int m) {
+  return m2l_lane_nv(p) - m2l_lane_nv(p - m);
+}
+// orders with a lane-parallel M2L kernel
+__host__ __device__ constexpr bool m2l_lane_order(int p) { return p == 8 || p == 12; }
+
 FMM_HD int sq_off(int l) { return (l * (l + 1) * (2 * l + 1)) / 6; }  // sum_{i<l} (i+1)^2
 FMM_HD int sq_size(int L) { return sq_off(L); }
 

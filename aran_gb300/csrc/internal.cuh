@@ -129,6 +129,7 @@ struct OpTables {
   DBuf<T> vl;       // tri(p+1)*(p+1) (L2L vertical, 2^-l folded)
   DBuf<T> gz, gm;   // gradient coefficients
   DBuf<T> dir_m2l, dir_m2m, dir_l2l;
+  DBuf<T> dir_lanes; // lane-parallel M2L stream tables (FP32, m2l_lane_order)
   DBuf<uint8_t> lm; // (l,m) of coefficient index, 2*tri(p+1)
 };
 
@@ -200,6 +201,8 @@ void build_kkylin_tables(AranGpuSolver3d *s);
 void kkylin_pass(AranGpuSolver3d *s, int stage);
 // m2l.cu
 void launch_m2l(AranGpuSolver3d *s, cudaStream_t st);
+bool launch_m2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, const cplx<float> *mult,
+                      cplx<float> *loc, cudaStream_t st);
 // p2p.cu
 constexpr int kBigRange = 2048;   // near ranges above this many particles are chunked
 void build_p2p_work(AranGpuSolver3d *s);

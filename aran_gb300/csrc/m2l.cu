@@ -20,6 +20,7 @@
 // do not fit in shared memory (NST = 0) the warps read the offset tables
 // and vertical factors straight from global memory (L2-resident).
 #include "internal.cuh"
+#include "async.cuh"
 
 namespace aran {
 
@@ -30,76 +31,16 @@ namespace {
 __constant__ uint16_t c_dir_codes[316];
 __constant__ int8_t c_dir_vec[316 * 3];
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *mb, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mb)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void fence_mbar_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *mb, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mb)),
-               "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *mb) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(mb))
-      : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *mb, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(mb)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// bounded wait: gives up after ~1M polls (each poll may itself suspend)
-__device__ __forceinline__ bool mbar_wait(uint64_t *mb, uint32_t parity) {
-  for (int i = 0; i < (1 << 20); ++i)
-    if (mbar_try_wait(mb, parity)) return true;
-  return false;
-}
-
-// 8-byte asynchronous global -> shared copy (one complex FP32 coefficient;
-// FP64 coefficients take two)
+// asynchronous copy of one complex coefficient (8 bytes FP32, 16 bytes FP64)
 template <typename T>
 __device__ __forceinline__ void cp_async_cplx(cplx<T> *dst, const cplx<T> *src) {
-  if (sizeof(cplx<T>) == 8) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src)
-                 : "memory");
-  } else {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src)
-                 : "memory");
-  }
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.wait_all;" ::: "memory");
+  if (sizeof(cplx<T>) == 8) cp_async8(dst, src);
+  else cp_async16(dst, src);
 }
 
 struct M2LOffsets {
   int ef, ei, ph, rp, vv, stride;  // in T units; ef/ei: (E, O) pairs in source-order planes
 };
-
-__device__ __forceinline__ void mbar_arrive(uint64_t *mb) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mb)) : "memory");
-}
 
 constexpr int kSibWarps = 8;   // consumers: one per child of the parent
 constexpr int kMaxRounds = ((kMaxOrder + 1) * (kMaxOrder + 2) / 2 + 31) / 32;
@@ -316,14 +257,14 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
         int c = lane + 32 * r;
         if (c < nm) {
           const int l = lm[2 * c];
-          const T *col0 = EOf + 2 * c;     // plane m at col0 + 2 m nm
+          const T *e = EOf + 2 * c;        // plane 0; plane m+1 is nm - tri(m+1) further
+          int step = 2 * (nm - 1);
           const int so = tri(l);
           T re[G], im[G];
 #pragma unroll
           for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
 #pragma unroll 2
-          for (int m = 0; m <= l; ++m) {
-            const T *e = col0 + 2 * m * nm;
+          for (int m = 0; m <= l; ++m, e += step, step -= 2 * (m + 1)) {
             const T ee = e[0], eo = e[1];
 #pragma unroll
             for (int g = 0; g < G; ++g) {
@@ -343,14 +284,15 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
         int k = lane + 32 * r;
         if (k < nl) {
           const int m = vmap[2 * k + 1];
-          // vertical factor times radial power for source degree n: vcol[n * nl]
-          const T *vcol = tb + D.vv + k;
+          // vertical factor times radial power for source degree n: row n of vv
+          const T *vcol = tb + D.vv + m2l_vrow_off(p, m) + k;
+          int vstep = m2l_vrow_len(p, m);
           T re[G], im[G];
 #pragma unroll
           for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
 #pragma unroll 2
-          for (int n = m; n < p; ++n) {
-            const T f = vcol[n * nl];
+          for (int n = m; n < p; ++n, vcol += vstep, vstep += p + 1 - n) {
+            const T f = vcol[0];
             const int sidx = nl + tri(n, m);
 #pragma unroll
             for (int g = 0; g < G; ++g) {
@@ -371,15 +313,15 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
         int c = lane + 32 * r;
         if (c < nl) {
           const int l = lm[2 * c], mp = lm[2 * c + 1];
-          const T *col0 = EOi + 2 * c;     // plane m at col0 + 2 m nl
+          const T *e = EOi + 2 * c;        // plane 0; plane m+1 is nl - tri(m+1) further
+          int step = 2 * (nl - 1);
           T re[G], im[G];
 #pragma unroll
           for (int g = 0; g < G; ++g) re[g] = im[g] = 0;
           // slot of (l, m) in m-major order: m(p+1) - m(m-1)/2 + (l - m)
           int slot = l;
 #pragma unroll 2
-          for (int m = 0; m <= l; ++m) {
-            const T *e = col0 + 2 * m * nl;
+          for (int m = 0; m <= l; ++m, e += step, step -= 2 * (m + 1)) {
             const T ee = e[0], eo = e[1];
 #pragma unroll
             for (int g = 0; g < G; ++g) {
@@ -472,6 +414,9 @@ void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const cplx<T> *mult, cplx<T> 
               cudaStream_t st) {
   DevTree &t = s->tree;
   if (t.n_parents == 0) return;
+  if constexpr (sizeof(T) == 4) {
+    if (launch_m2l_lanes(s, tb, mult, loc, st)) return;
+  }
   upload_codes(s->device);
   const int p = s->cfg.order;
   M2LOffsets D;

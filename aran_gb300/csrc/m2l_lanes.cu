@@ -1,0 +1,375 @@
+// m2l_lanes.cu -- lane-parallel M2L for the FP32 path at the orders
+// m2l_lane_order(p) accepts.  Same operator as m2l.cu (the "point and shoot"
+// translation of aran_spherical_seriesd_to_local_rotate,
+// aran/aransphericalseriesd-rotate.c:165-207, applied by far_func,
+// aran/aransolver3d.c:333-354) with the work laid out the other way round:
+//
+//  * after the z-phase, the rotation, the translation along z and the
+//    rotation back never mix real and imaginary parts (the even/odd Wigner
+//    blocks act on the real/imaginary parts, the vertical factors are real),
+//    so one lane carries the real part and its neighbour the imaginary part
+//    of one (target, source) translation;
+//  * a warp takes child w of the 16 parents of its CTA (lane pair i <->
+//    parent i), so at a given offset all 16 lane pairs apply the same table:
+//    every table read is a broadcast of 16 bytes (four factors) from shared
+//    memory, and a lane's whole series stays in registers, the order being a
+//    compile-time constant;
+//  * the two lanes of a pair exchange their rotated-back parts with one
+//    shuffle to apply the conjugate z-phase, and each lane accumulates its
+//    part of the target's local in shared memory (one word per lane, no
+//    conflicts), in the same offset order for every run.
+//
+// The offset tables stream through a two-slot ring of TMA bulk copies, as
+// in m2l.cu; the next offset's source multipoles are copied into shared
+// memory by cp.async while the current one is translated.  Every mbarrier
+// wait is bounded; a wait that gives up sets the error word and the CTA
+// stops.
+#include "internal.cuh"
+#include "async.cuh"
+
+namespace aran {
+
+namespace {
+
+constexpr int kLanePar = 16;     // parents per CTA: lane pair i <-> parent i
+constexpr int kLaneWarps = 8;    // consumer warps: warp w <-> child w
+constexpr int kLaneNst = 2;      // table ring slots
+constexpr unsigned kFull = 0xffffffffu;
+
+template <int P>
+struct LaneDims {
+  static constexpr int NM = P * (P + 1) / 2;        // multipole coefficients
+  static constexpr int NL = (P + 1) * (P + 2) / 2;  // local coefficients
+  static constexpr int NMP = (NM + 1) & ~1;         // staged multipole stride (16-byte rows)
+  static constexpr int STRIDE = m2l_lane_stride(P);
+};
+
+template <int P>
+constexpr size_t lanes_smem() {
+  using D = LaneDims<P>;
+  size_t off = (size_t)kLaneNst * D::STRIDE * sizeof(float);
+  off += 2 * kLaneNst * sizeof(uint64_t);
+  off += (size_t)kLaneWarps * kLanePar * D::NMP * sizeof(cplx<float>);
+  off += (size_t)kLaneWarps * D::NL * 32 * sizeof(float);
+  off += (size_t)kLanePar * 216 * sizeof(int);
+  off += 16 * sizeof(unsigned) + 320 * sizeof(uint16_t) + 320 * sizeof(uint16_t) + 320 * 3;
+  return off + 64;
+}
+
+__device__ __forceinline__ float sel4(const float4 &v, int k) {
+  return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+}
+
+template <int P>
+__global__ void __launch_bounds__(32 * (kLaneWarps + 1))
+    k_m2l_lanes(int nparents, const int *__restrict__ parents, const int *__restrict__ child,
+                const int *__restrict__ begin, const int *__restrict__ end,
+                const int *__restrict__ col, const int *__restrict__ ncol,
+                const int *__restrict__ ijk, const uint8_t *__restrict__ depth,
+                const float *__restrict__ dirs, double scale_e,
+                const cplx<float> *__restrict__ mult, cplx<float> *__restrict__ loc,
+                int *__restrict__ err) {
+  using D = LaneDims<P>;
+  constexpr int NM = D::NM, NL = D::NL, NMP = D::NMP, STRIDE = D::STRIDE;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // shared layout: ring tables | full[NST] | empty[NST] | staged multipoles
+  // [warp][pair][NMP] | local parts [warp][coefficient][lane] | 16 6x6x6
+  // source grids | offset mask | active offsets | offset codes | offset vectors
+  size_t off = 0;
+  float *tab = reinterpret_cast<float *>(smem_raw);
+  off += (size_t)kLaneNst * STRIDE * sizeof(float);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + off);
+  uint64_t *empty = full + kLaneNst;
+  off += 2 * kLaneNst * sizeof(uint64_t);
+  cplx<float> *stg = reinterpret_cast<cplx<float> *>(smem_raw + off);
+  off += (size_t)kLaneWarps * kLanePar * NMP * sizeof(cplx<float>);
+  float *accs = reinterpret_cast<float *>(smem_raw + off);
+  off += (size_t)kLaneWarps * NL * 32 * sizeof(float);
+  int *grid = reinterpret_cast<int *>(smem_raw + off);
+  off += (size_t)kLanePar * 216 * sizeof(int);
+  unsigned *mask = reinterpret_cast<unsigned *>(smem_raw + off);
+  off += 16 * sizeof(unsigned);
+  uint16_t *active = reinterpret_cast<uint16_t *>(smem_raw + off);
+  off += 320 * sizeof(uint16_t);
+  uint16_t *dcode = reinterpret_cast<uint16_t *>(smem_raw + off);
+  off += 320 * sizeof(uint16_t);
+  int8_t *dvec = reinterpret_cast<int8_t *>(smem_raw + off);
+  __shared__ int s_nact;
+
+  for (int i = threadIdx.x; i < kLanePar * 216; i += blockDim.x) grid[i] = -1;
+  for (int i = threadIdx.x; i < kLaneWarps * NL * 32; i += blockDim.x) accs[i] = 0.f;
+  if (threadIdx.x < 16) mask[threadIdx.x] = 0u;
+  // offsets (dx, dy, dz) in [-3,3]^3 minus [-1,1]^3, dz slowest: offset
+  // index = code - (near codes below it); code = (dx+3) + 7 (dy+3) + 49 (dz+3)
+  for (int code = threadIdx.x; code < 343; code += blockDim.x) {
+    const int a = code % 7, b = (code / 7) % 7, c = code / 49;
+    auto in = [](int v) { return v >= 2 && v <= 4; };
+    auto below = [](int v) { return v < 2 ? 0 : (v > 4 ? 3 : v - 2); };
+    if (in(a) && in(b) && in(c)) continue;
+    const int nb = 9 * below(c) + (in(c) ? 3 * below(b) + (in(b) ? below(a) : 0) : 0);
+    const int di = code - nb;
+    dcode[di] = (uint16_t)code;
+    dvec[3 * di] = (int8_t)(a - 3);
+    dvec[3 * di + 1] = (int8_t)(b - 3);
+    dvec[3 * di + 2] = (int8_t)(c - 3);
+  }
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < kLaneNst; ++b) {
+      mbar_init(&full[b], 1);
+      mbar_init(&empty[b], kLaneWarps);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  // the parents of this CTA: their colleagues' children fill the grids
+  for (int g = 0; g < kLanePar; ++g) {
+    const int pidx = blockIdx.x * kLanePar + g;
+    if (pidx >= nparents) break;
+    const int Pn = parents[pidx];
+    const int pi = ijk[3 * Pn], pj = ijk[3 * Pn + 1], pk = ijk[3 * Pn + 2];
+    const int nc = ncol[Pn];
+    for (int e = threadIdx.x; e < nc * 8; e += blockDim.x) {
+      const int q = col[27 * Pn + e / 8];
+      const int qc = child[q];
+      if (qc < 0) continue;
+      const int o = e & 7;
+      const int s = qc + o;
+      if (end[s] == begin[s]) continue;
+      const int gx = 2 * (ijk[3 * q] - pi + 1) + (o & 1);
+      const int gy = 2 * (ijk[3 * q + 1] - pj + 1) + ((o >> 1) & 1);
+      const int gz = 2 * (ijk[3 * q + 2] - pk + 1) + ((o >> 2) & 1);
+      grid[g * 216 + gx + 6 * (gy + 6 * gz)] = s;
+    }
+  }
+  __syncthreads();
+  // lane pair i = lane / 2 <-> parent i; h = 0 real part, 1 imaginary part
+  const int pi_ = lane >> 1, h = lane & 1;
+  int tgt = -1;
+  {
+    const int pidx = blockIdx.x * kLanePar + pi_;
+    if (w < kLaneWarps && pidx < nparents) {
+      const int t = child[parents[pidx]] + w;
+      if (end[t] > begin[t]) tgt = t;
+    }
+  }
+  const int tx = 2 + (w & 1), ty = 2 + ((w >> 1) & 1), tz = 2 + ((w >> 2) & 1);
+  auto source_of = [&](int di) -> int {
+    if (tgt < 0) return -1;
+    const int cx = tx - dvec[3 * di], cy = ty - dvec[3 * di + 1], cz = tz - dvec[3 * di + 2];
+    if (cx < 0 || cx > 5 || cy < 0 || cy > 5 || cz < 0 || cz > 5) return -1;
+    return grid[pi_ * 216 + cx + 6 * (cy + 6 * cz)];
+  };
+  if (w < kLaneWarps)
+    for (int di = 0; di < 316; ++di) {
+      const unsigned any = __ballot_sync(kFull, source_of(di) >= 0);
+      if (lane == 0 && any) atomicOr(&mask[di >> 5], 1u << (di & 31));
+    }
+  __syncthreads();
+  for (int di = threadIdx.x; di < 316; di += blockDim.x) {
+    const unsigned m = mask[di >> 5];
+    if ((m >> (di & 31)) & 1u) {
+      int pos = __popc(m & ((1u << (di & 31)) - 1u));
+      for (int k = 0; k < (di >> 5); ++k) pos += __popc(mask[k]);
+      active[pos] = (uint16_t)di;
+    }
+  }
+  if (threadIdx.x == 0) {
+    int tot = 0;
+    for (int k = 0; k < 10; ++k) tot += __popc(mask[k]);
+    s_nact = tot;
+  }
+  __syncthreads();
+  const int nact = s_nact;
+
+  if (w == kLaneWarps) {
+    // producer warp: stream the offset tables through the ring
+    if (lane == 0)
+      for (int i = 0; i < nact; ++i) {
+        const int b = i % kLaneNst;
+        if (i >= kLaneNst && !mbar_wait(&empty[b], ((i / kLaneNst) - 1) & 1)) {
+          atomicExch(err, 1);
+          break;
+        }
+        mbar_expect_tx(&full[b], STRIDE * (uint32_t)sizeof(float));
+        bulk_g2s(tab + (size_t)b * STRIDE, dirs + (size_t)dcode[active[i]] * STRIDE,
+                 STRIDE * (uint32_t)sizeof(float), &full[b]);
+      }
+    return;
+  }
+
+  cplx<float> *my_stg = stg + (size_t)(w * kLanePar + pi_) * NMP;
+  float *my_acc = accs + (size_t)w * NL * 32 + lane;   // coefficient c at my_acc[32 c]
+  int next_i = 0, next_s = -1;
+  auto find_next = [&](int from) {
+    for (next_i = from; next_i < nact; ++next_i) {
+      next_s = source_of(active[next_i]);
+      if (__any_sync(kFull, next_s >= 0)) break;
+    }
+  };
+  // the two lanes of a pair copy alternate 16-byte rows of the source
+  auto prefetch = [&]() {
+    if (next_i >= nact) return;
+    if (next_s >= 0) {
+      const cplx<float> *src = mult + (size_t)next_s * NM;
+      if (NM % 2 == 0) {
+        for (int q = h; q < NM / 2; q += 2) cp_async16(my_stg + 2 * q, src + 2 * q);
+      } else {
+        for (int c = h; c < NM; c += 2) cp_async8(my_stg + c, src + c);
+      }
+    } else {
+      for (int c = h; c < NM; c += 2) my_stg[c] = cmake<float>(0.f, 0.f);
+    }
+    cp_async_commit();
+  };
+  find_next(0);
+  prefetch();
+
+  for (int it = 0; it < nact; ++it) {
+    const int b = it % kLaneNst;
+    const bool ok = __all_sync(kFull, mbar_wait(&full[b], (it / kLaneNst) & 1));
+    if (!ok) {
+      if (lane == 0) atomicExch(err, 1);
+      break;
+    }
+    if (it == next_i) {
+      const float *tb = tab + (size_t)b * STRIDE;
+      const float2 *ph2 = reinterpret_cast<const float2 *>(tb);    // (cos, sin) of m phi
+      cp_async_wait_all();
+      __syncwarp();
+      // z-phase and rotation to the z axis (degrees < p): this lane's part
+      // of the source is x.re pa + x.im pb
+      float y[NM];
+      {
+        float pa[P], pb[P];
+#pragma unroll
+        for (int m = 0; m < P; ++m) {
+          const float2 e = ph2[m];
+          pa[m] = h ? e.y : e.x;
+          pb[m] = h ? e.x : -e.y;
+        }
+        const float4 *X4 = reinterpret_cast<const float4 *>(my_stg);
+        const float4 *F4 = reinterpret_cast<const float4 *>(tb + m2l_lane_f(P)) + h;
+        float4 xq = make_float4(0.f, 0.f, 0.f, 0.f), fq = xq;
+#pragma unroll
+        for (int l = 0; l < P; ++l) {
+          float xp[P];
+#pragma unroll
+          for (int m = 0; m <= l; ++m) {
+            const int c = l * (l + 1) / 2 + m;
+            if ((c & 1) == 0) xq = X4[c >> 1];
+            const float xr = (c & 1) ? xq.z : xq.x, xi = (c & 1) ? xq.w : xq.y;
+            xp[m] = fmaf(xr, pa[m], xi * pb[m]);
+          }
+#pragma unroll
+          for (int mp = 0; mp <= l; ++mp) {
+            float a = 0.f;
+#pragma unroll
+            for (int m = 0; m <= l; ++m) {
+              const int t = sq_off(l) + mp * (l + 1) + m;
+              if ((t & 3) == 0) fq = F4[2 * (t >> 2)];
+              a = fmaf(sel4(fq, t & 3), xp[m], a);
+            }
+            y[l * (l + 1) / 2 + mp] = a;
+          }
+        }
+      }
+      find_next(it + 1);
+      __syncwarp();           // both lanes of every pair are done with the staged source
+      prefetch();
+      // translation along z: z(j, m) = sum_n V(j, m, n) y(n, m), m-major slots
+      float z[NL];
+      {
+        const float4 *V4 = reinterpret_cast<const float4 *>(tb + m2l_lane_v(P));
+        float4 vq = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int m = 0; m <= P; ++m)
+#pragma unroll
+          for (int j = m; j <= P; ++j) {
+            float a = 0.f;
+#pragma unroll
+            for (int n = m; n < P; ++n) {
+              const int t = m2l_lane_vpre(P, m) + (j - m) * (P - m) + (n - m);
+              if ((t & 3) == 0) vq = V4[t >> 2];
+              a = fmaf(sel4(vq, t & 3), y[n * (n + 1) / 2 + m], a);
+            }
+            z[m * (P + 1) - m * (m - 1) / 2 + (j - m)] = a;
+          }
+      }
+      // rotation back (degrees <= p), conjugate z-phase, accumulate:
+      // real part += a cos + b sin, imaginary part += a cos - b sin, with a
+      // this lane's part and b the partner's
+      {
+        float cph[P + 1], sph[P + 1];
+#pragma unroll
+        for (int m = 0; m <= P; ++m) {
+          const float2 e = ph2[m];
+          cph[m] = e.x;
+          sph[m] = h ? -e.y : e.y;
+        }
+        const float4 *B4 = reinterpret_cast<const float4 *>(tb + m2l_lane_b(P)) + h;
+        float4 bq = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int l = 0; l <= P; ++l)
+#pragma unroll
+          for (int mp = 0; mp <= l; ++mp) {
+            float a = 0.f;
+#pragma unroll
+            for (int m = 0; m <= l; ++m) {
+              const int t = sq_off(l) + mp * (l + 1) + m;
+              if ((t & 3) == 0) bq = B4[2 * (t >> 2)];
+              a = fmaf(sel4(bq, t & 3), z[m * (P + 1) - m * (m - 1) / 2 + (l - m)], a);
+            }
+            const float o = __shfl_xor_sync(kFull, a, 1);
+            float *slot = my_acc + 32 * (l * (l + 1) / 2 + mp);
+            *slot += fmaf(a, cph[mp], o * sph[mp]);
+          }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[b]);
+  }
+  cp_async_wait_all();
+  if (nact > 0 && tgt >= 0) {
+    const float ih = (float)((double)(1ull << depth[tgt]) / scale_e);   // 2^depth / scale
+    float *lo = reinterpret_cast<float *>(loc) + (size_t)tgt * NL * 2 + h;
+    for (int c = 0; c < NL; ++c) lo[2 * c] = my_acc[32 * c] * ih;
+  }
+}
+
+template <int P>
+bool launch_p(AranGpuSolver3d *s, OpTables<float> &tb, const cplx<float> *mult,
+              cplx<float> *loc, cudaStream_t st) {
+  DevTree &t = s->tree;
+  const size_t sm = lanes_smem<P>();
+  int dev_smem = 0;
+  ACHECK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
+  if ((int)sm > dev_smem) return false;
+  ACHECK(cudaFuncSetAttribute(k_m2l_lanes<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sm));
+  k_m2l_lanes<P><<<ceil_div(t.n_parents, kLanePar), 32 * (kLaneWarps + 1), sm, st>>>(
+      t.n_parents, t.parents.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
+      t.ijk.ptr, t.depth.ptr, tb.dir_lanes.ptr, s->scale_e, mult, loc, s->err_dev.ptr);
+  ACHECK(cudaGetLastError());
+  s->launches++;
+  return true;
+}
+
+}  // namespace
+
+// Runs the M2L pass with the lane-parallel kernel when the order has one
+// (and ARAN_M2L_KERNEL is not "sibling"); false leaves it to m2l.cu.
+bool launch_m2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, const cplx<float> *mult,
+                      cplx<float> *loc, cudaStream_t st) {
+  const int p = s->cfg.order;
+  if (!m2l_lane_order(p) || tb.dir_lanes.ptr == nullptr || s->tree.n_parents == 0) return false;
+  const char *pick = getenv("ARAN_M2L_KERNEL");
+  if (pick && strcmp(pick, "sibling") == 0) return false;
+  switch (p) {
+    case 8: return launch_p<8>(s, tb, mult, loc, st);
+    case 12: return launch_p<12>(s, tb, mult, loc, st);
+    default: return false;
+  }
+}
+
+}  // namespace aran

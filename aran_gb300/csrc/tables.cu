@@ -29,14 +29,14 @@ __host__ __device__ DirLayout dir_layout(int p, int kind) {
     d.Lf = p; d.Li = p + 1; d.nrp = 2 * p + 2;
     d.ef = 0;
     d.of = -1;
-    d.ei = 2 * d.Lf * tri(d.Lf);
+    d.ei = 2 * m2l_plane_off(tri(d.Lf), d.Lf);
     d.oi = -1;
-    d.ph = d.ei + 2 * d.Li * tri(d.Li);
+    d.ph = d.ei + 2 * m2l_plane_off(tri(d.Li), d.Li);
     d.rp = d.ph + 2 * (p + 1);
     // vertical factors times the radial powers of this offset, m-major
-    // slot k of the local, source degree n: vv[n * tri(p+1) + k]
+    // slot k of the local, source degree n: vv[m2l_vrow_off(p, n) + k]
     d.vv = ((d.rp + d.nrp) + 3) & ~3;
-    d.stride = ((d.vv + tri(p + 1) * p) + 3) & ~3;
+    d.stride = ((d.vv + m2l_vrow_off(p, p)) + 3) & ~3;
     return d;
   } else if (kind == 1) { d.Lf = p; d.Li = p; d.nrp = p + 1; }          // M2M
   else { d.Lf = p + 1; d.Li = p + 1; d.nrp = p + 2; }                 // L2L
@@ -117,10 +117,51 @@ __global__ void k_m2l_vertical(int p, int ndir, int stride, int rp_off, int vv_o
   if (i >= (int64_t)ndir * nl * p) return;
   const int d = (int)(i / (nl * p)), e = (int)(i % (nl * p));
   const int k = e % nl, n = e / nl;
+  if (k >= m2l_vrow_len(p, n)) return;   // slot of order m > n: not stored
   int l, m;
   mmajor_lm(k, p, l, m);
   T *tb = dirs + (size_t)d * stride;
-  tb[vv_off + e] = vt[tri(l, m) * p + n] * tb[rp_off + l + n + 1];
+  tb[vv_off + m2l_vrow_off(p, n) + k] = vt[tri(l, m) * p + n] * tb[rp_off + l + n + 1];
+}
+
+// lane-parallel M2L stream tables (layout: m2l_lane_* in fmm_math.cuh),
+// gathered from the FP32 offset tables: same factors, consumption order
+__global__ void k_m2l_lane_tables(int p, int ndir, const float *__restrict__ src, DirLayout D,
+                                  float *__restrict__ dst) {
+  const int stride = m2l_lane_stride(p);
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)ndir * stride) return;
+  const int d = (int)(i / stride), e = (int)(i % stride);
+  const float *s = src + (size_t)d * D.stride;
+  const int F = m2l_lane_f(p), V = m2l_lane_v(p), B = m2l_lane_b(p);
+  // q-th float of a grouped rotation stream: term 4 (q / 8) + q % 4, part (q / 4) % 2
+  auto rot = [&](int q, int nterm, int nc, int base) -> float {
+    const int t = 4 * (q >> 3) + (q & 3), part = (q >> 2) & 1;
+    if (t >= nterm) return 0.f;
+    int l = 0;
+    while (sq_off(l + 1) <= t) ++l;
+    const int r = t - sq_off(l), mp = r / (l + 1), m = r % (l + 1);
+    return s[base + 2 * (m2l_plane_off(nc, m) + tri(l, mp) - tri(m)) + part];
+  };
+  float v = 0.f;
+  if (e < F) {
+    if (e < 2 * (p + 1)) v = s[D.ph + e];
+  } else if (e < V) {
+    v = rot(e - F, m2l_lane_nf(p), tri(p), D.ef);
+  } else if (e < B) {
+    const int t = e - V;
+    if (t < m2l_lane_nv(p)) {
+      int m = 0;
+      while (m2l_lane_vpre(p, m + 1) <= t) ++m;
+      const int r = t - m2l_lane_vpre(p, m);
+      const int j = m + r / (p - m), n = m + r % (p - m);
+      const int k = m * (p + 1) - m * (m - 1) / 2 + (j - m);   // m-major slot of (j, m)
+      v = s[D.vv + m2l_vrow_off(p, n) + k];
+    }
+  } else {
+    v = rot(e - B, m2l_lane_nb(p), tri(p + 1), D.ei);
+  }
+  dst[i] = v;
 }
 
 // one thread per direction: kind 0 = M2L offset code, 1 = M2M octant, 2 = L2L octant
@@ -163,12 +204,11 @@ __global__ void k_dir_tables(int p, int kind, int ndir, double ex, double ey, do
   // output coefficient each, read consecutive words at every step m
   auto put_cm = [&](int Lb, int base) {
     const int nc = tri(Lb);
-    for (int i = 0; i < 2 * Lb * nc; ++i) o[base + i] = (T)0;
     for (int l = 0; l < Lb; ++l)
       for (int mp = 0; mp <= l; ++mp)
         for (int m = 0; m <= l; ++m) {
           int src = sq_off(l) + mp * (l + 1) + m;
-          int dst = m * nc + tri(l, mp);
+          int dst = m2l_plane_off(nc, m) + tri(l, mp) - tri(m);
           o[base + 2 * dst] = (T)eo[src];
           o[base + 2 * dst + 1] = (T)eo[sq_size(Lb) + src];
         }
@@ -245,6 +285,14 @@ void build_tables_t(AranGpuSolver3d *s, OpTables<T> &tb, cudaStream_t st) {
       k_m2l_vertical<T><<<ceil_div(ne, 256), 256, 0, st>>>(p, ndir, L.stride, L.rp, L.vv,
                                                             tb.vt.ptr, dst.ptr);
       ACHECK(cudaGetLastError());
+      if (sizeof(T) == 4 && m2l_lane_order(p)) {
+        const int64_t nl = (int64_t)ndir * m2l_lane_stride(p);
+        tb.dir_lanes.reserve(nl);
+        k_m2l_lane_tables<<<ceil_div(nl, 256), 256, 0, st>>>(
+            p, ndir, reinterpret_cast<const float *>(dst.ptr), L,
+            reinterpret_cast<float *>(tb.dir_lanes.ptr));
+        ACHECK(cudaGetLastError());
+      }
     }
     ACHECK(cudaStreamSynchronize(st));
   }

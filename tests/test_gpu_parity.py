@@ -78,6 +78,36 @@ def test_mixed_matches_oracle(aran, oracle, case):
     assert rel_l2(fld, ofld) < MIXED_TOL
 
 
+M2L_KERNEL_CASES = [
+    ("plummer-p12", lambda n: W.plummer(n, 31), 40000, 32, 12, (-1, -1, -1), (1, 1, 1)),
+    ("uniform-p8", lambda n: W.uniform(n, 32), 30000, 16, 8, (0, 0, 0), (1, 1, 1)),
+    ("blobs-p12", lambda n: W.blobs(n, 33, nblobs=2), 9000, 8, 12, (0, 0, 0), (1, 1, 1)),
+]
+
+
+@pytest.mark.parametrize("case", M2L_KERNEL_CASES, ids=[c[0] for c in M2L_KERNEL_CASES])
+def test_mixed_m2l_kernels_agree(aran, oracle, case, monkeypatch):
+    """The FP32 lane-parallel M2L kernel (orders 8 and 12) and the sibling
+    kernel (every order; ARAN_M2L_KERNEL=sibling) apply the same tables in
+    FP32: both within the mixed tolerance of the oracle, and within 1e-6 of
+    each other."""
+    name, gen, n, maxbox, p, lb, ub = case
+    x, q = gen(n)
+    out = {}
+    for kernel in ("lanes", "sibling"):
+        monkeypatch.setenv("ARAN_M2L_KERNEL", kernel)
+        with aran.Solver3d(lb, ub, maxbox=maxbox, order=p, field=True, precision="mixed") as s:
+            out[kernel] = s.solve(x, q)
+    monkeypatch.delenv("ARAN_M2L_KERNEL")
+    opot, _ = oracle.solve(x, q, order=p, maxbox=maxbox, field=False, lb=lb, ub=ub)
+    ofld, _ = oracle.solve(x, q, order=p, maxbox=maxbox, field=True, lb=lb, ub=ub)
+    for kernel, (pot, fld) in out.items():
+        assert rel_l2(pot, opot) < MIXED_TOL, kernel
+        assert rel_l2(fld, ofld) < MIXED_TOL, kernel
+    assert rel_l2(out["lanes"][0], out["sibling"][0]) < 1e-6
+    assert rel_l2(out["lanes"][1], out["sibling"][1]) < 1e-6
+
+
 @pytest.mark.parametrize("p", [1, 2, 4, 6, 16, 20])
 def test_orders_fp64(aran, oracle, p):
     x, q = W.uniform(4000, 20 + p)
@@ -91,7 +121,8 @@ def test_orders_fp64(aran, oracle, p):
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 2e-6), ("mixed", 3e-6)])
 def test_p12_against_direct_sum(aran, oracle, precision, tol):
-    """BASELINE accuracy target: p=12 within ~1e-6 of the FP64 direct sum."""
+    """Accuracy target of the benchmark workloads: p=12 within ~1e-6 of the
+    FP64 direct sum."""
     x, q = W.uniform(30000, 2)
     with aran.Solver3d(maxbox=64, order=12, field=True, precision=precision) as s:
         pot, fld = s.solve(x, q)
@@ -220,8 +251,8 @@ def uniform_1m(oracle):
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 2e-6), ("mixed", 3e-6)])
 def test_1m_uniform_subset_vs_direct(aran, uniform_1m, precision, tol):
-    """configs[1] size: N=1M uniform, p=12, leaf 64; 10,000 targets against
-    the FP64 direct sum."""
+    """The uniform1m workload (N=1M uniform, p=12, leaf 64); 10,000 targets
+    against the FP64 direct sum."""
     x, q, tgt, rp, rf = uniform_1m
     with aran.Solver3d(maxbox=64, order=12, field=True, precision=precision) as s:
         pot, fld = s.solve(x, q)
