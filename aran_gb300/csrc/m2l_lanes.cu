@@ -14,6 +14,15 @@
 //    every table read is a broadcast of 16 bytes (four factors) from shared
 //    memory, and a lane's whole series stays in registers, the order being a
 //    compile-time constant;
+//  * child w = (bx, by, bz) reaches its sources through the offsets with
+//    d_x in [bx-3, bx+2] (same for y, z); the mirror image sigma_w (x -> -x
+//    where bx = 1, likewise y, z) maps them onto child 0's 189 offsets, and
+//    the translation obeys T_d = S T_{sigma d} S, with S the action of the
+//    mirror on series: (l, m) -> (-1)^{l+m} on a z flip, conjugation on a y
+//    flip, (-1)^m conjugation on an x flip.  So all eight warps walk child
+//    0's offsets together, each applying S to its sources on the way in and
+//    once to its accumulated locals on the way out: every table in the ring
+//    serves all eight warps;
 //  * the two lanes of a pair exchange their rotated-back parts with one
 //    shuffle to apply the conjugate z-phase, and each lane accumulates its
 //    part of the target's local in shared memory (one word per lane, no
@@ -92,7 +101,7 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
   off += 16 * sizeof(unsigned);
   uint16_t *active = reinterpret_cast<uint16_t *>(smem_raw + off);
   off += 320 * sizeof(uint16_t);
-  uint16_t *dcode = reinterpret_cast<uint16_t *>(smem_raw + off);
+  uint16_t *dcode = reinterpret_cast<uint16_t *>(smem_raw + off);   // 189 of them
   off += 320 * sizeof(uint16_t);
   int8_t *dvec = reinterpret_cast<int8_t *>(smem_raw + off);
   __shared__ int s_nact;
@@ -100,16 +109,17 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
   for (int i = threadIdx.x; i < kLanePar * 216; i += blockDim.x) grid[i] = -1;
   for (int i = threadIdx.x; i < kLaneWarps * NL * 32; i += blockDim.x) accs[i] = 0.f;
   if (threadIdx.x < 16) mask[threadIdx.x] = 0u;
-  // offsets (dx, dy, dz) in [-3,3]^3 minus [-1,1]^3, dz slowest: offset
-  // index = code - (near codes below it); code = (dx+3) + 7 (dy+3) + 49 (dz+3)
-  for (int code = threadIdx.x; code < 343; code += blockDim.x) {
-    const int a = code % 7, b = (code / 7) % 7, c = code / 49;
+  // child 0's offsets (dx, dy, dz) in [-3,2]^3 minus [-1,1]^3, dz slowest:
+  // index = L - (near cells below L), L = (dx+3) + 6 (dy+3) + 36 (dz+3); table
+  // code (dx+3) + 7 (dy+3) + 49 (dz+3)
+  for (int L = threadIdx.x; L < 216; L += blockDim.x) {
+    const int a = L % 6, b = (L / 6) % 6, c = L / 36;
     auto in = [](int v) { return v >= 2 && v <= 4; };
     auto below = [](int v) { return v < 2 ? 0 : (v > 4 ? 3 : v - 2); };
     if (in(a) && in(b) && in(c)) continue;
     const int nb = 9 * below(c) + (in(c) ? 3 * below(b) + (in(b) ? below(a) : 0) : 0);
-    const int di = code - nb;
-    dcode[di] = (uint16_t)code;
+    const int di = L - nb;
+    dcode[di] = (uint16_t)(a + 7 * b + 49 * c);
     dvec[3 * di] = (int8_t)(a - 3);
     dvec[3 * di + 1] = (int8_t)(b - 3);
     dvec[3 * di + 2] = (int8_t)(c - 3);
@@ -153,20 +163,24 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
       if (end[t] > begin[t]) tgt = t;
     }
   }
-  const int tx = 2 + (w & 1), ty = 2 + ((w >> 1) & 1), tz = 2 + ((w >> 2) & 1);
+  // child w = (bx, by, bz) at cell (2+bx, 2+by, 2+bz) of the grid; its
+  // offset for child 0's offset d is sigma_w d
+  const int bx = w & 1, by = (w >> 1) & 1, bz = (w >> 2) & 1;
+  const int tx = 2 + bx, ty = 2 + by, tz = 2 + bz;
   auto source_of = [&](int di) -> int {
     if (tgt < 0) return -1;
-    const int cx = tx - dvec[3 * di], cy = ty - dvec[3 * di + 1], cz = tz - dvec[3 * di + 2];
+    const int dx = dvec[3 * di], dy = dvec[3 * di + 1], dz = dvec[3 * di + 2];
+    const int cx = tx - (bx ? -dx : dx), cy = ty - (by ? -dy : dy), cz = tz - (bz ? -dz : dz);
     if (cx < 0 || cx > 5 || cy < 0 || cy > 5 || cz < 0 || cz > 5) return -1;
     return grid[pi_ * 216 + cx + 6 * (cy + 6 * cz)];
   };
   if (w < kLaneWarps)
-    for (int di = 0; di < 316; ++di) {
+    for (int di = 0; di < 189; ++di) {
       const unsigned any = __ballot_sync(kFull, source_of(di) >= 0);
       if (lane == 0 && any) atomicOr(&mask[di >> 5], 1u << (di & 31));
     }
   __syncthreads();
-  for (int di = threadIdx.x; di < 316; di += blockDim.x) {
+  for (int di = threadIdx.x; di < 189; di += blockDim.x) {
     const unsigned m = mask[di >> 5];
     if ((m >> (di & 31)) & 1u) {
       int pos = __popc(m & ((1u << (di & 31)) - 1u));
@@ -176,7 +190,7 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
   }
   if (threadIdx.x == 0) {
     int tot = 0;
-    for (int k = 0; k < 10; ++k) tot += __popc(mask[k]);
+    for (int k = 0; k < 6; ++k) tot += __popc(mask[k]);
     s_nact = tot;
   }
   __syncthreads();
@@ -237,16 +251,19 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
       const float2 *ph2 = reinterpret_cast<const float2 *>(tb);    // (cos, sin) of m phi
       cp_async_wait_all();
       __syncwarp();
-      // z-phase and rotation to the z axis (degrees < p): this lane's part
-      // of the source is x.re pa + x.im pb
+      // mirror S, z-phase and rotation to the z axis (degrees < p): this
+      // lane's part of the phased mirrored source (l, m) is
+      // sl (x.re pa[m] + x.im pb[m]), sl = -1 for odd l under a z flip
       float y[NM];
       {
         float pa[P], pb[P];
 #pragma unroll
         for (int m = 0; m < P; ++m) {
           const float2 e = ph2[m];
-          pa[m] = h ? e.y : e.x;
-          pb[m] = h ? e.x : -e.y;
+          const float g = ((bx ^ bz) & m & 1) ? -1.f : 1.f;       // (-1)^m of x and z flips
+          const float cj = (bx ^ by) ? -g : g;                     // conjugation
+          pa[m] = g * (h ? e.y : e.x);
+          pb[m] = cj * (h ? e.x : -e.y);
         }
         const float4 *X4 = reinterpret_cast<const float4 *>(my_stg);
         const float4 *F4 = reinterpret_cast<const float4 *>(tb + m2l_lane_f(P)) + h;
@@ -260,6 +277,7 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
             if ((c & 1) == 0) xq = X4[c >> 1];
             const float xr = (c & 1) ? xq.z : xq.x, xi = (c & 1) ? xq.w : xq.y;
             xp[m] = fmaf(xr, pa[m], xi * pb[m]);
+            if (bz && (l & 1)) xp[m] = -xp[m];
           }
 #pragma unroll
           for (int mp = 0; mp <= l; ++mp) {
@@ -296,17 +314,10 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
             z[m * (P + 1) - m * (m - 1) / 2 + (j - m)] = a;
           }
       }
-      // rotation back (degrees <= p), conjugate z-phase, accumulate:
-      // real part += a cos + b sin, imaginary part += a cos - b sin, with a
-      // this lane's part and b the partner's
+      // rotation back (degrees <= p); degree l of z dies as degree l of o
+      // is made, so the two share the registers
+      float o[NL];
       {
-        float cph[P + 1], sph[P + 1];
-#pragma unroll
-        for (int m = 0; m <= P; ++m) {
-          const float2 e = ph2[m];
-          cph[m] = e.x;
-          sph[m] = h ? -e.y : e.y;
-        }
         const float4 *B4 = reinterpret_cast<const float4 *>(tb + m2l_lane_b(P)) + h;
         float4 bq = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
@@ -320,20 +331,42 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
               if ((t & 3) == 0) bq = B4[2 * (t >> 2)];
               a = fmaf(sel4(bq, t & 3), z[m * (P + 1) - m * (m - 1) / 2 + (l - m)], a);
             }
-            const float o = __shfl_xor_sync(kFull, a, 1);
-            float *slot = my_acc + 32 * (l * (l + 1) / 2 + mp);
-            *slot += fmaf(a, cph[mp], o * sph[mp]);
+            o[l * (l + 1) / 2 + mp] = a;
           }
       }
+      // conjugate z-phase and accumulate, after the last table read: real
+      // part += a cos + b sin, imaginary part += a cos - b sin, with a this
+      // lane's part and b the partner's
+      float cph[P + 1], sph[P + 1];
+#pragma unroll
+      for (int m = 0; m <= P; ++m) {
+        const float2 e = ph2[m];
+        cph[m] = e.x;
+        sph[m] = h ? -e.y : e.y;
+      }
+#pragma unroll
+      for (int l = 0; l <= P; ++l)
+#pragma unroll
+        for (int mp = 0; mp <= l; ++mp) {
+          const float a = o[l * (l + 1) / 2 + mp];
+          const float bp = __shfl_xor_sync(kFull, a, 1);
+          float *slot = my_acc + 32 * (l * (l + 1) / 2 + mp);
+          *slot += fmaf(a, cph[mp], bp * sph[mp]);
+        }
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[b]);
   }
   cp_async_wait_all();
   if (nact > 0 && tgt >= 0) {
+    // back from the mirror frame: S on the accumulated local
     const float ih = (float)((double)(1ull << depth[tgt]) / scale_e);   // 2^depth / scale
     float *lo = reinterpret_cast<float *>(loc) + (size_t)tgt * NL * 2 + h;
-    for (int c = 0; c < NL; ++c) lo[2 * c] = my_acc[32 * c] * ih;
+    for (int l = 0, c = 0; l <= P; ++l)
+      for (int m = 0; m <= l; ++m, ++c) {
+        const bool neg = ((bz & (l + m)) ^ (bx & m) ^ (h & (bx ^ by))) & 1;
+        lo[2 * c] = my_acc[32 * c] * (neg ? -ih : ih);
+      }
   }
 }
 
