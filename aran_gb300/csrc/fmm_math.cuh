@@ -67,16 +67,17 @@ FMM_HD int m2l_vrow_off(int p, int n) {
 
 // Stream layout of the lane-parallel M2L tables (FP32, order p), one block
 // per offset, in the order the kernel consumes it: the z-phases (cos, sin)
-// of m = 0..p; the forward rotation terms (l < p, m' <= l, m <= l) in groups
-// of four, each group four even-part factors then four odd-part factors;
-// the vertical factors times the offset's radial powers, terms
-// (m <= p, j = m..p, n = m..p-1); the backward rotation terms (l <= p),
-// grouped like the forward ones.
-__host__ __device__ constexpr int m2l_lane_nf(int p) { return p * (p + 1) * (2 * p + 1) / 6; }
+// of m = 0..p; the forward rotation terms (l < p, m' <= l, m <= m': the
+// lower triangle of each even/odd Wigner block, the upper one following from
+// E[m][m'] = (-1)^{m-m'} E[m'][m] for m, m' > 0 and E[0][m] = 2 (-1)^m E[m][0],
+// O[0][m] = 0), in groups of four, each group four even-part factors then
+// four odd-part factors; the vertical factors times the offset's radial
+// powers, terms (m <= p, j = m..p, n = m..p-1); the backward rotation terms
+// (l <= p), grouped like the forward ones.
+__host__ __device__ constexpr int m2l_lane_tet(int l) { return l * (l + 1) * (l + 2) / 6; }
+__host__ __device__ constexpr int m2l_lane_nf(int p) { return m2l_lane_tet(p); }
+__host__ __device__ constexpr int m2l_lane_nb(int p) { return m2l_lane_tet(p + 1); }
 __host__ __device__ constexpr int m2l_lane_nv(int p) { return p * (p + 1) * (p + 2) / 3; }
-__host__ __device__ constexpr int m2l_lane_nb(int p) {
-  return (p + 1) * (p + 2) * (2 * p + 3) / 6;
-}
 __host__ __device__ constexpr int m2l_lane_f(int p) { return (2 * (p + 1) + 3) & ~3; }
 __host__ __device__ constexpr int m2l_lane_v(int p) {
   return m2l_lane_f(p) + 8 * ((m2l_lane_nf(p) + 3) / 4);

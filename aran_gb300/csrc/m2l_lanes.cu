@@ -42,7 +42,7 @@ namespace {
 
 constexpr int kLanePar = 16;     // parents per CTA: lane pair i <-> parent i
 constexpr int kLaneWarps = 8;    // consumer warps: warp w <-> child w
-constexpr int kLaneNst = 2;      // table ring slots
+constexpr int kLaneNst = 3;      // table ring slots
 constexpr unsigned kFull = 0xffffffffu;
 
 template <int P>
@@ -70,7 +70,7 @@ __device__ __forceinline__ float sel4(const float4 &v, int k) {
 }
 
 template <int P>
-__global__ void __launch_bounds__(32 * (kLaneWarps + 1))
+__global__ void __launch_bounds__(32 * kLaneWarps, 1)
     k_m2l_lanes(int nparents, const int *__restrict__ parents, const int *__restrict__ child,
                 const int *__restrict__ begin, const int *__restrict__ end,
                 const int *__restrict__ col, const int *__restrict__ ncol,
@@ -196,21 +196,18 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
   __syncthreads();
   const int nact = s_nact;
 
-  if (w == kLaneWarps) {
-    // producer warp: stream the offset tables through the ring
-    if (lane == 0)
-      for (int i = 0; i < nact; ++i) {
-        const int b = i % kLaneNst;
-        if (i >= kLaneNst && !mbar_wait(&empty[b], ((i / kLaneNst) - 1) & 1)) {
-          atomicExch(err, 1);
-          break;
-        }
-        mbar_expect_tx(&full[b], STRIDE * (uint32_t)sizeof(float));
-        bulk_g2s(tab + (size_t)b * STRIDE, dirs + (size_t)dcode[active[i]] * STRIDE,
-                 STRIDE * (uint32_t)sizeof(float), &full[b]);
-      }
-    return;
-  }
+  // the ring: thread 0 fills the first slots; afterwards warp 0 refills
+  // slot b with offset it + NST once all warps have released it (no
+  // separate producer warp, so two warps share each scheduler's registers)
+  constexpr uint32_t kTabBytes = STRIDE * (uint32_t)sizeof(float);
+  auto issue = [&](int i) {
+    const int b = i % kLaneNst;
+    mbar_expect_tx(&full[b], kTabBytes);
+    bulk_g2s(tab + (size_t)b * STRIDE, dirs + (size_t)dcode[active[i]] * STRIDE, kTabBytes,
+             &full[b]);
+  };
+  if (threadIdx.x == 0)
+    for (int i = 0; i < kLaneNst && i < nact; ++i) issue(i);
 
   cplx<float> *my_stg = stg + (size_t)(w * kLanePar + pi_) * NMP;
   float *my_acc = accs + (size_t)w * NL * 32 + lane;   // coefficient c at my_acc[32 c]
@@ -253,7 +250,7 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
       __syncwarp();
       // mirror S, z-phase and rotation to the z axis (degrees < p): this
       // lane's part of the phased mirrored source (l, m) is
-      // sl (x.re pa[m] + x.im pb[m]), sl = -1 for odd l under a z flip
+      // sn (x.re pa[m] + x.im pb[m]), sn = -1 for odd l under a z flip
       float y[NM];
       {
         float pa[P], pb[P];
@@ -267,29 +264,36 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
         }
         const float4 *X4 = reinterpret_cast<const float4 *>(my_stg);
         const float4 *F4 = reinterpret_cast<const float4 *>(tb + m2l_lane_f(P)) + h;
+        const float f0 = h ? 0.f : 2.f;
         float4 xq = make_float4(0.f, 0.f, 0.f, 0.f), fq = xq;
 #pragma unroll
         for (int l = 0; l < P; ++l) {
-          float xp[P];
+          const float sn = (bz && (l & 1)) ? -1.f : 1.f;
+          float xp[P], yd[P], yt[P];
 #pragma unroll
           for (int m = 0; m <= l; ++m) {
             const int c = l * (l + 1) / 2 + m;
             if ((c & 1) == 0) xq = X4[c >> 1];
             const float xr = (c & 1) ? xq.z : xq.x, xi = (c & 1) ? xq.w : xq.y;
-            xp[m] = fmaf(xr, pa[m], xi * pb[m]);
-            if (bz && (l & 1)) xp[m] = -xp[m];
+            xp[m] = sn * fmaf(xr, pa[m], xi * pb[m]);
+            yd[m] = 0.f;
+            yt[m] = 0.f;
           }
+          // lower triangle (m <= m') direct, upper triangle by symmetry
 #pragma unroll
-          for (int mp = 0; mp <= l; ++mp) {
-            float a = 0.f;
+          for (int mp = 0; mp <= l; ++mp)
 #pragma unroll
-            for (int m = 0; m <= l; ++m) {
-              const int t = sq_off(l) + mp * (l + 1) + m;
+            for (int m = 0; m <= mp; ++m) {
+              const int t = m2l_lane_tet(l) + mp * (mp + 1) / 2 + m;
               if ((t & 3) == 0) fq = F4[2 * (t >> 2)];
-              a = fmaf(sel4(fq, t & 3), xp[m], a);
+              const float v = sel4(fq, t & 3);
+              yd[mp] = fmaf(v, xp[m], yd[mp]);
+              if (m < mp) yt[m] = fmaf(v, (mp & 1) ? -xp[mp] : xp[mp], yt[m]);
             }
-            y[l * (l + 1) / 2 + mp] = a;
-          }
+          y[l * (l + 1) / 2] = fmaf(f0, yt[0], yd[0]);
+#pragma unroll
+          for (int m = 1; m <= l; ++m)
+            y[l * (l + 1) / 2 + m] = (m & 1) ? yd[m] - yt[m] : yd[m] + yt[m];
         }
       }
       find_next(it + 1);
@@ -319,20 +323,32 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
       float o[NL];
       {
         const float4 *B4 = reinterpret_cast<const float4 *>(tb + m2l_lane_b(P)) + h;
+        const float f0 = h ? 0.f : 2.f;
         float4 bq = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int l = 0; l <= P; ++l)
+        for (int l = 0; l <= P; ++l) {
+          float zi[P + 1], od[P + 1], ot[P + 1];
 #pragma unroll
-          for (int mp = 0; mp <= l; ++mp) {
-            float a = 0.f;
-#pragma unroll
-            for (int m = 0; m <= l; ++m) {
-              const int t = sq_off(l) + mp * (l + 1) + m;
-              if ((t & 3) == 0) bq = B4[2 * (t >> 2)];
-              a = fmaf(sel4(bq, t & 3), z[m * (P + 1) - m * (m - 1) / 2 + (l - m)], a);
-            }
-            o[l * (l + 1) / 2 + mp] = a;
+          for (int m = 0; m <= l; ++m) {
+            zi[m] = z[m * (P + 1) - m * (m - 1) / 2 + (l - m)];
+            od[m] = 0.f;
+            ot[m] = 0.f;
           }
+#pragma unroll
+          for (int mp = 0; mp <= l; ++mp)
+#pragma unroll
+            for (int m = 0; m <= mp; ++m) {
+              const int t = m2l_lane_tet(l) + mp * (mp + 1) / 2 + m;
+              if ((t & 3) == 0) bq = B4[2 * (t >> 2)];
+              const float v = sel4(bq, t & 3);
+              od[mp] = fmaf(v, zi[m], od[mp]);
+              if (m < mp) ot[m] = fmaf(v, (mp & 1) ? -zi[mp] : zi[mp], ot[m]);
+            }
+          o[l * (l + 1) / 2] = fmaf(f0, ot[0], od[0]);
+#pragma unroll
+          for (int m = 1; m <= l; ++m)
+            o[l * (l + 1) / 2 + m] = (m & 1) ? od[m] - ot[m] : od[m] + ot[m];
+        }
       }
       // conjugate z-phase and accumulate, after the last table read: real
       // part += a cos + b sin, imaginary part += a cos - b sin, with a this
@@ -355,7 +371,17 @@ __global__ void __launch_bounds__(32 * (kLaneWarps + 1))
         }
     }
     __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[b]);
+    if (lane == 0) {
+      mbar_arrive(&empty[b]);
+      if (w == 0 && it + kLaneNst < nact) {
+        if (!mbar_wait(&empty[b], (it / kLaneNst) & 1)) {
+          atomicExch(err, 1);
+        } else {
+          issue(it + kLaneNst);
+        }
+      }
+    }
+    __syncwarp();
   }
   cp_async_wait_all();
   if (nact > 0 && tgt >= 0) {
@@ -380,7 +406,7 @@ bool launch_p(AranGpuSolver3d *s, OpTables<float> &tb, const cplx<float> *mult,
   if ((int)sm > dev_smem) return false;
   ACHECK(cudaFuncSetAttribute(k_m2l_lanes<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)sm));
-  k_m2l_lanes<P><<<ceil_div(t.n_parents, kLanePar), 32 * (kLaneWarps + 1), sm, st>>>(
+  k_m2l_lanes<P><<<ceil_div(t.n_parents, kLanePar), 32 * kLaneWarps, sm, st>>>(
       t.n_parents, t.parents.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
       t.ijk.ptr, t.depth.ptr, tb.dir_lanes.ptr, s->scale_e, mult, loc, s->err_dev.ptr);
   ACHECK(cudaGetLastError());

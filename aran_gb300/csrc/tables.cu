@@ -134,13 +134,17 @@ __global__ void k_m2l_lane_tables(int p, int ndir, const float *__restrict__ src
   const int d = (int)(i / stride), e = (int)(i % stride);
   const float *s = src + (size_t)d * D.stride;
   const int F = m2l_lane_f(p), V = m2l_lane_v(p), B = m2l_lane_b(p);
-  // q-th float of a grouped rotation stream: term 4 (q / 8) + q % 4, part (q / 4) % 2
+  // q-th float of a grouped rotation stream: term 4 (q / 8) + q % 4, part
+  // (q / 4) % 2; term t = tet(l) + m'(m'+1)/2 + m is row m', column m of
+  // degree l
   auto rot = [&](int q, int nterm, int nc, int base) -> float {
     const int t = 4 * (q >> 3) + (q & 3), part = (q >> 2) & 1;
     if (t >= nterm) return 0.f;
     int l = 0;
-    while (sq_off(l + 1) <= t) ++l;
-    const int r = t - sq_off(l), mp = r / (l + 1), m = r % (l + 1);
+    while (m2l_lane_tet(l + 1) <= t) ++l;
+    int r = t - m2l_lane_tet(l), mp = 0;
+    while (tri(mp + 1) <= r) ++mp;
+    const int m = r - tri(mp);
     return s[base + 2 * (m2l_plane_off(nc, m) + tri(l, mp) - tri(m)) + part];
   };
   float v = 0.f;
