@@ -28,9 +28,9 @@
 //    part of the target's local in shared memory (one word per lane, no
 //    conflicts), in the same offset order for every run.
 //
-// The offset tables stream through a two-slot ring of TMA bulk copies, as
-// in m2l.cu; the next offset's source multipoles are copied into shared
-// memory by cp.async while the current one is translated.  Every mbarrier
+// The offset tables stream through a three-slot ring of TMA bulk copies;
+// the next offset's source multipoles are brought into shared memory by one
+// bulk copy each while the current one is translated.  Every mbarrier
 // wait is bounded; a wait that gives up sets the error word and the CTA
 // stops.
 #include "internal.cuh"
@@ -57,7 +57,7 @@ template <int P>
 constexpr size_t lanes_smem() {
   using D = LaneDims<P>;
   size_t off = (size_t)kLaneNst * D::STRIDE * sizeof(float);
-  off += 2 * kLaneNst * sizeof(uint64_t);
+  off += 2 * kLaneNst * sizeof(uint64_t) + kLaneWarps * sizeof(uint64_t);
   off += (size_t)kLaneWarps * kLanePar * D::NMP * sizeof(cplx<float>);
   off += (size_t)kLaneWarps * D::NL * 32 * sizeof(float);
   off += (size_t)kLanePar * 216 * sizeof(int);
@@ -90,7 +90,8 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
   off += (size_t)kLaneNst * STRIDE * sizeof(float);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + off);
   uint64_t *empty = full + kLaneNst;
-  off += 2 * kLaneNst * sizeof(uint64_t);
+  uint64_t *sbar = empty + kLaneNst;    // per warp: its staged sources have landed
+  off += 2 * kLaneNst * sizeof(uint64_t) + kLaneWarps * sizeof(uint64_t);
   cplx<float> *stg = reinterpret_cast<cplx<float> *>(smem_raw + off);
   off += (size_t)kLaneWarps * kLanePar * NMP * sizeof(cplx<float>);
   float *accs = reinterpret_cast<float *>(smem_raw + off);
@@ -129,6 +130,7 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
       mbar_init(&full[b], 1);
       mbar_init(&empty[b], kLaneWarps);
     }
+    for (int k = 0; k < kLaneWarps; ++k) mbar_init(&sbar[k], 1);
     fence_mbar_init();
   }
   __syncthreads();
@@ -206,8 +208,9 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
     bulk_g2s(tab + (size_t)b * STRIDE, dirs + (size_t)dcode[active[i]] * STRIDE, kTabBytes,
              &full[b]);
   };
+  int issued = 0;   // table copies issued (thread 0)
   if (threadIdx.x == 0)
-    for (int i = 0; i < kLaneNst && i < nact; ++i) issue(i);
+    for (; issued < kLaneNst && issued < nact; ++issued) issue(issued);
 
   cplx<float> *my_stg = stg + (size_t)(w * kLanePar + pi_) * NMP;
   float *my_acc = accs + (size_t)w * NL * 32 + lane;   // coefficient c at my_acc[32 c]
@@ -218,25 +221,29 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
       if (__any_sync(kFull, next_s >= 0)) break;
     }
   };
-  // the two lanes of a pair copy alternate 16-byte rows of the source
+  // one bulk copy per source (issued by the pair's first lane) completing
+  // on the warp's barrier; pairs without a source zero their slot
+  static_assert(NM % 2 == 0, "bulk copies of whole 16-byte rows");
+  constexpr uint32_t kSrcBytes = NM * (uint32_t)sizeof(cplx<float>);
+  bool pending = false;
+  uint32_t sph = 0;
   auto prefetch = [&]() {
     if (next_i >= nact) return;
+    const unsigned cp = __ballot_sync(kFull, h == 0 && next_s >= 0);
+    if (lane == 0) mbar_expect_tx(&sbar[w], (uint32_t)__popc(cp) * kSrcBytes);
+    __syncwarp();
     if (next_s >= 0) {
-      const cplx<float> *src = mult + (size_t)next_s * NM;
-      if (NM % 2 == 0) {
-        for (int q = h; q < NM / 2; q += 2) cp_async16(my_stg + 2 * q, src + 2 * q);
-      } else {
-        for (int c = h; c < NM; c += 2) cp_async8(my_stg + c, src + c);
-      }
+      if (h == 0) bulk_g2s(my_stg, mult + (size_t)next_s * NM, kSrcBytes, &sbar[w]);
     } else {
       for (int c = h; c < NM; c += 2) my_stg[c] = cmake<float>(0.f, 0.f);
     }
-    cp_async_commit();
+    pending = true;
   };
   find_next(0);
   prefetch();
 
-  for (int it = 0; it < nact; ++it) {
+  int it = 0;
+  for (; it < nact; ++it) {
     const int b = it % kLaneNst;
     const bool ok = __all_sync(kFull, mbar_wait(&full[b], (it / kLaneNst) & 1));
     if (!ok) {
@@ -246,7 +253,12 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
     if (it == next_i) {
       const float *tb = tab + (size_t)b * STRIDE;
       const float2 *ph2 = reinterpret_cast<const float2 *>(tb);    // (cos, sin) of m phi
-      cp_async_wait_all();
+      if (!__all_sync(kFull, mbar_wait(&sbar[w], sph))) {
+        if (lane == 0) atomicExch(err, 1);
+        break;
+      }
+      sph ^= 1u;
+      pending = false;
       __syncwarp();
       // mirror S, z-phase and rotation to the z axis (degrees < p): this
       // lane's part of the phased mirrored source (l, m) is
@@ -378,12 +390,16 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
           atomicExch(err, 1);
         } else {
           issue(it + kLaneNst);
+          ++issued;
         }
       }
     }
     __syncwarp();
   }
-  cp_async_wait_all();
+  // copies still in flight after an early exit land before the CTA leaves
+  if (pending) mbar_wait(&sbar[w], sph);
+  if (threadIdx.x == 0)
+    for (int i = it; i < issued; ++i) mbar_wait(&full[i % kLaneNst], (i / kLaneNst) & 1);
   if (nact > 0 && tgt >= 0) {
     // back from the mirror frame: S on the accumulated local
     const float ih = (float)((double)(1ull << depth[tgt]) / scale_e);   // 2^depth / scale
