@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(128, 10) k_p2p(
   for (int tb = 0; tb < nt; tb += gsz) {
     const int ti = tb + threadIdx.x / tpt;
     const bool active = ti < nt;
+    if (!__any_sync(kFull, active)) continue;   // a warp with no target of this pass
     const int t = b + (active ? ti : 0);
     double pot = 0, fx = 0, fy = 0, fz = 0;
     // mixed: per-source-leaf FP32 sums are added with Kahan compensation in

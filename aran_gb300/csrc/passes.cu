@@ -268,8 +268,8 @@ __global__ void k_l2l_rotate(int cnt, int off, const int *__restrict__ parent,
 // ---------------------------------------------------------------------------
 // L2P with gradient: aran_development3d_local_gradient_evaluate
 // (arandevelopment3d.c:542-552, aransphericalseriesd.c:419-546) and the
-// local evaluation of arandevelopment3d.c:485-494.  One block per leaf, one
-// thread per particle.  The gradient uses the derivative identities of the
+// local evaluation of arandevelopment3d.c:485-494.  One warp per leaf (four
+// leaves per block), one lane per particle.  The gradient uses the derivative identities of the
 // regular solid harmonics (fmm_math.cuh gen_grad_coefs): d/dz and
 // d/dx - i d/dy of a degree-p local are degree-(p-1) locals built once per
 // leaf, so a particle only evaluates S_l^m(xhat) once.
@@ -283,17 +283,22 @@ __global__ void k_l2p(int nleaves, const int *__restrict__ leaf_node, const int 
                       double *__restrict__ acc_fld) {
   extern __shared__ unsigned char smem_raw[];
   const int nl = tri(p + 1), nm = tri(p);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   T *rec = reinterpret_cast<T *>(smem_raw);
-  cplx<T> *Lc = reinterpret_cast<cplx<T> *>(rec + ((2 * nl + 1) & ~1));
+  // per warp: the leaf's local, and the d/dz and d/dx - i d/dy locals
+  cplx<T> *Lc = reinterpret_cast<cplx<T> *>(rec + ((2 * nl + 1) & ~1)) +
+                (size_t)w * (nl + nm + p * p);
   cplx<T> *A = Lc + nl;
   cplx<T> *B = A + nm;
-  const int L = blockIdx.x;
-  const int node = leaf_node[L];
   for (int i = threadIdx.x; i < 2 * nl; i += blockDim.x) rec[i] = rec_g[i];
-  for (int c = threadIdx.x; c < nl; c += blockDim.x) Lc[c] = loc[(size_t)node * nl + c];
   __syncthreads();
+  const int L = blockIdx.x * (blockDim.x >> 5) + w;
+  if (L >= nleaves) return;
+  const int node = leaf_node[L];
+  for (int c = lane; c < nl; c += 32) Lc[c] = loc[(size_t)node * nl + c];
+  __syncwarp();
   if (FIELD) {
-    for (int c = threadIdx.x; c < nm; c += blockDim.x) {
+    for (int c = lane; c < nm; c += 32) {
       // c = tri(l', m): A = L(l'+1, m) * gz
       int lp = 0;
       while (tri(lp + 1) <= c) ++lp;
@@ -302,7 +307,7 @@ __global__ void k_l2p(int nleaves, const int *__restrict__ leaf_node, const int 
       T g = gz_g[c];
       A[c] = cmake<T>(v.re * g, v.im * g);
     }
-    for (int c = threadIdx.x; c < p * p; c += blockDim.x) {
+    for (int c = lane; c < p * p; c += 32) {
       int lp = 0;
       while ((lp + 1) * (lp + 1) <= c) ++lp;
       int mp = c - lp * lp - lp;
@@ -317,10 +322,10 @@ __global__ void k_l2p(int nleaves, const int *__restrict__ leaf_node, const int 
       B[c] = cmake<T>(v.re * g, v.im * g);
     }
   }
-  __syncthreads();
+  __syncwarp();
   const int b = begin[node], e = end[node];
   const T ih = inv_scale<T>(depth[node], scale_e);
-  for (int i = b + threadIdx.x; i < e; i += blockDim.x) {
+  for (int i = b + lane; i < e; i += 32) {
     real4<T> r = rel[i];
     T x = r.x * ih, y = r.y * ih, z = r.z * ih;
     T r2 = x * x + y * y + z * z;
@@ -512,16 +517,19 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   ACHECK(cudaStreamWaitEvent(st, s->ev[2 * Stage::P2P + 1], 0));
   ACHECK(cudaEventRecord(s->ev[2 * Stage::L2P], st));
   {
-    size_t sm = ((2 * nl + 1) & ~1) * sizeof(T) + (size_t)(nl + nm + p * p) * sizeof(cplx<T>) + 64;
+    constexpr int LPB = 4;   // leaves (warps) per block
+    size_t sm = ((2 * nl + 1) & ~1) * sizeof(T) +
+                (size_t)LPB * (nl + nm + p * p) * sizeof(cplx<T>) + 64;
     smem_opt_in(k_l2p<T, true>, sm);
     smem_opt_in(k_l2p<T, false>, sm);
+    const int nb = ceil_div(t.nleaves, LPB);
     if (field)
-      k_l2p<T, true><<<t.nleaves, 64, sm, st>>>(t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
+      k_l2p<T, true><<<nb, 32 * LPB, sm, st>>>(t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
                                                  t.depth.ptr, rel, p, tb.rec.ptr, tb.gz.ptr,
                                                  tb.gm.ptr, s->scale_e, loc, s->acc_pot.ptr,
                                                  s->acc_fld.ptr);
     else
-      k_l2p<T, false><<<t.nleaves, 64, sm, st>>>(t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
+      k_l2p<T, false><<<nb, 32 * LPB, sm, st>>>(t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
                                                   t.depth.ptr, rel, p, tb.rec.ptr, tb.gz.ptr,
                                                   tb.gm.ptr, s->scale_e, loc, s->acc_pot.ptr,
                                                   s->acc_fld.ptr);
