@@ -254,6 +254,116 @@ __global__ void __launch_bounds__(128, 10) k_p2p(
   }
 }
 
+// Mixed near field, one warp per target leaf (four per block).  The warp
+// walks the leaf's near source leaves; for each it stages up to 32 source
+// points in shared memory, shifted to the target leaf's frame by the lane
+// that loads them, and every lane sums them against its own targets from
+// broadcast reads: lanes per target S = 4 (n <= 8), 2 (n <= 16), else 1
+// (32 targets per pass), so the per-leaf set-up (centres, Kahan adds of the
+// leaf partials) is paid once per lane per source leaf.
+// Ranges of more than kBigRange points are left to the chunked pass.
+template <bool FIELD>
+__global__ void __launch_bounds__(128, 7) k_p2p_warp(
+    int nleaves, const int *__restrict__ near_off, const int *__restrict__ near_rng,
+    const int2 *__restrict__ be, const float4 *__restrict__ chi, const float4 *__restrict__ clo,
+    const double *__restrict__ sx, const double *__restrict__ sy, const double *__restrict__ sz,
+    const real4<float> *__restrict__ rel32, double *__restrict__ acc_pot,
+    double *__restrict__ acc_fld) {
+  __shared__ float4 sbuf[4][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int L = blockIdx.x * 4 + w;
+  if (L >= nleaves) return;
+  const int2 tbe = be[L];
+  const int b = tbe.x, nt = tbe.y - tbe.x;
+  const int S = nt <= 8 ? 4 : (nt <= 16 ? 2 : 1);
+  const int sub = lane & (S - 1);
+  const float4 tch = chi[L], tcl = clo[L];
+  const float thr2 = tch.w;
+  const int r0 = near_off[L], r1 = near_off[L + 1];
+  float4 *buf = sbuf[w];
+  const int step = 32 / S;
+  for (int tb = 0; tb < nt; tb += step) {
+    const int ti0 = tb + lane / S;
+    const bool act0 = ti0 < nt;
+    const int t0 = b + (act0 ? ti0 : 0);
+    const real4<float> q0 = rel32[t0];
+    float ks[4] = {}, kc[4] = {};
+    auto kahan = [](float &sum, float &comp, float v) {
+      const float y = v - comp;
+      const float t2 = sum + y;
+      comp = (t2 - sum) - y;
+      sum = t2;
+    };
+    // one target against the staged source k (point j): partial sums p[4]
+    auto pair = [&](const real4<float> &q, int t, const float4 &sv, int j, float *p) {
+      float dx = q.x - sv.x, dy = q.y - sv.y, dz = q.z - sv.z;
+      float r2 = dx * dx + dy * dy + dz * dz;
+      if (__builtin_expect(r2 < thr2, 0)) {
+        if (j == t) {
+          r2 = 0.f;
+        } else {
+          // close pair: difference from the FP64 positions
+          dx = (float)(sx[t] - sx[j]);
+          dy = (float)(sy[t] - sy[j]);
+          dz = (float)(sz[t] - sz[j]);
+          r2 = dx * dx + dy * dy + dz * dz;
+        }
+      }
+      const bool ok = FIELD ? (r2 > 1e-10f) : (r2 > 0.f);
+      const float inv = ok ? rsqrtf(r2) : 0.f;
+      const float qi = sv.w * inv;
+      p[0] += qi;
+      if (FIELD) {
+        const float q3 = qi * inv * inv;
+        p[1] -= q3 * dx;
+        p[2] -= q3 * dy;
+        p[3] -= q3 * dz;
+      }
+    };
+    for (int rr = r0; rr < r1; ++rr) {
+      const int la = near_rng[2 * rr], lb = near_rng[2 * rr + 1];
+      if (lb <= la) continue;
+      if (rng_count(be, la, lb) > kBigRange) continue;  // chunked by the BIG pass
+      for (int lf = la; lf < lb; ++lf) {
+        const int2 sbe = be[lf];
+        const float4 sh = chi[lf], sl = clo[lf];
+        // source leaf centre relative to the target leaf centre
+        const float cx = (sh.x - tch.x) + (sl.x - tcl.x);
+        const float cy = (sh.y - tch.y) + (sl.y - tcl.y);
+        const float cz = (sh.z - tch.z) + (sl.z - tcl.z);
+        for (int j0 = sbe.x; j0 < sbe.y; j0 += 32) {
+          const int cnt = min(32, sbe.y - j0);
+          __syncwarp();
+          if (lane < cnt) {
+            const real4<float> r = rel32[j0 + lane];
+            buf[lane] = make_float4(cx + r.x, cy + r.y, cz + r.z, r.q);
+          }
+          __syncwarp();
+          float p0[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+          for (int k = sub; k < cnt; k += S) pair(q0, t0, buf[k], j0 + k, p0);
+#pragma unroll
+          for (int c = 0; c < (FIELD ? 4 : 1); ++c) kahan(ks[c], kc[c], p0[c]);
+        }
+      }
+    }
+    double v[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) v[c] = (double)ks[c] - (double)kc[c];
+    for (int o = 1; o < S; o <<= 1)
+#pragma unroll
+      for (int c = 0; c < (FIELD ? 4 : 1); ++c) v[c] += __shfl_xor_sync(kFull, v[c], o);
+    if (act0 && sub == 0) {
+      acc_pot[t0] = v[0];
+      if (FIELD) {
+        acc_fld[3 * (size_t)t0] = v[1];
+        acc_fld[3 * (size_t)t0 + 1] = v[2];
+        acc_fld[3 * (size_t)t0 + 2] = v[3];
+      }
+    }
+  }
+}
+
 template <bool FIELD, bool MIXED, bool BIG>
 void launch_one(AranGpuSolver3d *s, int grid, cudaStream_t st) {
   DevTree &t = s->tree;
@@ -268,7 +378,16 @@ void launch_one(AranGpuSolver3d *s, int grid, cudaStream_t st) {
 
 template <bool FIELD, bool MIXED>
 void launch_pair(AranGpuSolver3d *s, cudaStream_t st) {
-  launch_one<FIELD, MIXED, false>(s, s->tree.nleaves, st);
+  DevTree &t = s->tree;
+  if (MIXED) {
+    k_p2p_warp<FIELD><<<ceil_div(t.nleaves, 4), 128, 0, st>>>(
+        t.nleaves, t.near_off.ptr, t.near_rng.ptr, t.leaf_be.ptr, t.leaf_chi.ptr, t.leaf_clo.ptr,
+        s->sx.ptr, s->sy.ptr, s->sz.ptr, s->rel32.ptr, s->acc_pot.ptr, s->acc_fld.ptr);
+    ACHECK(cudaGetLastError());
+    s->launches++;
+  } else {
+    launch_one<FIELD, MIXED, false>(s, s->tree.nleaves, st);
+  }
   if (s->tree.n_big) launch_one<FIELD, MIXED, true>(s, s->tree.n_big, st);
 }
 
