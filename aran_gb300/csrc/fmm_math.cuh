@@ -66,18 +66,27 @@ FMM_HD int m2l_vrow_off(int p, int n) {
 }
 
 // Stream layout of the lane-parallel M2L tables (FP32, order p), one block
-// per offset, in the order the kernel consumes it: the z-phases (cos, sin)
-// of m = 0..p; the forward rotation terms (l < p, m' <= l, m <= m': the
-// lower triangle of each even/odd Wigner block, the upper one following from
-// E[m][m'] = (-1)^{m-m'} E[m'][m] for m, m' > 0 and E[0][m] = 2 (-1)^m E[m][0],
-// O[0][m] = 0), in groups of four, each group four even-part factors then
-// four odd-part factors; the vertical factors times the offset's radial
-// powers, terms (m <= p, j = m..p, n = m..p-1); the backward rotation terms
-// (l <= p), grouped like the forward ones.
+// per offset, in the order the kernel consumes it:
+//  * the z-phases (cos, sin) of m = 0..p;
+//  * the forward rotation terms (l < p, m' <= l, m <= m'): the lower
+//    triangle of each even/odd Wigner block, the upper one following from
+//    E[m][m'] = (-1)^{m-m'} E[m'][m] for m, m' > 0, E[0][m] = 2 (-1)^m E[m][0]
+//    and O[0][m] = 0; degree l scaled by 1/beta_l; in groups of four, each
+//    group four even-part factors then four odd-part factors;
+//  * the vertical factors times the offset's radial powers, which are
+//    V(j, m, n) = (-1)^{j+m} beta_j / beta_n S(j, n) with S symmetric in
+//    (j, n): per m, the lower triangle of S over j, n in [m, p) (rows j,
+//    columns n <= j), then the row j = p;
+//  * the backward rotation terms (l <= p), grouped like the forward ones,
+//    column m of degree l scaled by (-1)^{l+m} beta_l, which makes each block
+//    symmetric (F[m][m'] = F[m'][m] for m, m' > 0, F[0][m] = 2 F[m][0] for
+//    the even part, 0 for the odd one).
 __host__ __device__ constexpr int m2l_lane_tet(int l) { return l * (l + 1) * (l + 2) / 6; }
 __host__ __device__ constexpr int m2l_lane_nf(int p) { return m2l_lane_tet(p); }
 __host__ __device__ constexpr int m2l_lane_nb(int p) { return m2l_lane_tet(p + 1); }
-__host__ __device__ constexpr int m2l_lane_nv(int p) { return p * (p + 1) * (p + 2) / 3; }
+// vertical terms of the orders m..p: sum over k = p - m of k (k + 3) / 2
+__host__ __device__ constexpr int m2l_lane_vtail(int k) { return k * (k + 1) * (k + 5) / 6; }
+__host__ __device__ constexpr int m2l_lane_nv(int p) { return m2l_lane_vtail(p); }
 __host__ __device__ constexpr int m2l_lane_f(int p) { return (2 * (p + 1) + 3) & ~3; }
 __host__ __device__ constexpr int m2l_lane_v(int p) {
   return m2l_lane_f(p) + 8 * ((m2l_lane_nf(p) + 3) / 4);
@@ -90,7 +99,7 @@ __host__ __device__ constexpr int m2l_lane_stride(int p) {
 }
 // index of the first vertical term of order m
 __host__ __device__ constexpr int m2l_lane_vpre(int p, int m) {
-  return m2l_lane_nv(p) - m2l_lane_nv(p - m);
+  return m2l_lane_vtail(p) - m2l_lane_vtail(p - m);
 }
 // orders with a lane-parallel M2L kernel
 __host__ __device__ constexpr bool m2l_lane_order(int p) { return p == 8 || p == 12; }

@@ -311,24 +311,41 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
       find_next(it + 1);
       __syncwarp();           // both lanes of every pair are done with the staged source
       prefetch();
-      // translation along z: z(j, m) = sum_n V(j, m, n) y(n, m), m-major slots
+      // translation along z in the scaled frame (y carries 1/beta_n from
+      // the forward table, the backward table restores (-1)^{j+m} beta_j):
+      // z(j, m) = sum_n S(j, n) y(n, m), S symmetric, m-major slots
       float z[NL];
       {
         const float4 *V4 = reinterpret_cast<const float4 *>(tb + m2l_lane_v(P));
         float4 vq = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int m = 0; m <= P; ++m)
+        for (int m = 0; m <= P; ++m) {
+          constexpr int KM = P + 1;
+          const int k = P - m;
+          float zz[KM];
 #pragma unroll
-          for (int j = m; j <= P; ++j) {
-            float a = 0.f;
+          for (int jj = 0; jj <= k; ++jj) zz[jj] = 0.f;
 #pragma unroll
-            for (int n = m; n < P; ++n) {
-              const int t = m2l_lane_vpre(P, m) + (j - m) * (P - m) + (n - m);
+          for (int jj = 0; jj < k; ++jj)
+#pragma unroll
+            for (int nn = 0; nn <= jj; ++nn) {
+              const int t = m2l_lane_vpre(P, m) + jj * (jj + 1) / 2 + nn;
               if ((t & 3) == 0) vq = V4[t >> 2];
-              a = fmaf(sel4(vq, t & 3), y[n * (n + 1) / 2 + m], a);
+              const float v = sel4(vq, t & 3);
+              const int n = m + nn, j = m + jj;
+              zz[jj] = fmaf(v, y[n * (n + 1) / 2 + m], zz[jj]);
+              if (nn < jj) zz[nn] = fmaf(v, y[j * (j + 1) / 2 + m], zz[nn]);
             }
-            z[m * (P + 1) - m * (m - 1) / 2 + (j - m)] = a;
+#pragma unroll
+          for (int nn = 0; nn < k; ++nn) {
+            const int t = m2l_lane_vpre(P, m) + k * (k + 1) / 2 + nn;
+            if ((t & 3) == 0) vq = V4[t >> 2];
+            const int n = m + nn;
+            zz[k] = fmaf(sel4(vq, t & 3), y[n * (n + 1) / 2 + m], zz[k]);
           }
+#pragma unroll
+          for (int jj = 0; jj <= k; ++jj) z[m * (P + 1) - m * (m - 1) / 2 + jj] = zz[jj];
+        }
       }
       // rotation back (degrees <= p); degree l of z dies as degree l of o
       // is made, so the two share the registers
@@ -354,12 +371,11 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
               if ((t & 3) == 0) bq = B4[2 * (t >> 2)];
               const float v = sel4(bq, t & 3);
               od[mp] = fmaf(v, zi[m], od[mp]);
-              if (m < mp) ot[m] = fmaf(v, (mp & 1) ? -zi[mp] : zi[mp], ot[m]);
+              if (m < mp) ot[m] = fmaf(v, zi[mp], ot[m]);
             }
           o[l * (l + 1) / 2] = fmaf(f0, ot[0], od[0]);
 #pragma unroll
-          for (int m = 1; m <= l; ++m)
-            o[l * (l + 1) / 2 + m] = (m & 1) ? od[m] - ot[m] : od[m] + ot[m];
+          for (int m = 1; m <= l; ++m) o[l * (l + 1) / 2 + m] = od[m] + ot[m];
         }
       }
       // conjugate z-phase and accumulate, after the last table read: real

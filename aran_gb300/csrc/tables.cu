@@ -137,7 +137,7 @@ __global__ void k_m2l_lane_tables(int p, int ndir, const float *__restrict__ src
   // q-th float of a grouped rotation stream: term 4 (q / 8) + q % 4, part
   // (q / 4) % 2; term t = tet(l) + m'(m'+1)/2 + m is row m', column m of
   // degree l
-  auto rot = [&](int q, int nterm, int nc, int base) -> float {
+  auto rot = [&](int q, int nterm, int nc, int base, bool back) -> float {
     const int t = 4 * (q >> 3) + (q & 3), part = (q >> 2) & 1;
     if (t >= nterm) return 0.f;
     int l = 0;
@@ -145,25 +145,36 @@ __global__ void k_m2l_lane_tables(int p, int ndir, const float *__restrict__ src
     int r = t - m2l_lane_tet(l), mp = 0;
     while (tri(mp + 1) <= r) ++mp;
     const int m = r - tri(mp);
-    return s[base + 2 * (m2l_plane_off(nc, m) + tri(l, mp) - tri(m)) + part];
+    const double f = back ? (((l + m) & 1) ? -beta_l(l) : beta_l(l)) : 1. / beta_l(l);
+    return (float)(f * s[base + 2 * (m2l_plane_off(nc, m) + tri(l, mp) - tri(m)) + part]);
   };
   float v = 0.f;
   if (e < F) {
     if (e < 2 * (p + 1)) v = s[D.ph + e];
   } else if (e < V) {
-    v = rot(e - F, m2l_lane_nf(p), tri(p), D.ef);
+    v = rot(e - F, m2l_lane_nf(p), tri(p), D.ef, false);
   } else if (e < B) {
     const int t = e - V;
     if (t < m2l_lane_nv(p)) {
       int m = 0;
       while (m2l_lane_vpre(p, m + 1) <= t) ++m;
-      const int r = t - m2l_lane_vpre(p, m);
-      const int j = m + r / (p - m), n = m + r % (p - m);
-      const int k = m * (p + 1) - m * (m - 1) / 2 + (j - m);   // m-major slot of (j, m)
-      v = s[D.vv + m2l_vrow_off(p, n) + k];
+      const int r = t - m2l_lane_vpre(p, m), k = p - m;
+      int j, n;
+      if (r < tri(k)) {          // lower triangle: row j, column n <= j
+        int jj = 0;
+        while (tri(jj + 1) <= r) ++jj;
+        j = m + jj;
+        n = m + (r - tri(jj));
+      } else {                   // row j = p
+        j = p;
+        n = m + (r - tri(k));
+      }
+      const int slot = m * (p + 1) - m * (m - 1) / 2 + (j - m);   // m-major slot of (j, m)
+      const double sg = ((j + m) & 1) ? -1. : 1.;
+      v = (float)(sg * beta_l(n) / beta_l(j) * s[D.vv + m2l_vrow_off(p, n) + slot]);
     }
   } else {
-    v = rot(e - B, m2l_lane_nb(p), tri(p + 1), D.ei);
+    v = rot(e - B, m2l_lane_nb(p), tri(p + 1), D.ei, true);
   }
   dst[i] = v;
 }
