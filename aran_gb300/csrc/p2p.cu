@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(128, 10) k_p2p(
 // leaf partials) is paid once per lane per source leaf.
 // Ranges of more than kBigRange points are left to the chunked pass.
 template <bool FIELD>
-__global__ void __launch_bounds__(128, 7) k_p2p_warp(
+__global__ void __launch_bounds__(128, 8) k_p2p_warp(
     int nleaves, const int *__restrict__ near_off, const int *__restrict__ near_rng,
     const int2 *__restrict__ be, const float4 *__restrict__ chi, const float4 *__restrict__ clo,
     const double *__restrict__ sx, const double *__restrict__ sy, const double *__restrict__ sz,
@@ -275,10 +275,13 @@ __global__ void __launch_bounds__(128, 7) k_p2p_warp(
   if (L >= nleaves) return;
   const int2 tbe = be[L];
   const int b = tbe.x, nt = tbe.y - tbe.x;
-  const int S = nt <= 8 ? 4 : (nt <= 16 ? 2 : 1);
+  // lanes per target as a compile-time constant: one body per S
+  const int Sd = nt <= 8 ? 4 : (nt <= 16 ? 2 : 1);
+  auto body = [&](auto sc) {
+  constexpr int S = decltype(sc)::value;
   const int sub = lane & (S - 1);
   const float4 tch = chi[L], tcl = clo[L];
-  const float thr2 = tch.w;
+  const float thr2 = FIELD ? fmaxf(tch.w, 1e-10f) : tch.w;
   const int r0 = near_off[L], r1 = near_off[L + 1];
   float4 *buf = sbuf[w];
   const int step = 32 / S;
@@ -298,20 +301,27 @@ __global__ void __launch_bounds__(128, 7) k_p2p_warp(
     auto pair = [&](const real4<float> &q, int t, const float4 &sv, int j, float *p) {
       float dx = q.x - sv.x, dy = q.y - sv.y, dz = q.z - sv.z;
       float r2 = dx * dx + dy * dy + dz * dz;
+      float qq = sv.w;
+      // close pairs (and the guard of the field kernel, r2 <= 1e-10, or the
+      // pair of a point with itself) take the rare branch: a zero charge
+      // there keeps the common path free of selects
       if (__builtin_expect(r2 < thr2, 0)) {
         if (j == t) {
-          r2 = 0.f;
+          qq = 0.f;
+          r2 = 1.f;
         } else {
-          // close pair: difference from the FP64 positions
           dx = (float)(sx[t] - sx[j]);
           dy = (float)(sy[t] - sy[j]);
           dz = (float)(sz[t] - sz[j]);
           r2 = dx * dx + dy * dy + dz * dz;
+          if (!(FIELD ? (r2 > 1e-10f) : (r2 > 0.f))) {
+            qq = 0.f;
+            r2 = 1.f;
+          }
         }
       }
-      const bool ok = FIELD ? (r2 > 1e-10f) : (r2 > 0.f);
-      const float inv = ok ? rsqrtf(r2) : 0.f;
-      const float qi = sv.w * inv;
+      const float inv = rsqrtf(r2);
+      const float qi = qq * inv;
       p[0] += qi;
       if (FIELD) {
         const float q3 = qi * inv * inv;
@@ -362,6 +372,10 @@ __global__ void __launch_bounds__(128, 7) k_p2p_warp(
       }
     }
   }
+  };
+  if (Sd == 4) body(std::integral_constant<int, 4>{});
+  else if (Sd == 2) body(std::integral_constant<int, 2>{});
+  else body(std::integral_constant<int, 1>{});
 }
 
 template <bool FIELD, bool MIXED, bool BIG>

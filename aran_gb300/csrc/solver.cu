@@ -257,6 +257,8 @@ int aran_gpu_solver3d_tree_lists(AranGpuSolver3d *s, uint64_t *node_ids, int32_t
       if (node_leaf) node_leaf[i] = child[i] < 0 ? 1 : 0;
     }
     if (far_pairs) {
+      build_far_lists(s);
+      ACHECK(cudaStreamSynchronize(s->s0));
       std::vector<int> off(nn + 1), src(t.n_far);
       ACHECK(cudaMemcpy(off.data(), t.far_off.ptr, (nn + 1) * sizeof(int), cudaMemcpyDeviceToHost));
       if (t.n_far) ACHECK(cudaMemcpy(src.data(), t.far_src.ptr, t.n_far * sizeof(int), cudaMemcpyDeviceToHost));

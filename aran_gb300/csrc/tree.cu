@@ -472,6 +472,24 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
   ACHECK(cudaEventRecord(s->ev[2 * Stage::TREE + 1], st));
 }
 
+// M2L pair lists (source node and offset code per pair, CSR over the target
+// nodes) from the counts build_lists scanned into far_off
+void build_far_lists(AranGpuSolver3d *s) {
+  DevTree &t = s->tree;
+  if (t.far_built) return;
+  cudaStream_t st = s->s0;
+  const int TB = 256;
+  const int nn = t.nnodes;
+  t.far_src.reserve(t.n_far + 1);
+  t.far_dir.reserve(t.n_far + 1);
+  k_far<<<ceil_div(nn, TB), TB, 0, st>>>(nn, 0, t.begin.ptr, t.end.ptr, t.child.ptr, t.parent.ptr,
+                                          t.ijk.ptr, t.col.ptr, t.ncol.ptr, nullptr, t.far_off.ptr,
+                                          t.far_src.ptr, t.far_dir.ptr, 1);
+  ACHECK(cudaGetLastError());
+  s->launches++;
+  t.far_built = true;
+}
+
 void build_lists(AranGpuSolver3d *s) {
   cudaStream_t st = s->s0;
   DevTree &t = s->tree;
@@ -500,12 +518,11 @@ void build_lists(AranGpuSolver3d *s) {
   ACHECK(cudaMemcpyAsync(&nfar, t.far_off.ptr + nn, sizeof(int), cudaMemcpyDeviceToHost, st));
   ACHECK(cudaStreamSynchronize(st));
   t.n_far = nfar;
-  t.far_src.reserve(nfar + 1);
-  t.far_dir.reserve(nfar + 1);
-  k_far<<<ceil_div(nn, TB), TB, 0, st>>>(nn, 0, t.begin.ptr, t.end.ptr, t.child.ptr, t.parent.ptr,
-                                          t.ijk.ptr, t.col.ptr, t.ncol.ptr, nullptr, t.far_off.ptr,
-                                          t.far_src.ptr, t.far_dir.ptr, 1);
-  s->launches++;
+  // the pair lists themselves only feed the kkylin M2L (the rotation
+  // kernels find their sources from the colleague grids); otherwise they
+  // are written when asked for (build_far_lists)
+  t.far_built = false;
+  if (s->cfg.flavour == ARAN_FLAVOUR_KKYLIN) build_far_lists(s);
 
   // leaves in Morton order
   DBuf<int> &lflags = s->idx_in;  // reuse (n ints)
