@@ -51,11 +51,18 @@ WORKLOADS = {
 
 
 def m2l_flops(p: int) -> int:
-    """Algorithmic flops of one rotate-flavour M2L: 4[A(p-1) + B(p) + A(p)]
-    with A(L) = (L+1)(L+2)(4L+3)/6 (real d-matrix x complex rotation MACs)
-    and B(p) = p(p+1)(p+2)/3 (vertical translation MACs)."""
-    A = lambda L: (L + 1) * (L + 2) * (4 * L + 3) // 6
-    return 4 * (A(p - 1) + p * (p + 1) * (p + 2) // 3 + A(p))
+    """Algorithmic flops of one rotate-flavour M2L as the GPU applies it:
+    2 flops per multiply-add of
+      * the z-phase of the tri(p) source and tri(p+1) local coefficients
+        (4 multiply-adds per complex product),
+      * the forward rotation, sum_{l<p} (l+1)^2 real factors on each of the
+        real and imaginary parts (even/odd Wigner blocks),
+      * the translation along z, p(p+1)(p+2)/3 real factors on both parts,
+      * the backward rotation, sum_{l<=p} (l+1)^2 on both parts."""
+    sq = lambda L: L * (L + 1) * (2 * L + 1) // 6          # sum_{l<L} (l+1)^2
+    tri = lambda L: L * (L + 1) // 2
+    macs = 4 * (tri(p) + tri(p + 1)) + 2 * (sq(p) + p * (p + 1) * (p + 2) // 3 + sq(p + 1))
+    return 2 * macs
 
 
 def make_workload(name: str, seed_offset: int = 0):
@@ -306,7 +313,11 @@ def cpu_baseline(name: str, n_sample: int, procs: int, rounds: int = 1) -> dict:
 
 
 # ----------------------------------------------------------------- GPU arm
-M2L_DRAM_BYTES_PER_NODE = (28.17408e6 + 0.37632e6) / 37449
+# DRAM bytes of the FP32 M2L launch per tree node: ncu capture of
+# k_m2l_lanes<12> on uniform1m (37449 nodes), dram__bytes_read.sum +
+# dram__bytes_write.sum = 26.004224 MB + 0.010496 MB
+# (profiles/m2l_lanes_uniform1m_p12_mixed.md)
+M2L_DRAM_BYTES_PER_NODE = (26.004224e6 + 0.010496e6) / 37449
 
 
 def run_gpu(args):
@@ -455,7 +466,10 @@ def run_gpu(args):
     # written local once (FP32 complex), at the HBM roofline
     alg_bytes = (info["far"] * (p * (p + 1) // 2) + info["nodes"] * ((p + 1) * (p + 2) // 2)) * 8
     roof = {
-        "kernel": "k_m2l_sibling<float> (rotate M2L, all levels, one launch)",
+        "kernel": ("k_m2l_sibling<float> (rotate M2L, all levels, one launch)"
+                   if os.environ.get("ARAN_M2L_KERNEL") == "sibling" or p not in (8, 12)
+                   or args.precision != "mixed" else
+                   f"k_m2l_lanes<{p}> (rotate M2L, FP32 lane pairs, all levels, one launch)"),
         "bound": "fp32",
         "achieved": round(achieved, 3), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
         "frac": round(achieved / fp32_peak, 4),
@@ -468,9 +482,8 @@ def run_gpu(args):
                      "achieved_gbs": round(alg_bytes / m2l_s / 1e9, 1),
                      "peak_gbs": peaks.get("hbm_gbs", 6803.8),
                      "frac": round(alg_bytes / m2l_s / 1e9 / peaks.get("hbm_gbs", 6803.8), 4)},
-        # DRAM bytes per launch: ncu capture of this kernel on uniform1m
-        # (profiles/m2l_sibling_uniform1m_p12_mixed.md), 762 B per tree node,
-        # scaled by this tree's node count
+        # DRAM bytes per launch: ncu capture of this kernel on uniform1m,
+        # 694 B per tree node, scaled by this tree's node count
         "traffic": (args.m2l_traffic if args.m2l_traffic is not None
                     else round(M2L_DRAM_BYTES_PER_NODE * info["nodes"])),
         "traffic_source": ("--m2l-traffic" if args.m2l_traffic is not None else
