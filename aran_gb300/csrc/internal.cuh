@@ -113,6 +113,7 @@ struct DevTree {
   int n_parents = 0;
   int n_big = 0;
   int64_t n_far = 0;
+  bool far_counted = false;           // far_off and n_far made (count_far_lists)
   bool far_built = false;             // far_src/far_dir written (build_far_lists)
   int64_t n_near_rng = 0;
 };
@@ -193,6 +194,7 @@ namespace aran {
 // tree.cu
 void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double *d_q);
 void build_lists(AranGpuSolver3d *s);
+void count_far_lists(AranGpuSolver3d *s);
 void build_far_lists(AranGpuSolver3d *s);
 // tables.cu
 void build_tables(AranGpuSolver3d *s);

@@ -560,6 +560,7 @@ void scatter_outputs(AranGpuSolver3d *s, double *pot, double *fld) {
 
 void compute_stats(AranGpuSolver3d *s) {
   DevTree &t = s->tree;
+  count_far_lists(s);
   s->stats_dev.reserve(3);
   ACHECK(cudaMemsetAsync(s->stats_dev.ptr, 0, 3 * sizeof(unsigned long long), s->s0));
   int nmax = t.nnodes > t.nleaves ? t.nnodes : t.nleaves;

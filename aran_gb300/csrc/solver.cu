@@ -213,6 +213,11 @@ int aran_gpu_solver3d_tree_info(AranGpuSolver3d *s, int64_t info[5]) {
   if (!s || !info) return fail(ARAN_ERR_INVALID, "NULL argument");
   if (!s->have_tree) return fail(ARAN_ERR_INVALID, "no solve has run yet");
   DevTree &t = s->tree;
+  try {
+    count_far_lists(s);
+  } catch (const CudaError &ce) {
+    return from_cuda(ce);
+  }
   info[0] = t.nnodes;
   info[1] = t.n_far;
   // directed near leaf entries: expand the ranges

@@ -472,11 +472,38 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
   ACHECK(cudaEventRecord(s->ev[2 * Stage::TREE + 1], st));
 }
 
+// M2L pair counts per target node, scanned into far_off (n_far = their
+// sum, the M2L counter).  The rotation kernels do not need them, so they are
+// made when the counter, the lists or the tree summary is asked for.
+void count_far_lists(AranGpuSolver3d *s) {
+  DevTree &t = s->tree;
+  if (t.far_counted) return;
+  cudaStream_t st = s->s0;
+  const int TB = 256;
+  const int nn = t.nnodes;
+  t.far_off.reserve(nn + 1);
+  DBuf<int> &cntbuf = s->scan_tmp;
+  cntbuf.reserve((size_t)nn + 1);
+  k_far<<<ceil_div(nn, TB), TB, 0, st>>>(nn, 0, t.begin.ptr, t.end.ptr, t.child.ptr, t.parent.ptr,
+                                          t.ijk.ptr, t.col.ptr, t.ncol.ptr, cntbuf.ptr, nullptr,
+                                          nullptr, nullptr, 0);
+  ACHECK(cudaGetLastError());
+  s->launches++;
+  ACHECK(cudaMemsetAsync(cntbuf.ptr + nn, 0, sizeof(int), st));
+  exclusive_scan(s, cntbuf.ptr, t.far_off.ptr, nn + 1, st);
+  int nfar = 0;
+  ACHECK(cudaMemcpyAsync(&nfar, t.far_off.ptr + nn, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaStreamSynchronize(st));
+  t.n_far = nfar;
+  t.far_counted = true;
+}
+
 // M2L pair lists (source node and offset code per pair, CSR over the target
-// nodes) from the counts build_lists scanned into far_off
+// nodes)
 void build_far_lists(AranGpuSolver3d *s) {
   DevTree &t = s->tree;
   if (t.far_built) return;
+  count_far_lists(s);
   cudaStream_t st = s->s0;
   const int TB = 256;
   const int nn = t.nnodes;
@@ -504,23 +531,12 @@ void build_lists(AranGpuSolver3d *s) {
                                                     t.parent.ptr, t.ijk.ptr, t.col.ptr, t.ncol.ptr);
     s->launches++;
   }
-  // far lists over all nodes
-  t.far_off.reserve(nn + 1);
   DBuf<int> &cntbuf = s->scan_tmp;
   cntbuf.reserve((size_t)nn + 1 + (size_t)n + 1);
-  k_far<<<ceil_div(nn, TB), TB, 0, st>>>(nn, 0, t.begin.ptr, t.end.ptr, t.child.ptr, t.parent.ptr,
-                                          t.ijk.ptr, t.col.ptr, t.ncol.ptr, cntbuf.ptr, nullptr,
-                                          nullptr, nullptr, 0);
-  s->launches++;
-  ACHECK(cudaMemsetAsync(cntbuf.ptr + nn, 0, sizeof(int), st));
-  exclusive_scan(s, cntbuf.ptr, t.far_off.ptr, nn + 1, st);
-  int nfar = 0;
-  ACHECK(cudaMemcpyAsync(&nfar, t.far_off.ptr + nn, sizeof(int), cudaMemcpyDeviceToHost, st));
-  ACHECK(cudaStreamSynchronize(st));
-  t.n_far = nfar;
-  // the pair lists themselves only feed the kkylin M2L (the rotation
-  // kernels find their sources from the colleague grids); otherwise they
-  // are written when asked for (build_far_lists)
+  // M2L pairs: the lists only feed the kkylin M2L (the rotation kernels
+  // find their sources from the colleague grids); otherwise counts and
+  // lists are made when asked for (count_far_lists, build_far_lists)
+  t.far_counted = false;
   t.far_built = false;
   if (s->cfg.flavour == ARAN_FLAVOUR_KKYLIN) build_far_lists(s);
 
