@@ -260,7 +260,10 @@ __global__ void __launch_bounds__(128, 10) k_p2p(
 // that loads them, and every lane sums them against its own targets from
 // broadcast reads: lanes per target S = 4 (n <= 8), 2 (n <= 16), else 1
 // (32 targets per pass), so the per-leaf set-up (centres, Kahan adds of the
-// leaf partials) is paid once per lane per source leaf.
+// leaf partials) is paid once per lane per source leaf.  The pair loop has no
+// branch: the distance is clamped below at h/8, and a lane whose chunk held a
+// closer pair (or the point itself) takes the stand-ins back and adds those
+// pairs from the FP64 positions afterwards.
 // Ranges of more than kBigRange points are left to the chunked pass.
 template <bool FIELD>
 __global__ void __launch_bounds__(128, 8) k_p2p_warp(
@@ -297,37 +300,54 @@ __global__ void __launch_bounds__(128, 8) k_p2p_warp(
       comp = (t2 - sum) - y;
       sum = t2;
     };
-    // one target against the staged source k (point j): partial sums p[4]
-    auto pair = [&](const real4<float> &q, int t, const float4 &sv, int j, float *p) {
-      float dx = q.x - sv.x, dy = q.y - sv.y, dz = q.z - sv.z;
-      float r2 = dx * dx + dy * dy + dz * dz;
-      float qq = sv.w;
-      // close pairs (and the guard of the field kernel, r2 <= 1e-10, or the
-      // pair of a point with itself) take the rare branch: a zero charge
-      // there keeps the common path free of selects
-      if (__builtin_expect(r2 < thr2, 0)) {
-        if (j == t) {
-          qq = 0.f;
-          r2 = 1.f;
-        } else {
-          dx = (float)(sx[t] - sx[j]);
-          dy = (float)(sy[t] - sy[j]);
-          dz = (float)(sz[t] - sz[j]);
-          r2 = dx * dx + dy * dy + dz * dz;
-          if (!(FIELD ? (r2 > 1e-10f) : (r2 > 0.f))) {
-            qq = 0.f;
-            r2 = 1.f;
-          }
-        }
-      }
-      const float inv = rsqrtf(r2);
-      const float qi = qq * inv;
+    // one target against a staged source, r2 clamped below at thr2 (h/8
+    // squared, at least the field guard 1e-10): close pairs and the point
+    // itself add a bounded stand-in that close_fix takes back
+    auto pair = [&](const real4<float> &q, const float4 &sv, float *p, float &rmin) {
+      const float dx = q.x - sv.x, dy = q.y - sv.y, dz = q.z - sv.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      rmin = fminf(rmin, r2);
+      const float inv = rsqrtf(fmaxf(r2, thr2));
+      const float qi = sv.w * inv;
       p[0] += qi;
       if (FIELD) {
         const float q3 = qi * inv * inv;
         p[1] -= q3 * dx;
         p[2] -= q3 * dy;
         p[3] -= q3 * dz;
+      }
+    };
+    // for a close pair: remove the stand-in (the same FP32 expressions) and
+    // add the pair from the FP64 positions (nothing for the point itself or
+    // inside the field guard)
+    auto close_fix = [&](const real4<float> &q, int t, const float4 &sv, int j, float *p) {
+      const float dx = q.x - sv.x, dy = q.y - sv.y, dz = q.z - sv.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (!(r2 < thr2)) return;
+      {
+        const float inv = rsqrtf(fmaxf(r2, thr2));
+        const float qi = sv.w * inv;
+        p[0] -= qi;
+        if (FIELD) {
+          const float q3 = qi * inv * inv;
+          p[1] += q3 * dx;
+          p[2] += q3 * dy;
+          p[3] += q3 * dz;
+        }
+      }
+      if (j == t) return;
+      const float ex = (float)(sx[t] - sx[j]), ey = (float)(sy[t] - sy[j]),
+                  ez = (float)(sz[t] - sz[j]);
+      const float e2 = ex * ex + ey * ey + ez * ez;
+      if (!(FIELD ? (e2 > 1e-10f) : (e2 > 0.f))) return;
+      const float inv = rsqrtf(e2);
+      const float qi = sv.w * inv;
+      p[0] += qi;
+      if (FIELD) {
+        const float q3 = qi * inv * inv;
+        p[1] -= q3 * ex;
+        p[2] -= q3 * ey;
+        p[3] -= q3 * ez;
       }
     };
     for (int rr = r0; rr < r1; ++rr) {
@@ -350,8 +370,12 @@ __global__ void __launch_bounds__(128, 8) k_p2p_warp(
           }
           __syncwarp();
           float p0[4] = {0.f, 0.f, 0.f, 0.f};
+          float rmin = 3.0e38f;
 #pragma unroll 4
-          for (int k = sub; k < cnt; k += S) pair(q0, t0, buf[k], j0 + k, p0);
+          for (int k = sub; k < cnt; k += S) pair(q0, buf[k], p0, rmin);
+          const bool flag = rmin < thr2;
+          if (__any_sync(kFull, flag) && flag)
+            for (int k = sub; k < cnt; k += S) close_fix(q0, t0, buf[k], j0 + k, p0);
 #pragma unroll
           for (int c = 0; c < (FIELD ? 4 : 1); ++c) kahan(ks[c], kc[c], p0[c]);
         }

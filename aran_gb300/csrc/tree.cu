@@ -84,47 +84,56 @@ __device__ __forceinline__ int digit_at(const uint64_t *k, int j, int shift) {
   return (int)((k[j] >> shift) & 7ull);
 }
 
+// eight threads per node of the level, thread c making child c: its range
+// ends at the first key of the parent's range whose digit at this depth
+// exceeds c (one binary search per thread), and begins where child c-1 ends
+// (the neighbouring lane's result)
 __global__ void k_make_children(int cnt, int off, int child_off, const int *__restrict__ flags,
                                 const int *__restrict__ pos, const uint64_t *__restrict__ skeys,
                                 int d, NodeArrays na, double lbx, double lby, double lbz,
                                 double ubx, double uby, double ubz) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= cnt) return;
-  int node = off + i;
-  if (!flags[i]) {
-    na.child[node] = -1;
-    return;
-  }
-  int base = child_off + 8 * pos[i];
-  na.child[node] = base;
-  int b = na.begin[node], e = na.end[node];
-  int shift = 3 * (kKeyBits - d - 1);
-  uint64_t pk = na.key[node];
-  int pi = na.ijk[3 * node], pj = na.ijk[3 * node + 1], pk3 = na.ijk[3 * node + 2];
-  int start = b;
-  for (int c = 0; c < 8; ++c) {
-    // first index in [start, e) whose digit is > c
-    int lo = start, hi = e;
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int i = (int)(g >> 3), c = (int)(g & 7);
+  const bool live = i < cnt;
+  const int node = off + (live ? i : 0);
+  const bool split = live && flags[i] != 0;
+  int lo = 0, b = 0;
+  if (split) {
+    b = na.begin[node];
+    const int e = na.end[node];
+    const int shift = 3 * (kKeyBits - d - 1);
+    lo = b;
+    int hi = e;
     while (lo < hi) {
-      int mid = (lo + hi) >> 1;
+      const int mid = (lo + hi) >> 1;
       if (digit_at(skeys, mid, shift) <= c) lo = mid + 1; else hi = mid;
     }
-    int cn = base + c;
-    na.key[cn] = (pk << 3) | (uint64_t)c;
-    int ci = (pi << 1) | (c & 1), cj = (pj << 1) | ((c >> 1) & 1), ck = (pk3 << 1) | ((c >> 2) & 1);
-    na.ijk[3 * cn] = ci;
-    na.ijk[3 * cn + 1] = cj;
-    na.ijk[3 * cn + 2] = ck;
-    na.depth[cn] = (uint8_t)(d + 1);
-    na.begin[cn] = start;
-    na.end[cn] = lo;
-    na.child[cn] = -1;
-    na.parent[cn] = node;
-    na.center[3 * cn] = node_center_axis(lbx, ubx, d + 1, ci);
-    na.center[3 * cn + 1] = node_center_axis(lby, uby, d + 1, cj);
-    na.center[3 * cn + 2] = node_center_axis(lbz, ubz, d + 1, ck);
-    start = lo;
   }
+  // the eight threads of a node are eight consecutive lanes
+  const int prev = __shfl_up_sync(0xffffffffu, lo, 1, 8);
+  if (!live) return;
+  if (!split) {
+    if (c == 0) na.child[node] = -1;
+    return;
+  }
+  const int base = child_off + 8 * pos[i];
+  if (c == 0) na.child[node] = base;
+  const uint64_t pk = na.key[node];
+  const int pi = na.ijk[3 * node], pj = na.ijk[3 * node + 1], pk3 = na.ijk[3 * node + 2];
+  const int cn = base + c;
+  na.key[cn] = (pk << 3) | (uint64_t)c;
+  const int ci = (pi << 1) | (c & 1), cj = (pj << 1) | ((c >> 1) & 1), ck = (pk3 << 1) | ((c >> 2) & 1);
+  na.ijk[3 * cn] = ci;
+  na.ijk[3 * cn + 1] = cj;
+  na.ijk[3 * cn + 2] = ck;
+  na.depth[cn] = (uint8_t)(d + 1);
+  na.begin[cn] = c == 0 ? b : prev;
+  na.end[cn] = lo;
+  na.child[cn] = -1;
+  na.parent[cn] = node;
+  na.center[3 * cn] = node_center_axis(lbx, ubx, d + 1, ci);
+  na.center[3 * cn + 1] = node_center_axis(lby, uby, d + 1, cj);
+  na.center[3 * cn + 2] = node_center_axis(lbz, ubz, d + 1, ck);
 }
 
 __device__ __forceinline__ bool adjacent(const int *ijk, int a, int b) {
@@ -459,7 +468,7 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
       grow_nodes(t, need, child_off, st);
       na = arrays(t);
     }
-    k_make_children<<<ceil_div(cnt, TB), TB, 0, st>>>(cnt, off, child_off, flags.ptr, pos,
+    k_make_children<<<ceil_div(8 * (int64_t)cnt, TB), TB, 0, st>>>(cnt, off, child_off, flags.ptr, pos,
                                                        s->keys_out.ptr, d, na, c.lb[0], c.lb[1],
                                                        c.lb[2], c.ub[0], c.ub[1], c.ub[2]);
     s->launches++;
