@@ -53,39 +53,47 @@ __device__ __forceinline__ int rng_count(const int2 *be, int la, int lb) {
   return be[lb - 1].y - be[la].x;
 }
 
-// heavy ranges -> leaf-aligned chunks; mode 0 counts, mode 1 writes
-__global__ void k_big_items(int nleaves, const int *__restrict__ near_off,
+// heavy ranges -> leaf-aligned chunks, one thread per near range: mode 0
+// adds the chunk count to *cnt, mode 1 claims slots from *cnt and writes the
+// chunks (target leaf found by binary search over near_off)
+__global__ void k_big_items(int64_t nrng, int nleaves, const int *__restrict__ near_off,
                             const int *__restrict__ near_rng, const int2 *__restrict__ be,
-                            int *__restrict__ cnt, const int *__restrict__ off,
-                            int4 *__restrict__ items, int mode) {
-  int L = blockIdx.x * blockDim.x + threadIdx.x;
-  if (L >= nleaves) return;
-  int k = 0, w = mode ? off[L] : 0;
-  for (int r = near_off[L]; r < near_off[L + 1]; ++r) {
-    int la = near_rng[2 * r], lb = near_rng[2 * r + 1];
-    if (lb <= la) continue;
-    int c = rng_count(be, la, lb);
-    if (c <= kBigRange) continue;
-    int nch = (c + kBigRange - 1) / kBigRange;
-    int p0 = be[la].x;
-    int prev = la;
-    for (int i = 1; i <= nch; ++i) {
-      int nxt = lb;
-      if (i < nch) {
-        // first leaf in [prev, lb) whose begin >= p0 + i*kBigRange
-        int lo = prev, hi = lb, target = p0 + i * kBigRange;
-        while (lo < hi) {
-          int mid = (lo + hi) >> 1;
-          if (be[mid].x < target) lo = mid + 1; else hi = mid;
-        }
-        nxt = lo;
-      }
-      if (mode) items[w + k] = make_int4(L, prev, nxt, 0);
-      ++k;
-      prev = nxt;
-    }
+                            int *__restrict__ cnt, int4 *__restrict__ items, int mode) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nrng) return;
+  const int la = near_rng[2 * r], lb = near_rng[2 * r + 1];
+  if (lb <= la) return;
+  const int c = rng_count(be, la, lb);
+  if (c <= kBigRange) return;
+  const int nch = (c + kBigRange - 1) / kBigRange;
+  if (!mode) {
+    atomicAdd(cnt, nch);
+    return;
   }
-  if (!mode) cnt[L] = k;
+  const int w = atomicAdd(cnt, nch);
+  int lo = 0, hi = nleaves;                   // last leaf L with near_off[L] <= r
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (near_off[mid] <= r) lo = mid; else hi = mid;
+  }
+  const int L = lo;
+  const int p0 = be[la].x;
+  int prev = la;
+  for (int i = 1; i <= nch; ++i) {
+    int nxt = lb;
+    if (i < nch) {
+      // first leaf in [prev, lb) whose begin >= p0 + i*kBigRange
+      int l2 = prev, h2 = lb;
+      const int target = p0 + i * kBigRange;
+      while (l2 < h2) {
+        const int mid = (l2 + h2) >> 1;
+        if (be[mid].x < target) l2 = mid + 1; else h2 = mid;
+      }
+      nxt = l2;
+    }
+    items[w + i - 1] = make_int4(L, prev, nxt, 0);
+    prev = nxt;
+  }
 }
 
 template <typename T, bool FIELD, bool MIXED, bool BIG>
@@ -447,28 +455,24 @@ void build_p2p_work(AranGpuSolver3d *s) {
   ACHECK(cudaGetLastError());
   s->launches++;
   DBuf<int> &cnt = s->scan_tmp;
-  cnt.reserve(2 * (size_t)nl + 2);
-  int *off = cnt.ptr + nl + 1;
-  k_big_items<<<ceil_div(nl, TB), TB, 0, st>>>(nl, t.near_off.ptr, t.near_rng.ptr, t.leaf_be.ptr,
-                                               cnt.ptr, nullptr, nullptr, 0);
-  ACHECK(cudaGetLastError());
-  s->launches++;
-  ACHECK(cudaMemsetAsync(cnt.ptr + nl, 0, sizeof(int), st));
-  {
-    size_t bytes = 0;
-    ACHECK(cub::DeviceScan::ExclusiveSum(nullptr, bytes, cnt.ptr, off, nl + 1, st));
-    s->cub_tmp.reserve(bytes);
-    ACHECK(cub::DeviceScan::ExclusiveSum(s->cub_tmp.ptr, bytes, cnt.ptr, off, nl + 1, st));
-    s->launches += 2;
-  }
+  cnt.reserve(2);
+  const int64_t nr = t.n_near_rng;
   int nbig = 0;
-  ACHECK(cudaMemcpyAsync(&nbig, off + nl, sizeof(int), cudaMemcpyDeviceToHost, st));
-  ACHECK(cudaStreamSynchronize(st));
+  if (nr > 0) {
+    ACHECK(cudaMemsetAsync(cnt.ptr, 0, sizeof(int), st));
+    k_big_items<<<ceil_div(nr, TB), TB, 0, st>>>(nr, nl, t.near_off.ptr, t.near_rng.ptr,
+                                                 t.leaf_be.ptr, cnt.ptr, nullptr, 0);
+    ACHECK(cudaGetLastError());
+    s->launches++;
+    ACHECK(cudaMemcpyAsync(&nbig, cnt.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ACHECK(cudaStreamSynchronize(st));
+  }
   t.n_big = nbig;
   if (nbig) {
     t.big_items.reserve(nbig);
-    k_big_items<<<ceil_div(nl, TB), TB, 0, st>>>(nl, t.near_off.ptr, t.near_rng.ptr,
-                                                 t.leaf_be.ptr, cnt.ptr, off, t.big_items.ptr, 1);
+    ACHECK(cudaMemsetAsync(cnt.ptr, 0, sizeof(int), st));
+    k_big_items<<<ceil_div(nr, TB), TB, 0, st>>>(nr, nl, t.near_off.ptr, t.near_rng.ptr,
+                                                 t.leaf_be.ptr, cnt.ptr, t.big_items.ptr, 1);
     ACHECK(cudaGetLastError());
     s->launches++;
   }

@@ -39,6 +39,19 @@ def check_lists(s, oracle, x, maxbox, lb, ub, max_depth=21):
     assert np.array_equal(g["perm"], o["perm"])
 
 
+def cluster_beside_sparse(n, seed=16):
+    """93 % of the points in a cube of side 0.05 at the centre, the rest
+    uniform: coarse leaves touch the cluster's deep subtree, so near ranges
+    of more than 2,048 points (the chunked P2P pass) occur.  (Dense enough
+    for that, sparse enough that no pair falls inside the field kernel's
+    |r| <= 1e-5 guard, which the potential-only oracle solve does not have.)"""
+    rng = np.random.default_rng(seed)
+    k = int(n * 0.93)
+    x = np.concatenate([0.5 + rng.uniform(-0.025, 0.025, (k, 3)), rng.uniform(0, 1, (n - k, 3))])
+    q = rng.uniform(-1, 1, n)
+    return x, q
+
+
 CASES = [
     # name, generator, n, maxbox, p, lb, ub
     ("uniform", lambda n: W.uniform(n, 11), 6000, 20, 8, (0, 0, 0), (1, 1, 1)),
@@ -47,6 +60,7 @@ CASES = [
     ("blobs", lambda n: W.blobs(n, 14, nblobs=3), 15000, 24, 8, (0, 0, 0), (1, 1, 1)),
     ("circle-maxbox1", lambda n: W.circle(n), 240, 1, 12, (-1, -1, -1), (1, 1, 1)),
     ("box-aspect", lambda n: W.uniform(n, 15), 8000, 16, 8, (0, 0, 0), (1.0, 1.5, 3.0)),
+    ("cluster-heavy-ranges", cluster_beside_sparse, 30000, 16, 8, (0, 0, 0), (1, 1, 1)),
 ]
 
 
