@@ -143,33 +143,35 @@ struct DirOffsets {
 // ---------------------------------------------------------------------------
 // M2M rotate: aran/aransphericalseriesd-rotate.c:219-263 applied to the
 // multipole (aran_development3d_m2m_rotate, arandevelopment3d.c:402-409).
-// One warp per internal node of the level, summing its non-empty children.
+// One block per internal node of the level: warp o translates child o, and
+// the eight contributions are summed in child order.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_m2m_rotate(int cnt, int off, const int *__restrict__ child,
+__global__ void __launch_bounds__(256) k_m2m_rotate(int cnt, int off, const int *__restrict__ child,
                              const int *__restrict__ begin, const int *__restrict__ end, int p,
                              const T *__restrict__ dirs, DirOffsets D, const T *__restrict__ vm,
                              const uint8_t *__restrict__ lm_g, cplx<T> *__restrict__ mult) {
+  // one block of eight warps per node of the level, warp o translating
+  // child o; the eight contributions are summed in child order
   extern __shared__ unsigned char smem_raw[];
   const int nm = tri(p);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-  uint8_t *lm = smem_raw;
-  cplx<T> *bufs = reinterpret_cast<cplx<T> *>(smem_raw + ((2 * tri(p + 1) + 15) & ~15));
-  for (int i = threadIdx.x; i < 2 * tri(p + 1); i += blockDim.x) lm[i] = lm_g[i];
-  __syncthreads();
-  const int P = off + blockIdx.x * wpb + w;
-  if (P >= off + cnt) return;
+  const int lane = threadIdx.x & 31, o = threadIdx.x >> 5;
+  const int P = off + blockIdx.x;
+  if (blockIdx.x >= cnt) return;
   const int c0 = child[P];
   if (c0 < 0) return;
-  cplx<T> *src = bufs + (size_t)w * 2 * nm;
+  uint8_t *lm = smem_raw;
+  cplx<T> *bufs = reinterpret_cast<cplx<T> *>(smem_raw + ((2 * tri(p + 1) + 15) & ~15));
+  cplx<T> *part = bufs + (size_t)8 * 2 * nm;   // [child][coefficient]
+  for (int i = threadIdx.x; i < 2 * tri(p + 1); i += blockDim.x) lm[i] = lm_g[i];
+  __syncthreads();
+  cplx<T> *src = bufs + (size_t)o * 2 * nm;
   cplx<T> *rot = src + nm;
-  cplx<T> acc[(kMaxOrder * (kMaxOrder + 1) / 2 + 31) / 32];
-  const int K = (nm + 31) / 32;
-#pragma unroll
-  for (int k = 0; k < (kMaxOrder * (kMaxOrder + 1) / 2 + 31) / 32; ++k) acc[k] = cmake<T>(0, 0);
-  for (int o = 0; o < 8; ++o) {
-    int ch = c0 + o;
-    if (end[ch] == begin[ch]) continue;
+  cplx<T> *out = part + (size_t)o * nm;
+  const int ch = c0 + o;
+  if (end[ch] == begin[ch]) {
+    for (int c = lane; c < nm; c += 32) out[c] = cmake<T>(0, 0);
+  } else {
     const T *tab = dirs + (size_t)o * D.stride;
     load_phased(mult + (size_t)ch * nm, nm, lm, tab + D.ph, src, lane);
     __syncwarp();
@@ -190,23 +192,21 @@ __global__ void k_m2m_rotate(int cnt, int off, const int *__restrict__ child,
       src[c] = cmake<T>(re, im);
     }
     __syncwarp();
-#pragma unroll
-    for (int k = 0; k < (kMaxOrder * (kMaxOrder + 1) / 2 + 31) / 32; ++k) {
-      int c = lane + 32 * k;
-      if (k < K && c < nm) {
-        int l = lm[2 * c], mp = lm[2 * c + 1];
-        cplx<T> v = rot_one(tab + D.ei, tab + D.oi, src, l, mp);
-        T cr = tab[D.ph + 2 * mp], ci = -tab[D.ph + 2 * mp + 1];
-        acc[k].re += v.re * cr - v.im * ci;
-        acc[k].im += v.re * ci + v.im * cr;
-      }
+    for (int c = lane; c < nm; c += 32) {
+      int l = lm[2 * c], mp = lm[2 * c + 1];
+      cplx<T> v = rot_one(tab + D.ei, tab + D.oi, src, l, mp);
+      T cr = tab[D.ph + 2 * mp], ci = -tab[D.ph + 2 * mp + 1];
+      out[c] = cmake<T>(v.re * cr - v.im * ci, v.re * ci + v.im * cr);
     }
-    __syncwarp();
   }
-#pragma unroll
-  for (int k = 0; k < (kMaxOrder * (kMaxOrder + 1) / 2 + 31) / 32; ++k) {
-    int c = lane + 32 * k;
-    if (k < K && c < nm) mult[(size_t)P * nm + c] = acc[k];
+  __syncthreads();
+  for (int c = threadIdx.x; c < nm; c += blockDim.x) {
+    cplx<T> a = cmake<T>(0, 0);
+    for (int k = 0; k < 8; ++k) {
+      a.re += part[(size_t)k * nm + c].re;
+      a.im += part[(size_t)k * nm + c].im;
+    }
+    mult[(size_t)P * nm + c] = a;
   }
 }
 
@@ -475,13 +475,12 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   if (kk) kkylin_pass(s, 0);
   else {
     DirOffsets D = offsets<T>(p, 1);
-    const int WPB = 4;
-    size_t sm = ((2 * nl + 15) & ~15) + (size_t)WPB * 2 * nm * sizeof(cplx<T>) + 64;
+    size_t sm = ((2 * nl + 15) & ~15) + (size_t)8 * 3 * nm * sizeof(cplx<T>) + 64;
     smem_opt_in(k_m2m_rotate<T>, sm);
     for (int d = t.nlevels - 2; d >= 0; --d) {
       if (t.level_internal[d] == 0) continue;
       int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
-      k_m2m_rotate<T><<<ceil_div(cnt, WPB), WPB * 32, sm, st>>>(
+      k_m2m_rotate<T><<<cnt, 256, sm, st>>>(
           cnt, off, t.child.ptr, t.begin.ptr, t.end.ptr, p, tb.dir_m2m.ptr, D, tb.vm.ptr,
           tb.lm.ptr, mult);
       ACHECK(cudaGetLastError());

@@ -146,33 +146,55 @@ __device__ __forceinline__ int ncount(const int *begin, const int *end, int a) {
   return end[a] - begin[a];
 }
 
+// one warp per node of the level: lane j < 27 takes colleague j of the
+// parent and keeps those of its children that are non-empty and adjacent;
+// a warp prefix sum places them in (colleague, child) order
 __global__ void k_colleagues(int cnt, int off, const int *__restrict__ begin,
                              const int *__restrict__ end, const int *__restrict__ child,
                              const int *__restrict__ parent, const int *__restrict__ ijk,
                              int *__restrict__ col, int *__restrict__ ncol) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= cnt) return;
-  int c = off + i;
-  int k = 0;
-  if (ncount(begin, end, c) > 0) {
-    int p = parent[c];
-    if (p < 0) {
-      col[27 * c] = c;
-      k = 1;
-    } else {
-      int np = ncol[p];
-      for (int j = 0; j < np; ++j) {
-        int q = col[27 * p + j];
-        int c0 = child[q];
-        if (c0 < 0) continue;
-        for (int o = 0; o < 8; ++o) {
-          int s = c0 + o;
-          if (ncount(begin, end, s) > 0 && adjacent(ijk, c, s) && k < 27) col[27 * c + k++] = s;
-        }
-      }
-    }
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int i = (int)(g >> 5), lane = (int)(g & 31);
+  if (i >= cnt) return;               // whole warps leave together
+  const int c = off + i;
+  if (ncount(begin, end, c) == 0) {
+    if (lane == 0) ncol[c] = 0;
+    return;
   }
-  ncol[c] = k;
+  const int p = parent[c];
+  if (p < 0) {
+    if (lane == 0) {
+      col[27 * c] = c;
+      ncol[c] = 1;
+    }
+    return;
+  }
+  const int np = ncol[p];
+  unsigned keep = 0;                  // bit o: child o of colleague `lane` is kept
+  int c0 = -1;
+  if (lane < np) {
+    const int q = col[27 * p + lane];
+    c0 = child[q];
+    if (c0 >= 0)
+      for (int o = 0; o < 8; ++o) {
+        const int s = c0 + o;
+        if (ncount(begin, end, s) > 0 && adjacent(ijk, c, s)) keep |= 1u << o;
+      }
+  }
+  const int mine = __popc(keep);
+  int before = mine;                  // inclusive prefix over lanes
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, before, d);
+    if (lane >= d) before += v;
+  }
+  int k = before - mine;
+  for (int o = 0; o < 8; ++o)
+    if ((keep >> o) & 1u) {
+      if (k < 27) col[27 * c + k] = c0 + o;
+      ++k;
+    }
+  const int total = __shfl_sync(0xffffffffu, before, 31);
+  if (lane == 0) ncol[c] = total < 27 ? total : 27;
 }
 
 // M2L sources of node t (same depth, not adjacent, children of the parent's
@@ -536,7 +558,7 @@ void build_lists(AranGpuSolver3d *s) {
   t.ncol.reserve(nn);
   for (int d = 0; d < t.nlevels; ++d) {
     int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
-    k_colleagues<<<ceil_div(cnt, TB), TB, 0, st>>>(cnt, off, t.begin.ptr, t.end.ptr, t.child.ptr,
+    k_colleagues<<<ceil_div(32 * (int64_t)cnt, TB), TB, 0, st>>>(cnt, off, t.begin.ptr, t.end.ptr, t.child.ptr,
                                                     t.parent.ptr, t.ijk.ptr, t.col.ptr, t.ncol.ptr);
     s->launches++;
   }
