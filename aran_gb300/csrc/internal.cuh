@@ -106,6 +106,7 @@ struct DevTree {
   DBuf<int2> leaf_be;                 // particle [begin, end) per leaf ordinal
   DBuf<float4> leaf_chi, leaf_clo;    // FP32 leaf centre split hi + lo; chi.w = close-pair r^2
   DBuf<int4> big_items;               // (leaf, lf_a, lf_b, 0): chunks of heavy near ranges
+  DBuf<int> big_rng;                  // [0] chunk total, [1] range count, then heavy range indices
   DBuf<int> semi_off;                 // CSR over leaves of semifar nodes (threshold > 0)
   DBuf<int> semi_node, semi_leaf;     // per semifar pair: deep node, coarse leaf ordinal
   int n_semi = 0;

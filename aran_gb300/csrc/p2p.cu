@@ -53,47 +53,37 @@ __device__ __forceinline__ int rng_count(const int2 *be, int la, int lb) {
   return be[lb - 1].y - be[la].x;
 }
 
-// heavy ranges -> leaf-aligned chunks, one thread per near range: mode 0
-// adds the chunk count to *cnt, mode 1 claims slots from *cnt and writes the
-// chunks (target leaf found by binary search over near_off)
-__global__ void k_big_items(int64_t nrng, int nleaves, const int *__restrict__ near_off,
-                            const int *__restrict__ near_rng, const int2 *__restrict__ be,
-                            int *__restrict__ cnt, int4 *__restrict__ items, int mode) {
-  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= nrng) return;
+// heavy ranges -> leaf-aligned chunks of about kBigRange points: one block
+// per heavy range (listed by k_near with the offset of its first chunk), one
+// thread per chunk, whose ends are the first leaves whose points start at or
+// beyond p0 + i kBigRange (binary searches, independent per chunk)
+__global__ void k_big_items(const int *__restrict__ heavy, int nleaves,
+                            const int *__restrict__ near_off, const int *__restrict__ near_rng,
+                            const int2 *__restrict__ be, int4 *__restrict__ items) {
+  const int r = heavy[2 * blockIdx.x], coff = heavy[2 * blockIdx.x + 1];
   const int la = near_rng[2 * r], lb = near_rng[2 * r + 1];
-  if (lb <= la) return;
   const int c = rng_count(be, la, lb);
-  if (c <= kBigRange) return;
   const int nch = (c + kBigRange - 1) / kBigRange;
-  if (!mode) {
-    atomicAdd(cnt, nch);
-    return;
-  }
-  const int w = atomicAdd(cnt, nch);
-  int lo = 0, hi = nleaves;                   // last leaf L with near_off[L] <= r
+  int lo = 0, hi = nleaves;                   // target leaf: last L with near_off[L] <= r
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
     if (near_off[mid] <= r) lo = mid; else hi = mid;
   }
   const int L = lo;
   const int p0 = be[la].x;
-  int prev = la;
-  for (int i = 1; i <= nch; ++i) {
-    int nxt = lb;
-    if (i < nch) {
-      // first leaf in [prev, lb) whose begin >= p0 + i*kBigRange
-      int l2 = prev, h2 = lb;
-      const int target = p0 + i * kBigRange;
-      while (l2 < h2) {
-        const int mid = (l2 + h2) >> 1;
-        if (be[mid].x < target) l2 = mid + 1; else h2 = mid;
-      }
-      nxt = l2;
+  auto boundary = [&](int i) -> int {          // first leaf of chunk i
+    if (i <= 0) return la;
+    if (i >= nch) return lb;
+    int l2 = la, h2 = lb;
+    const int target = p0 + i * kBigRange;
+    while (l2 < h2) {
+      const int mid = (l2 + h2) >> 1;
+      if (be[mid].x < target) l2 = mid + 1; else h2 = mid;
     }
-    items[w + i - 1] = make_int4(L, prev, nxt, 0);
-    prev = nxt;
-  }
+    return l2;
+  };
+  for (int i = threadIdx.x; i < nch; i += blockDim.x)
+    items[coff + i] = make_int4(L, boundary(i), boundary(i + 1), 0);
 }
 
 template <typename T, bool FIELD, bool MIXED, bool BIG>
@@ -454,25 +444,18 @@ void build_p2p_work(AranGpuSolver3d *s) {
                                                t.leaf_be.ptr, t.leaf_chi.ptr, t.leaf_clo.ptr);
   ACHECK(cudaGetLastError());
   s->launches++;
-  DBuf<int> &cnt = s->scan_tmp;
-  cnt.reserve(2);
-  const int64_t nr = t.n_near_rng;
-  int nbig = 0;
-  if (nr > 0) {
-    ACHECK(cudaMemsetAsync(cnt.ptr, 0, sizeof(int), st));
-    k_big_items<<<ceil_div(nr, TB), TB, 0, st>>>(nr, nl, t.near_off.ptr, t.near_rng.ptr,
-                                                 t.leaf_be.ptr, cnt.ptr, nullptr, 0);
-    ACHECK(cudaGetLastError());
-    s->launches++;
-    ACHECK(cudaMemcpyAsync(&nbig, cnt.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  // chunk total and heavy-range count, as k_near listed them
+  int hb[2] = {0, 0};
+  if (t.n_near_rng > 0) {
+    ACHECK(cudaMemcpyAsync(hb, t.big_rng.ptr, sizeof(hb), cudaMemcpyDeviceToHost, st));
     ACHECK(cudaStreamSynchronize(st));
   }
+  const int nbig = hb[0], nheavy = hb[1];
   t.n_big = nbig;
   if (nbig) {
     t.big_items.reserve(nbig);
-    ACHECK(cudaMemsetAsync(cnt.ptr, 0, sizeof(int), st));
-    k_big_items<<<ceil_div(nr, TB), TB, 0, st>>>(nr, nl, t.near_off.ptr, t.near_rng.ptr,
-                                                 t.leaf_be.ptr, cnt.ptr, t.big_items.ptr, 1);
+    k_big_items<<<nheavy, 64, 0, st>>>(t.big_rng.ptr + 2, nl, t.near_off.ptr, t.near_rng.ptr,
+                                       t.leaf_be.ptr, t.big_items.ptr);
     ACHECK(cudaGetLastError());
     s->launches++;
   }

@@ -113,7 +113,7 @@ void aran_gpu_solver3d_destroy(AranGpuSolver3d *s) {
   s->mult64.release(); s->loc64.release(); s->mult32.release(); s->loc32.release();
   s->scan_tmp.release(); s->stats_dev.release(); s->err_dev.release();
   t.leaf_be.release(); t.leaf_chi.release(); t.leaf_clo.release(); t.big_items.release();
-  t.parents.release();
+  t.parents.release(); t.big_rng.release();
   s->kk64.release();
   s->kk32.release();
   for (auto &ev : s->ev)

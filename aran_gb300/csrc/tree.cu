@@ -146,9 +146,41 @@ __device__ __forceinline__ int ncount(const int *begin, const int *end, int a) {
   return end[a] - begin[a];
 }
 
-// one warp per node of the level: lane j < 27 takes colleague j of the
-// parent and keeps those of its children that are non-empty and adjacent;
-// a warp prefix sum places them in (colleague, child) order
+// colleagues of the nodes of one level, the non-empty adjacent children of
+// the parent's colleagues in (colleague, child) order.  Thread per node for
+// wide levels:
+__global__ void k_colleagues_thread(int cnt, int off, const int *__restrict__ begin,
+                                    const int *__restrict__ end, const int *__restrict__ child,
+                                    const int *__restrict__ parent, const int *__restrict__ ijk,
+                                    int *__restrict__ col, int *__restrict__ ncol) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  int c = off + i;
+  int k = 0;
+  if (ncount(begin, end, c) > 0) {
+    int p = parent[c];
+    if (p < 0) {
+      col[27 * c] = c;
+      k = 1;
+    } else {
+      int np = ncol[p];
+      for (int j = 0; j < np; ++j) {
+        int q = col[27 * p + j];
+        int c0 = child[q];
+        if (c0 < 0) continue;
+        for (int o = 0; o < 8; ++o) {
+          int s = c0 + o;
+          if (ncount(begin, end, s) > 0 && adjacent(ijk, c, s) && k < 27) col[27 * c + k++] = s;
+        }
+      }
+    }
+  }
+  ncol[c] = k;
+}
+
+// and one warp per node for narrow levels (shorter dependent chains): lane
+// j < 27 takes colleague j of the parent and keeps those of its children
+// that are non-empty and adjacent; a warp prefix sum places them in order
 __global__ void k_colleagues(int cnt, int off, const int *__restrict__ begin,
                              const int *__restrict__ end, const int *__restrict__ child,
                              const int *__restrict__ parent, const int *__restrict__ ijk,
@@ -287,17 +319,29 @@ __global__ void k_near(int nleaves, const int *__restrict__ leaf_node, const int
                        const uint8_t *__restrict__ depth, int T, int *__restrict__ near_cnt,
                        const int *__restrict__ near_off, int *__restrict__ near_rng,
                        int *__restrict__ semi_cnt, const int *__restrict__ semi_off,
-                       int *__restrict__ semi_node, int *__restrict__ semi_leaf, int mode) {
+                       int *__restrict__ semi_node, int *__restrict__ semi_leaf,
+                       int *__restrict__ big, int mode) {
   int L = blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= nleaves) return;
   int node = leaf_node[L];
   int k = 0, ks = 0;
   int w = mode ? near_off[L] : 0;
   int ws = (mode && T > 0) ? semi_off[L] : 0;
+  // a range is every leaf under node q, so it holds end[q] - begin[q]
+  // points; ranges above kBigRange are listed for the chunked P2P pass:
+  // big[0] = chunk total, big[1] = heavy ranges, then per heavy range its
+  // index and the offset of its first chunk
   auto emit = [&](int q) {
     if (mode) {
       near_rng[2 * (w + k)] = lf_begin[q];
       near_rng[2 * (w + k) + 1] = lf_end[q];
+      const int c = end[q] - begin[q];
+      if (c > kBigRange) {
+        const int coff = atomicAdd(&big[0], (c + kBigRange - 1) / kBigRange);
+        const int h = atomicAdd(&big[1], 1);
+        big[2 + 2 * h] = w + k;
+        big[3 + 2 * h] = coff;
+      }
     }
     ++k;
   };
@@ -558,8 +602,14 @@ void build_lists(AranGpuSolver3d *s) {
   t.ncol.reserve(nn);
   for (int d = 0; d < t.nlevels; ++d) {
     int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
-    k_colleagues<<<ceil_div(32 * (int64_t)cnt, TB), TB, 0, st>>>(cnt, off, t.begin.ptr, t.end.ptr, t.child.ptr,
-                                                    t.parent.ptr, t.ijk.ptr, t.col.ptr, t.ncol.ptr);
+    if (cnt >= 16384)
+      k_colleagues_thread<<<ceil_div(cnt, TB), TB, 0, st>>>(cnt, off, t.begin.ptr, t.end.ptr,
+                                                           t.child.ptr, t.parent.ptr, t.ijk.ptr,
+                                                           t.col.ptr, t.ncol.ptr);
+    else
+      k_colleagues<<<ceil_div(32 * (int64_t)cnt, TB), TB, 0, st>>>(cnt, off, t.begin.ptr, t.end.ptr,
+                                                                 t.child.ptr, t.parent.ptr, t.ijk.ptr,
+                                                                 t.col.ptr, t.ncol.ptr);
     s->launches++;
   }
   DBuf<int> &cntbuf = s->scan_tmp;
@@ -615,7 +665,7 @@ void build_lists(AranGpuSolver3d *s) {
                                                 t.child.ptr, t.parent.ptr, t.col.ptr, t.ncol.ptr,
                                                 t.lf_begin.ptr, t.lf_end.ptr, t.ijk.ptr, t.depth.ptr,
                                                 T, cntbuf.ptr, nullptr, nullptr, semi_cnt, nullptr,
-                                                nullptr, nullptr, 0);
+                                                nullptr, nullptr, nullptr, 0);
   s->launches++;
   ACHECK(cudaMemsetAsync(cntbuf.ptr + nleaves, 0, sizeof(int), st));
   exclusive_scan(s, cntbuf.ptr, t.near_off.ptr, nleaves + 1, st);
@@ -635,11 +685,15 @@ void build_lists(AranGpuSolver3d *s) {
     t.semi_node.reserve(nsemi + 1);
     t.semi_leaf.reserve(nsemi + 1);
   }
+  // heavy-range list (k_near's write pass fills it): at most one entry per range
+  t.big_rng.reserve(2 * (size_t)nrng + 2);
+  ACHECK(cudaMemsetAsync(t.big_rng.ptr, 0, 2 * sizeof(int), st));
   k_near<<<ceil_div(nleaves, TB), TB, 0, st>>>(nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
                                                 t.child.ptr, t.parent.ptr, t.col.ptr, t.ncol.ptr,
                                                 t.lf_begin.ptr, t.lf_end.ptr, t.ijk.ptr, t.depth.ptr,
                                                 T, nullptr, t.near_off.ptr, t.near_rng.ptr, nullptr,
-                                                t.semi_off.ptr, t.semi_node.ptr, t.semi_leaf.ptr, 1);
+                                                t.semi_off.ptr, t.semi_node.ptr, t.semi_leaf.ptr,
+                                                t.big_rng.ptr, 1);
   s->launches++;
   // internal nodes of depth >= 1: one M2L block each (their children)
   {
