@@ -32,6 +32,15 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+// 1/sqrt(x) on the MUFU unit with denormals flushed: without the flush the
+// FP32 rsqrt carries a denormal rescaling path; the near-field distances
+// here are at least 1e-10 squared box units, far from denormal
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __global__ void k_leaf_info(int nleaves, const int *__restrict__ leaf_node,
                             const int *__restrict__ begin, const int *__restrict__ end,
                             const uint8_t *__restrict__ depth, const double *__restrict__ center,
@@ -167,7 +176,7 @@ __global__ void __launch_bounds__(128, 10) k_p2p(
             }
           }
           const bool ok = FIELD ? (r2 > 1e-10f) : (r2 > 0.f);
-          const float inv = ok ? rsqrtf(r2) : 0.f;
+          const float inv = ok ? rsqrt_ftz(r2) : 0.f;
           const float qi = sj.q * inv;
           p0 += qi;
           if (FIELD) {
@@ -305,7 +314,7 @@ __global__ void __launch_bounds__(128, 8) k_p2p_warp(
       const float dx = q.x - sv.x, dy = q.y - sv.y, dz = q.z - sv.z;
       const float r2 = dx * dx + dy * dy + dz * dz;
       rmin = fminf(rmin, r2);
-      const float inv = rsqrtf(fmaxf(r2, thr2));
+      const float inv = rsqrt_ftz(fmaxf(r2, thr2));
       const float qi = sv.w * inv;
       p[0] += qi;
       if (FIELD) {
@@ -323,7 +332,7 @@ __global__ void __launch_bounds__(128, 8) k_p2p_warp(
       const float r2 = dx * dx + dy * dy + dz * dz;
       if (!(r2 < thr2)) return;
       {
-        const float inv = rsqrtf(fmaxf(r2, thr2));
+        const float inv = rsqrt_ftz(fmaxf(r2, thr2));
         const float qi = sv.w * inv;
         p[0] -= qi;
         if (FIELD) {
@@ -338,7 +347,7 @@ __global__ void __launch_bounds__(128, 8) k_p2p_warp(
                   ez = (float)(sz[t] - sz[j]);
       const float e2 = ex * ex + ey * ey + ez * ez;
       if (!(FIELD ? (e2 > 1e-10f) : (e2 > 0.f))) return;
-      const float inv = rsqrtf(e2);
+      const float inv = rsqrt_ftz(e2);
       const float qi = sv.w * inv;
       p[0] += qi;
       if (FIELD) {
