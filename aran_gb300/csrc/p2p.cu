@@ -265,8 +265,8 @@ __global__ void __launch_bounds__(128, 10) k_p2p(
 // walks the leaf's near source leaves; for each it stages up to 32 source
 // points in shared memory, shifted to the target leaf's frame by the lane
 // that loads them, and every lane sums them against its own targets from
-// broadcast reads: lanes per target S = 4 (n <= 8), 2 (n <= 16), else 1
-// (32 targets per pass), so the per-leaf set-up (centres, Kahan adds of the
+// broadcast reads: lanes per target S = 32 / (n rounded up to a power of
+// two) for n <= 16, else 1 (32 targets per pass), so the per-leaf set-up (centres, Kahan adds of the
 // leaf partials) is paid once per lane per source leaf.  The pair loop has no
 // branch: the distance is clamped below at h/8, and a lane whose chunk held a
 // closer pair (or the point itself) takes the stand-ins back and adds those
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(128, 8) k_p2p_warp(
   const int2 tbe = be[L];
   const int b = tbe.x, nt = tbe.y - tbe.x;
   // lanes per target as a compile-time constant: one body per S
-  const int Sd = nt <= 8 ? 4 : (nt <= 16 ? 2 : 1);
+  const int Sd = nt <= 1 ? 32 : (nt <= 2 ? 16 : (nt <= 4 ? 8 : (nt <= 8 ? 4 : (nt <= 16 ? 2 : 1))));
   auto body = [&](auto sc) {
   constexpr int S = decltype(sc)::value;
   const int sub = lane & (S - 1);
@@ -404,7 +404,10 @@ __global__ void __launch_bounds__(128, 8) k_p2p_warp(
     }
   }
   };
-  if (Sd == 4) body(std::integral_constant<int, 4>{});
+  if (Sd == 32) body(std::integral_constant<int, 32>{});
+  else if (Sd == 16) body(std::integral_constant<int, 16>{});
+  else if (Sd == 8) body(std::integral_constant<int, 8>{});
+  else if (Sd == 4) body(std::integral_constant<int, 4>{});
   else if (Sd == 2) body(std::integral_constant<int, 2>{});
   else body(std::integral_constant<int, 1>{});
 }

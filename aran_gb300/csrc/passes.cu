@@ -300,16 +300,19 @@ __global__ void k_l2p(int nleaves, const int *__restrict__ leaf_node, const int 
   if (FIELD) {
     for (int c = lane; c < nm; c += 32) {
       // c = tri(l', m): A = L(l'+1, m) * gz
-      int lp = 0;
+      // degree of the triangular index c: floor((sqrt(8c+1)-1)/2), corrected
+      int lp = (int)((sqrtf(8.f * c + 1.f) - 1.f) * 0.5f);
       while (tri(lp + 1) <= c) ++lp;
+      while (tri(lp) > c) --lp;
       int m = c - tri(lp);
       cplx<T> v = Lc[tri(lp + 1, m)];
       T g = gz_g[c];
       A[c] = cmake<T>(v.re * g, v.im * g);
     }
     for (int c = lane; c < p * p; c += 32) {
-      int lp = 0;
+      int lp = (int)sqrtf((float)c);   // floor(sqrt(c)), corrected
       while ((lp + 1) * (lp + 1) <= c) ++lp;
+      while (lp * lp > c) --lp;
       int mp = c - lp * lp - lp;
       int m = mp + 1;
       cplx<T> v;
