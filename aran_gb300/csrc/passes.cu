@@ -104,6 +104,117 @@ __global__ void k_p2m(int nleaves, const int *__restrict__ leaf_node, const int 
   for (int c = lane; c < nm; c += 32) mult[(size_t)node * nm + c] = out[c];
 }
 
+// The same P2M at a compile-time order (FP32) with the sum over a leaf's
+// particles done by butterflies: the terms of each particle (lane) are made
+// in m-major order (the recurrence's natural order) into a 32-value buffer;
+// each full buffer is summed over the warp by one butterfly of 31 shuffles
+// (afterwards lane k holds value k of the batch) instead of a 5-shuffle tree
+// per value, and the lanes' batch sums add up over the leaf's chunks.
+template <int P>
+__global__ void __launch_bounds__(128) k_p2m_bfly(int nleaves, const int *__restrict__ leaf_node,
+                                               const int *__restrict__ begin,
+                                               const int *__restrict__ end,
+                                               const uint8_t *__restrict__ depth,
+                                               const real4<float> *__restrict__ rel,
+                                               const float *__restrict__ rec_g,
+                                               const float *__restrict__ p2mf_g, double scale_e,
+                                               float *__restrict__ mult) {
+  constexpr int NM = P * (P + 1) / 2, NV = 2 * NM, NB = (NV + 31) / 32;
+  __shared__ float rec[(P + 1) * (P + 2)];
+  __shared__ float p2mf[P + 1];
+  for (int i = threadIdx.x; i < (P + 1) * (P + 2); i += blockDim.x) rec[i] = rec_g[i];
+  for (int i = threadIdx.x; i <= P; i += blockDim.x) p2mf[i] = p2mf_g[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int L = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (L >= nleaves) return;
+  const int node = leaf_node[L];
+  const int b = begin[node], e = end[node];
+  const float ih = inv_scale<float>(depth[node], scale_e);
+  float acc[NB];
+#pragma unroll
+  for (int k = 0; k < NB; ++k) acc[k] = 0.f;
+  for (int base = b; base < e; base += 32) {
+    const int i = base + lane;
+    float x = 0.f, y = 0.f, z = 0.f, q = 0.f;
+    if (i < e) {
+      const real4<float> r = rel[i];
+      x = r.x * ih;
+      y = r.y * ih;
+      z = r.z * ih;
+      q = r.q;
+    }
+    const float r2 = x * x + y * y + z * z;
+    float u[32];
+    float dre = rec[0], dim = 0.f;
+#pragma unroll
+    for (int m = 0; m < P; ++m) {
+      if (m > 0) {
+        const float a = rec[2 * tri(m, m)];
+        const float nre = a * (x * dre - y * dim), nim = a * (x * dim + y * dre);
+        dre = nre;
+        dim = nim;
+      }
+      float s1re = dre, s1im = dim, s2re = 0.f, s2im = 0.f;
+#pragma unroll
+      for (int l = m; l < P; ++l) {
+        float sre = dre, sim = dim;
+        if (l > m) {
+          const float c0 = rec[2 * tri(l, m)], c1 = rec[2 * tri(l, m) + 1];
+          sre = c0 * z * s1re - c1 * r2 * s2re;
+          sim = c0 * z * s1im - c1 * r2 * s2im;
+          s2re = s1re;
+          s2im = s1im;
+          s1re = sre;
+          s1im = sim;
+        }
+        const float f = q * p2mf[l];
+        // value index 2 slot + part, slot the m-major place of (l, m)
+        const int kr = 2 * (m * P - m * (m - 1) / 2 + (l - m));
+#pragma unroll
+        for (int part = 0; part < 2; ++part) {
+          const int k = kr + part;
+          u[k & 31] = part ? -f * sim : f * sre;
+          if ((k & 31) == 31 || k == NV - 1) {
+            if (k == NV - 1)            // last, partial batch: zero its tail
+#pragma unroll
+              for (int t = 0; t < 32; ++t)
+                if (t > (k & 31)) u[t] = 0.f;
+            // butterfly: the lane keeps the half whose index bit o matches
+            // its lane bit and adds the partner's half; lane j ends with
+            // value j of the batch summed over the warp
+#pragma unroll
+            for (int st = 0; st < 5; ++st) {
+              const int o = 16 >> st, n = 32 >> st;
+              const bool upper = (lane & o) != 0;
+#pragma unroll
+              for (int t = 0; t < n / 2; ++t) {
+                const float send = upper ? u[t] : u[t + n / 2];
+                const float keep = upper ? u[t + n / 2] : u[t];
+                u[t] = keep + __shfl_xor_sync(kFull, send, o);
+              }
+            }
+            acc[k >> 5] += u[0];
+          }
+        }
+      }
+    }
+  }
+  // lane k of batch bt holds m-major value 32 bt + k: slot (l, m), part
+#pragma unroll
+  for (int bt = 0; bt < NB; ++bt) {
+    const int kv = 32 * bt + lane;
+    if (kv >= NV) continue;
+    int slot = kv >> 1, m = 0;
+    while (slot > P - 1 - m) {
+      slot -= P - m;
+      ++m;
+    }
+    const int l = m + slot;
+    mult[(size_t)node * NV + 2 * tri(l, m) + (kv & 1)] = acc[bt];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // warp-cooperative pieces of the rotation operators
 // ---------------------------------------------------------------------------
@@ -463,11 +574,19 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   ACHECK(cudaEventRecord(s->ev[2 * Stage::P2M], st));
   {
     const int WPB = 4;
-    size_t sm = (2 * nl + p + 2) * sizeof(T) + (size_t)WPB * nm * sizeof(cplx<T>) + 64;
-    smem_opt_in(k_p2m<T>, sm);
-    k_p2m<T><<<ceil_div(t.nleaves, WPB), WPB * 32, sm, st>>>(
-        t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr, t.depth.ptr, rel, p, tb.rec.ptr,
-        tb.p2mf.ptr, s->scale_e, mult);
+    if (sizeof(T) == 4 && p == 12) {
+      k_p2m_bfly<12><<<ceil_div(t.nleaves, WPB), WPB * 32, 0, st>>>(
+          t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr, t.depth.ptr,
+          reinterpret_cast<const real4<float> *>(rel), reinterpret_cast<const float *>(tb.rec.ptr),
+          reinterpret_cast<const float *>(tb.p2mf.ptr), s->scale_e,
+          reinterpret_cast<float *>(mult));
+    } else {
+      size_t sm = (2 * nl + p + 2) * sizeof(T) + (size_t)WPB * nm * sizeof(cplx<T>) + 64;
+      smem_opt_in(k_p2m<T>, sm);
+      k_p2m<T><<<ceil_div(t.nleaves, WPB), WPB * 32, sm, st>>>(
+          t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr, t.depth.ptr, rel, p, tb.rec.ptr,
+          tb.p2mf.ptr, s->scale_e, mult);
+    }
     ACHECK(cudaGetLastError());
     s->launches++;
   }
