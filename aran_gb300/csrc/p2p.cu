@@ -427,7 +427,7 @@ void launch_one(AranGpuSolver3d *s, int grid, cudaStream_t st) {
 template <bool FIELD, bool MIXED>
 void launch_pair(AranGpuSolver3d *s, cudaStream_t st) {
   DevTree &t = s->tree;
-  if (MIXED) {
+  if constexpr (MIXED) {
     k_p2p_warp<FIELD><<<ceil_div(t.nleaves, 4), 128, 0, st>>>(
         t.nleaves, t.near_off.ptr, t.near_rng.ptr, t.leaf_be.ptr, t.leaf_chi.ptr, t.leaf_clo.ptr,
         s->sx.ptr, s->sy.ptr, s->sz.ptr, s->rel32.ptr, s->acc_pot.ptr, s->acc_fld.ptr);
