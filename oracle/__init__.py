@@ -1,6 +1,6 @@
 """CPU oracle for the LibAran 3D/2D FMM hot path -- TEST INFRASTRUCTURE ONLY.
 
-This package is the checker for the GPU path.  Only the test suite,
+The GPU path is tested against this package.  Only the test suite,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` load it;
 the product library never imports, links or calls anything here.
 

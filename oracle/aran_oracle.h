@@ -1,7 +1,7 @@
 /*
  * aran_oracle.h -- CPU restatement of LibAran's 3D (and 2D) FMM hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU path:
+ * TEST INFRASTRUCTURE ONLY.  The GPU path is tested against this library:
  * only the parity tests, the smoke check and the CPU-baseline leg of the
  * benchmark load it.  It is never linked into, called by, or shipped with the
  * GPU product library.
