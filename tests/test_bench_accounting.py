@@ -1,0 +1,27 @@
+"""The benchmark's roofline accounting (CPU only): the flop count of one M2L
+equals the multiply-adds of the operator the GPU applies, counted term by
+term as the lane kernel walks them (z-phases, forward rotation, translation
+along z, backward rotation, conjugate z-phases)."""
+import bench
+
+
+def enumerate_macs(p):
+    macs = 0
+    nm, nl = p * (p + 1) // 2, (p + 1) * (p + 2) // 2
+    macs += 4 * nm                      # z-phase of the source (complex product)
+    for part in range(2):               # real and imaginary parts
+        for l in range(p):              # forward rotation, degrees < p
+            macs += (l + 1) ** 2
+        for m in range(p + 1):          # translation along z, m-major slots
+            for j in range(m, p + 1):
+                macs += p - m
+        for l in range(p + 1):          # backward rotation, degrees <= p
+            macs += (l + 1) ** 2
+    macs += 4 * nl                      # conjugate z-phase of the local
+    return macs
+
+
+def test_m2l_flops_match_enumerated_terms():
+    for p in (4, 8, 12, 16, 20):
+        assert bench.m2l_flops(p) == 2 * enumerate_macs(p), p
+    assert bench.m2l_flops(12) == 10140
