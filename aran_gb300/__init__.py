@@ -102,6 +102,8 @@ def load(build_if_missing: bool = True):
     L.aran_gpu_solver3d_timings.restype = C.c_int
     L.aran_gpu_solver3d_launches.argtypes = [vp]
     L.aran_gpu_solver3d_launches.restype = C.c_int64
+    L.aran_gpu_solver3d_set_fp64_root_depth.argtypes = [vp, C.c_int]
+    L.aran_gpu_solver3d_set_fp64_root_depth.restype = C.c_int
     L.aran_gpu_p2p_direct_noalloc.argtypes = [C.c_int64, vp, vp, vp, vp]
     L.aran_gpu_p2p_direct_noalloc.restype = C.c_int
     L.aran_gpu_footprint_bytes.argtypes = [C.POINTER(Config3d), C.c_int64]
@@ -234,12 +236,14 @@ class Solver3d:
     family; ``field`` selects newtonfield3 (potential + field) over newtonpot3
     (potential only); ``precision`` is "fp64" (plain path) or "mixed";
     ``semifar_threshold`` > 0 turns on the semifar P2L/M2P interactions of
-    ``aran_solver3d_set_functions_full`` for nodes holding more points.
+    ``aran_solver3d_set_functions_full`` for nodes holding more points;
+    ``fp64_root_depth`` (mixed precision) keeps the expansions of depths
+    <= it in FP64 (-1: none; None: the library's default, 3 from order 16).
     """
 
     def __init__(self, lbound=(0.0, 0.0, 0.0), ubound=(1.0, 1.0, 1.0), *, maxbox=64, order=12,
                  flavour="rotate", field=True, precision="fp64", max_depth=21,
-                 semifar_threshold=0):
+                 semifar_threshold=0, fp64_root_depth=None):
         L = load()
         cfg = make_config(lbound, ubound, maxbox=maxbox, order=order, flavour=flavour,
                           field=field, precision=precision, max_depth=max_depth,
@@ -250,6 +254,8 @@ class Solver3d:
         h = C.c_void_p()
         _check(L.aran_gpu_solver3d_create(C.byref(cfg), C.byref(h)))
         self._h = h
+        if fp64_root_depth is not None:
+            _check(L.aran_gpu_solver3d_set_fp64_root_depth(h, int(fp64_root_depth)))
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -50,10 +50,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *mb, uint32_t parity) {
   return ok != 0;
 }
 
-// bounded wait: gives up after ~1M polls (each poll may itself suspend)
-__device__ __forceinline__ bool mbar_wait(uint64_t *mb, uint32_t parity) {
-  for (int i = 0; i < (1 << 20); ++i)
+constexpr int kWaitPolls = 1 << 20;
+
+// bounded wait: gives up after `polls` polls (each poll may itself suspend)
+__device__ __forceinline__ bool mbar_wait(uint64_t *mb, uint32_t parity, int polls = kWaitPolls) {
+  for (int i = 0; i < polls; ++i)
     if (mbar_try_wait(mb, parity)) return true;
+  return false;
+}
+
+// bounded wait that also gives up once the error word `flag` is non-zero
+// (another warp or CTA stopped: the phase it was to complete may never come)
+__device__ __forceinline__ bool mbar_wait_or_flag(uint64_t *mb, uint32_t parity, const int *flag,
+                                                  int polls = kWaitPolls) {
+  for (int i = 0; i < polls; ++i) {
+    if (mbar_try_wait(mb, parity)) return true;
+    if ((i & 63) == 63 && *(const volatile int *)flag) return false;
+  }
   return false;
 }
 

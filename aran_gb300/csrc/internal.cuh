@@ -20,6 +20,15 @@ struct CudaError {
   std::string where;
 };
 
+// invalid input found on the device before any output was written
+struct InputError {
+  std::string msg;
+};
+
+// bits of the solver's device error word
+constexpr int kErrTimeout = 1;     // a bounded mbarrier wait gave up
+constexpr int kErrNonFinite = 2;   // NaN/Inf coordinate or charge
+
 // sets the thread's last error and returns the status code
 inline int fail(int code, const std::string &msg) {
   set_error(msg);
@@ -188,6 +197,9 @@ struct AranGpuSolver3d {
   double ms[16] = {};
   int64_t launches = 0;
   bool have_tree = false;
+  // mixed precision: nodes of depth <= root64_depth keep FP64 expansions
+  // (M2M into them, M2L and L2L at them in FP64); -1 = none
+  int root64_depth = -1;
 };
 
 namespace aran {
@@ -199,15 +211,17 @@ void count_far_lists(AranGpuSolver3d *s);
 void build_far_lists(AranGpuSolver3d *s);
 // tables.cu
 void build_tables(AranGpuSolver3d *s);
+void build_tables_fp64(AranGpuSolver3d *s);   // FP64 tables beside a mixed solver's FP32 ones
 // passes.cu
 void run_passes(AranGpuSolver3d *s);
 // kkylin.cu: stage 0 = M2M, 1 = M2L, 2 = L2L
 void build_kkylin_tables(AranGpuSolver3d *s);
 void kkylin_pass(AranGpuSolver3d *s, int stage);
-// m2l.cu
-void launch_m2l(AranGpuSolver3d *s, cudaStream_t st);
-bool launch_m2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, const cplx<float> *mult,
-                      cplx<float> *loc, cudaStream_t st);
+// m2l.cu: M2L into the children of parents[first, first + count), in FP64
+// (mult64/loc64) or FP32 (mult32/loc32)
+void launch_m2l(AranGpuSolver3d *s, bool fp64, int first, int count, cudaStream_t st);
+bool launch_m2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, const int *parents, int count,
+                      const cplx<float> *mult, cplx<float> *loc, cudaStream_t st);
 // p2p.cu
 constexpr int kBigRange = 2048;   // near ranges above this many particles are chunked
 void build_p2p_work(AranGpuSolver3d *s);
@@ -220,6 +234,11 @@ void launch_semifar_m2p(AranGpuSolver3d *s, cudaStream_t st);
 void copy_expansions(AranGpuSolver3d *s, double *mult, double *local);
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// poll limit of the M2L consumers' waits for a table copy: 2^20, or the
+// value of ARAN_DEBUG_WAIT_POLLS (a test sets it to 0 to make the wait give
+// up; copies already issued are still waited for with the full limit)
+int consumer_wait_polls();
 
 // lets a kernel use more than the default 48 KB of dynamic shared memory
 template <typename K>

@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
                   const T *__restrict__ dirs, M2LOffsets D,
                   const uint8_t *__restrict__ lm_g, double scale_e,
                   const cplx<T> *__restrict__ mult, cplx<T> *__restrict__ loc,
-                  int *__restrict__ err) {
+                  int *__restrict__ err, int polls) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int nm = tri(p), nl = tri(p + 1);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -166,17 +166,25 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
 
   if (w == kSibWarps) {
     // producer warp: stream the offset tables through the NST-slot ring
-    if (NST > 0 && lane == 0)
+    if (NST > 0 && lane == 0) {
+      int issued = 0;
       for (int i = 0; i < nact; ++i) {
         const int b = i % (NST > 0 ? NST : 1);
-        if (i >= NST && !mbar_wait(&empty[b], ((i / (NST > 0 ? NST : 1)) - 1) & 1)) {
-          atomicExch(err, 1);
+        if (i >= NST && !mbar_wait_or_flag(&empty[b], ((i / (NST > 0 ? NST : 1)) - 1) & 1, err)) {
+          atomicOr(err, kErrTimeout);
           break;
         }
         mbar_expect_tx(&full[b], tbytes);
         bulk_g2s(tab + (size_t)b * D.stride, dirs + (size_t)c_dir_codes[active[i]] * D.stride,
                  tbytes, &full[b]);
+        ++issued;
       }
+      // the last copy of every slot has landed before the CTA can leave
+      // (earlier ones were waited for by the consumers before the slot was
+      // refilled), also when the consumers stopped early
+      for (int i = issued > NST ? issued - NST : 0; i < issued; ++i)
+        mbar_wait(&full[i % (NST > 0 ? NST : 1)], (i / (NST > 0 ? NST : 1)) & 1);
+    }
     return;
   }
 
@@ -223,8 +231,8 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
 
   for (int i = 0; i < nact; ++i) {
     const int b = i % (NST > 0 ? NST : 1);
-    if (NST > 0 && !mbar_wait(&full[b], (i / (NST > 0 ? NST : 1)) & 1)) {
-      atomicExch(err, 1);
+    if (NST > 0 && !mbar_wait_or_flag(&full[b], (i / (NST > 0 ? NST : 1)) & 1, err, polls)) {
+      atomicOr(err, kErrTimeout);
       break;
     }
     if (i == next_i) {
@@ -343,6 +351,7 @@ __global__ void __launch_bounds__(32 * (kSibWarps + 1), sizeof(T) == 4 ? 3 : 2)
     __syncwarp();
     if (NST > 0 && lane == 0) mbar_arrive(&empty[b]);
   }
+  cp_async_wait_all();   // source copies still in flight after an early stop
   if (nact > 0) {
 #pragma unroll
     for (int g = 0; g < G; ++g) {
@@ -392,30 +401,29 @@ size_t m2l_smem(int p, int stride) {
 }
 
 template <typename T, int NST, int R, int G>
-bool try_launch(AranGpuSolver3d *s, OpTables<T> &tb, const M2LOffsets &D, const cplx<T> *mult,
-                cplx<T> *loc, cudaStream_t st, int dev_smem) {
+bool try_launch(AranGpuSolver3d *s, OpTables<T> &tb, const M2LOffsets &D, const int *parents,
+                int count, const cplx<T> *mult, cplx<T> *loc, cudaStream_t st, int dev_smem) {
   DevTree &t = s->tree;
   const int p = s->cfg.order;
   size_t sm = m2l_smem<T, NST, G>(p, D.stride);
   if ((int)sm > dev_smem) return false;
   ACHECK(cudaFuncSetAttribute(k_m2l_sibling<T, NST, R, G>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  k_m2l_sibling<T, NST, R, G><<<ceil_div(t.n_parents, G), 32 * (kSibWarps + 1), sm, st>>>(
-      t.n_parents, t.parents.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
+  k_m2l_sibling<T, NST, R, G><<<ceil_div(count, G), 32 * (kSibWarps + 1), sm, st>>>(
+      count, parents, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
       t.ijk.ptr, t.depth.ptr, p, tb.dir_m2l.ptr, D, tb.lm.ptr, s->scale_e, mult, loc,
-      s->err_dev.ptr);
+      s->err_dev.ptr, consumer_wait_polls());
   ACHECK(cudaGetLastError());
   s->launches++;
   return true;
 }
 
 template <typename T>
-void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const cplx<T> *mult, cplx<T> *loc,
-              cudaStream_t st) {
-  DevTree &t = s->tree;
-  if (t.n_parents == 0) return;
+void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const int *parents, int count,
+              const cplx<T> *mult, cplx<T> *loc, cudaStream_t st) {
+  if (count <= 0) return;
   if constexpr (sizeof(T) == 4) {
-    if (launch_m2l_lanes(s, tb, mult, loc, st)) return;
+    if (launch_m2l_lanes(s, tb, parents, count, mult, loc, st)) return;
   }
   upload_codes(s->device);
   const int p = s->cfg.order;
@@ -434,32 +442,35 @@ void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const cplx<T> *mult, cplx<T> 
   // (two table slots keep a p <= 12 FP32 CTA under a third of the shared
   // memory, so three CTAs share an SM)
   if (nl <= 96) {
-    if (sizeof(T) == 8 && try_launch<T, 3, 3, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 2, 3, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 1, 3, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 1, 3, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (sizeof(T) == 8 && try_launch<T, 3, 3, 2>(s, tb, D, parents, count, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 2, 3, 2>(s, tb, D, parents, count, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 3, 2>(s, tb, D, parents, count, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 3, 1>(s, tb, D, parents, count, mult, loc, st, dev_smem)) return;
   } else if (nl <= 160) {
-    if (try_launch<T, 1, 5, 2>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 1, 5, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 5, 2>(s, tb, D, parents, count, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 5, 1>(s, tb, D, parents, count, mult, loc, st, dev_smem)) return;
   } else if (nl <= 256) {
-    if (try_launch<T, 3, 8, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 1, 8, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 0, 8, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 3, 8, 1>(s, tb, D, parents, count, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, 8, 1>(s, tb, D, parents, count, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 0, 8, 1>(s, tb, D, parents, count, mult, loc, st, dev_smem)) return;
   } else {
-    if (try_launch<T, 1, kMaxRounds, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
-    if (try_launch<T, 0, kMaxRounds, 1>(s, tb, D, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 1, kMaxRounds, 1>(s, tb, D, parents, count, mult, loc, st, dev_smem)) return;
+    if (try_launch<T, 0, kMaxRounds, 1>(s, tb, D, parents, count, mult, loc, st, dev_smem)) return;
   }
   throw CudaError{cudaErrorInvalidConfiguration, "M2L shared memory exceeds the device limit"};
 }
 
 }  // namespace
 
-void launch_m2l(AranGpuSolver3d *s, cudaStream_t st) {
-  if (s->cfg.precision == ARAN_PRECISION_MIXED)
-    launch_t<float>(s, s->t32, reinterpret_cast<const cplx<float> *>(s->mult32.ptr),
+void launch_m2l(AranGpuSolver3d *s, bool fp64, int first, int count, cudaStream_t st) {
+  const int *parents = s->tree.parents.ptr + first;
+  if (!fp64)
+    launch_t<float>(s, s->t32, parents, count,
+                    reinterpret_cast<const cplx<float> *>(s->mult32.ptr),
                     reinterpret_cast<cplx<float> *>(s->loc32.ptr), st);
   else
-    launch_t<double>(s, s->t64, reinterpret_cast<const cplx<double> *>(s->mult64.ptr),
+    launch_t<double>(s, s->t64, parents, count,
+                     reinterpret_cast<const cplx<double> *>(s->mult64.ptr),
                      reinterpret_cast<cplx<double> *>(s->loc64.ptr), st);
 }
 

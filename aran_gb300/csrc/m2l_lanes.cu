@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
                 const int *__restrict__ ijk, const uint8_t *__restrict__ depth,
                 const float *__restrict__ dirs, double scale_e,
                 const cplx<float> *__restrict__ mult, cplx<float> *__restrict__ loc,
-                int *__restrict__ err) {
+                int *__restrict__ err, int polls) {
   using D = LaneDims<P>;
   constexpr int NM = D::NM, NL = D::NL, NMP = D::NMP, STRIDE = D::STRIDE;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -245,16 +245,16 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
   int it = 0;
   for (; it < nact; ++it) {
     const int b = it % kLaneNst;
-    const bool ok = __all_sync(kFull, mbar_wait(&full[b], (it / kLaneNst) & 1));
+    const bool ok = __all_sync(kFull, mbar_wait_or_flag(&full[b], (it / kLaneNst) & 1, err, polls));
     if (!ok) {
-      if (lane == 0) atomicExch(err, 1);
+      if (lane == 0) atomicOr(err, kErrTimeout);
       break;
     }
     if (it == next_i) {
       const float *tb = tab + (size_t)b * STRIDE;
       const float2 *ph2 = reinterpret_cast<const float2 *>(tb);    // (cos, sin) of m phi
       if (!__all_sync(kFull, mbar_wait(&sbar[w], sph))) {
-        if (lane == 0) atomicExch(err, 1);
+        if (lane == 0) atomicOr(err, kErrTimeout);
         break;
       }
       sph ^= 1u;
@@ -402,8 +402,8 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
     if (lane == 0) {
       mbar_arrive(&empty[b]);
       if (w == 0 && it + kLaneNst < nact) {
-        if (!mbar_wait(&empty[b], (it / kLaneNst) & 1)) {
-          atomicExch(err, 1);
+        if (!mbar_wait_or_flag(&empty[b], (it / kLaneNst) & 1, err)) {
+          atomicOr(err, kErrTimeout);
         } else {
           issue(it + kLaneNst);
           ++issued;
@@ -429,8 +429,8 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
 }
 
 template <int P>
-bool launch_p(AranGpuSolver3d *s, OpTables<float> &tb, const cplx<float> *mult,
-              cplx<float> *loc, cudaStream_t st) {
+bool launch_p(AranGpuSolver3d *s, OpTables<float> &tb, const int *parents, int count,
+              const cplx<float> *mult, cplx<float> *loc, cudaStream_t st) {
   DevTree &t = s->tree;
   const size_t sm = lanes_smem<P>();
   int dev_smem = 0;
@@ -438,9 +438,10 @@ bool launch_p(AranGpuSolver3d *s, OpTables<float> &tb, const cplx<float> *mult,
   if ((int)sm > dev_smem) return false;
   ACHECK(cudaFuncSetAttribute(k_m2l_lanes<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)sm));
-  k_m2l_lanes<P><<<ceil_div(t.n_parents, kLanePar), 32 * kLaneWarps, sm, st>>>(
-      t.n_parents, t.parents.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
-      t.ijk.ptr, t.depth.ptr, tb.dir_lanes.ptr, s->scale_e, mult, loc, s->err_dev.ptr);
+  k_m2l_lanes<P><<<ceil_div(count, kLanePar), 32 * kLaneWarps, sm, st>>>(
+      count, parents, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
+      t.ijk.ptr, t.depth.ptr, tb.dir_lanes.ptr, s->scale_e, mult, loc, s->err_dev.ptr,
+      consumer_wait_polls());
   ACHECK(cudaGetLastError());
   s->launches++;
   return true;
@@ -450,15 +451,15 @@ bool launch_p(AranGpuSolver3d *s, OpTables<float> &tb, const cplx<float> *mult,
 
 // Runs the M2L pass with the lane-parallel kernel when the order has one
 // (and ARAN_M2L_KERNEL is not "sibling"); false leaves it to m2l.cu.
-bool launch_m2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, const cplx<float> *mult,
-                      cplx<float> *loc, cudaStream_t st) {
+bool launch_m2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, const int *parents, int count,
+                      const cplx<float> *mult, cplx<float> *loc, cudaStream_t st) {
   const int p = s->cfg.order;
-  if (!m2l_lane_order(p) || tb.dir_lanes.ptr == nullptr || s->tree.n_parents == 0) return false;
+  if (!m2l_lane_order(p) || tb.dir_lanes.ptr == nullptr || count <= 0) return false;
   const char *pick = getenv("ARAN_M2L_KERNEL");
   if (pick && strcmp(pick, "sibling") == 0) return false;
   switch (p) {
-    case 8: return launch_p<8>(s, tb, mult, loc, st);
-    case 12: return launch_p<12>(s, tb, mult, loc, st);
+    case 8: return launch_p<8>(s, tb, parents, count, mult, loc, st);
+    case 12: return launch_p<12>(s, tb, parents, count, mult, loc, st);
     default: return false;
   }
 }

@@ -12,19 +12,29 @@
 //
 // Properties a caller must know:
 //  * the scratch array (4 doubles per particle, kNoAllocMax particles, 4 MiB)
-//    is reserved on every GPU that loads the library and stays reserved until
-//    the process exits;
-//  * its device address is looked up with cudaGetSymbolAddress the first
-//    time the function runs on a device (with that device current); that
-//    first call should therefore come before any stream capture;
+//    belongs to the library's device code: it is placed on a GPU when that
+//    code is loaded there and stays until the process exits.  CUDA loads
+//    modules lazily by default (CUDA_MODULE_LOADING=LAZY since CUDA 12.2),
+//    so on each device the first call (or the first use of any other
+//    kernel of the library there) loads it, which takes device memory and
+//    can fail for lack of it.  Callers make one warm-up call per device at
+//    start-up, before the region where they may not allocate and before any
+//    stream capture (or run with CUDA_MODULE_LOADING=EAGER);
+//  * every call looks up the array's device address with
+//    cudaGetSymbolAddress, with the caller's device current: the host-side
+//    symbol is only a stand-in for it.  Once the module is loaded the lookup
+//    allocates nothing, and doing it per call stays right after a
+//    cudaDeviceReset or a new primary context;
+//  * the kernels run on the legacy default stream (stream 0) and the call
+//    synchronises that stream before returning: the caller finishes writing
+//    d_xyz and d_q (synchronises its own, e.g. non-blocking, streams) first,
+//    and no call can be made while a global-mode stream capture is open;
 //  * every call shares the array and the last call's contents remain in it;
 //    the function clears what it accumulates before using it, so calls that
 //    run one after the other are independent, but calls that overlap on the
 //    GPU (from several host threads, or several processes sharing a context)
 //    race on the array;
 //  * it allocates nothing: no cudaMalloc/cudaFree or allocating library call.
-#include <mutex>
-
 #include "internal.cuh"
 
 namespace aran {
@@ -35,9 +45,6 @@ constexpr int kNoAllocMax = 131072;  // particles
 constexpr int kNoAllocChunk = 4096;  // sources per block
 
 static __device__ __align__(256) double g_noalloc_acc[4 * kNoAllocMax];
-
-std::mutex g_noalloc_mu;
-double *g_noalloc_ptr[64] = {};
 
 __global__ void k_noalloc_clear(int n4, double *__restrict__ acc) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -58,8 +65,8 @@ __global__ void k_noalloc_pairs(int n, const double *__restrict__ xyz, const dou
     double dx = tx - xyz[3 * j], dy = ty - xyz[3 * j + 1], dz = tz - xyz[3 * j + 2];
     double r2 = dx * dx + dy * dy + dz * dz;
     // the solver's single-leaf rule: field mode keeps |r| > 1e-5, potential
-    // mode skips only the particle itself
-    bool ok = field ? (r2 > 1e-10) : (j != t);
+    // mode skips the particle itself and coincident particles (r == 0)
+    bool ok = field ? (r2 > 1e-10) : (r2 > 0.);
     double inv = ok ? rsqrt(r2) : 0.;
     double qi = q[j] * inv;
     pot += qi;
@@ -113,26 +120,14 @@ extern "C" int aran_gpu_p2p_direct_noalloc(int64_t n, const double *d_xyz, const
     set_error(std::string("aran_gpu_p2p_direct_noalloc: no current device: ") + cudaGetErrorString(e));
     return ARAN_ERR_NO_DEVICE;
   }
-  if (dev < 0 || dev >= 64) {
-    set_error("aran_gpu_p2p_direct_noalloc: device index out of range");
-    return ARAN_ERR_INVALID;
-  }
+  // the symbol is only a host-side stand-in: ask the runtime for the
+  // array's address on the current device
   double *acc = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-      // the symbol is only a host-side stand-in: ask the runtime for its
-      // device address on this (current) device
-      void *p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_acc);
-      if (e != cudaSuccess || !p) {
-        set_error(std::string("aran_gpu_p2p_direct_noalloc: cudaGetSymbolAddress failed: ") +
-                  cudaGetErrorString(e));
-        return ARAN_ERR_CUDA;
-      }
-      g_noalloc_ptr[dev] = static_cast<double *>(p);
-    }
-    acc = g_noalloc_ptr[dev];
+  e = cudaGetSymbolAddress(reinterpret_cast<void **>(&acc), g_noalloc_acc);
+  if (e != cudaSuccess || !acc) {
+    set_error(std::string("aran_gpu_p2p_direct_noalloc: cudaGetSymbolAddress failed: ") +
+              cudaGetErrorString(e));
+    return ARAN_ERR_CUDA;
   }
   const int nn = (int)n;
   const int TB = 128;

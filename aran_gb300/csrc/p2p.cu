@@ -196,7 +196,8 @@ __global__ void __launch_bounds__(128, 10) k_p2p(
         for (int j = sbe.x + j0; j < sbe.y; j += js) {
           const double dx = tx64 - sx[j], dy = ty64 - sy[j], dz = tz64 - sz[j];
           const double r2 = dx * dx + dy * dy + dz * dz;
-          const bool ok = FIELD ? (r2 > 1e-10) : (j != t);
+          // the point itself and coincident points: r2 == 0, skipped
+          const bool ok = FIELD ? (r2 > 1e-10) : (r2 > 0.);
           const double inv = ok ? rsqrt(r2) : 0.;
           const double qi = sq[j] * inv;
           pot += qi;

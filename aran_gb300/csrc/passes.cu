@@ -545,6 +545,70 @@ DirOffsets offsets(int p, int kind) {
   return d;
 }
 
+// M2M into the parents of depths dhi down to dlo (deepest first)
+template <typename T>
+void m2m_levels(AranGpuSolver3d *s, OpTables<T> &tb, cplx<T> *mult, int dhi, int dlo,
+                cudaStream_t st) {
+  DevTree &t = s->tree;
+  const int p = s->cfg.order;
+  const int nm = tri(p), nl = tri(p + 1);
+  DirOffsets D = offsets<T>(p, 1);
+  size_t sm = ((2 * nl + 15) & ~15) + (size_t)8 * 3 * nm * sizeof(cplx<T>) + 64;
+  smem_opt_in(k_m2m_rotate<T>, sm);
+  for (int d = dhi; d >= dlo; --d) {
+    if (d < 0 || d > t.nlevels - 2 || t.level_internal[d] == 0) continue;
+    int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
+    k_m2m_rotate<T><<<cnt, 256, sm, st>>>(cnt, off, t.child.ptr, t.begin.ptr, t.end.ptr, p,
+                                          tb.dir_m2m.ptr, D, tb.vm.ptr, tb.lm.ptr, mult);
+    ACHECK(cudaGetLastError());
+    s->launches++;
+  }
+}
+
+// L2L into the nodes of depths dlo up to dhi (from depth 3: locals of depths
+// 0-1 are zero, no far pairs above depth 2)
+template <typename T>
+void l2l_levels(AranGpuSolver3d *s, OpTables<T> &tb, cplx<T> *loc, int dlo, int dhi,
+                cudaStream_t st) {
+  DevTree &t = s->tree;
+  const int p = s->cfg.order;
+  const int nl = tri(p + 1);
+  DirOffsets D = offsets<T>(p, 2);
+  const int WPB = 4;
+  size_t sm = ((2 * nl + 15) & ~15) + (size_t)WPB * 2 * nl * sizeof(cplx<T>) + 64;
+  smem_opt_in(k_l2l_rotate<T>, sm);
+  for (int d = dlo < 3 ? 3 : dlo; d <= dhi && d < t.nlevels; ++d) {
+    int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
+    k_l2l_rotate<T><<<ceil_div(cnt, WPB), WPB * 32, sm, st>>>(
+        cnt, off, t.parent.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, p, tb.dir_l2l.ptr, D,
+        tb.vl.ptr, tb.lm.ptr, loc);
+    ACHECK(cudaGetLastError());
+    s->launches++;
+  }
+}
+
+// b[i] = (float) a[i] (WIDEN false) or b[i] (+)= (double) a[i] (WIDEN true)
+template <bool WIDEN, bool ADD>
+__global__ void k_convert(int64_t n, const void *__restrict__ a, void *__restrict__ b) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (WIDEN) {
+    double v = (double)static_cast<const float *>(a)[i];
+    double *o = static_cast<double *>(b);
+    o[i] = ADD ? o[i] + v : v;
+  } else {
+    static_cast<float *>(b)[i] = (float)static_cast<const double *>(a)[i];
+  }
+}
+
+template <bool WIDEN, bool ADD>
+void convert(AranGpuSolver3d *s, int64_t n, const void *a, void *b, cudaStream_t st) {
+  if (n <= 0) return;
+  k_convert<WIDEN, ADD><<<ceil_div(n, 256), 256, 0, st>>>(n, a, b);
+  ACHECK(cudaGetLastError());
+  s->launches++;
+}
+
 template <typename T>
 void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &locb,
                   const real4<T> *rel) {
@@ -553,12 +617,31 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   const int p = s->cfg.order;
   const int nm = tri(p), nl = tri(p + 1);
   const bool field = s->cfg.field != 0;
+  const bool kk = s->cfg.flavour == ARAN_FLAVOUR_KKYLIN;
   multb.reserve((size_t)t.nnodes * nm * 2);
   locb.reserve((size_t)t.nnodes * nl * 2);
   cplx<T> *mult = reinterpret_cast<cplx<T> *>(multb.ptr);
   cplx<T> *loc = reinterpret_cast<cplx<T> *>(locb.ptr);
   s->acc_pot.reserve(t.n);
   s->acc_fld.reserve(3 * t.n);
+  // FP64 root levels of the mixed rotation path: nodes of depth <= R keep
+  // FP64 expansions (the first n_root nodes, level-major order); M2M into
+  // them, M2L at them and L2L between them run in FP64
+  const int R = (sizeof(T) == 4 && !kk && s->root64_depth >= 0)
+                    ? (s->root64_depth < t.nlevels - 1 ? s->root64_depth : t.nlevels - 1)
+                    : -1;
+  const int n_root = R >= 0 ? t.level_off[R + 1] : 0;
+  const int n_root_src = R >= 0 ? t.level_off[R + 2 < t.nlevels ? R + 2 : t.nlevels] : 0;
+  int n_root_parents = 0;   // parents of depth < R: their children have depth <= R
+  for (int d = 1; d < R; ++d) n_root_parents += t.level_internal[d];
+  cplx<double> *mult64 = nullptr, *loc64 = nullptr;
+  if (R >= 0) {
+    build_tables_fp64(s);
+    s->mult64.reserve((size_t)n_root_src * nm * 2);
+    s->loc64.reserve((size_t)n_root * nl * 2);
+    mult64 = reinterpret_cast<cplx<double> *>(s->mult64.ptr);
+    loc64 = reinterpret_cast<cplx<double> *>(s->loc64.ptr);
+  }
 
   // near field on the second stream, as soon as the lists exist
   ACHECK(cudaStreamWaitEvent(s->s1, s->ev[2 * Stage::LISTS + 1], 0));
@@ -569,6 +652,7 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   // clear (aran/aransolver3d.c:399-410)
   ACHECK(cudaMemsetAsync(multb.ptr, 0, (size_t)t.nnodes * nm * 2 * sizeof(T), st));
   ACHECK(cudaMemsetAsync(locb.ptr, 0, (size_t)t.nnodes * nl * 2 * sizeof(T), st));
+  if (R >= 0) ACHECK(cudaMemsetAsync(s->loc64.ptr, 0, (size_t)n_root * nl * 2 * sizeof(double), st));
 
   // P2M
   ACHECK(cudaEventRecord(s->ev[2 * Stage::P2M], st));
@@ -593,45 +677,38 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
   ACHECK(cudaEventRecord(s->ev[2 * Stage::P2M + 1], st));
   // M2M, deepest level first
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2M], st));
-  const bool kk = s->cfg.flavour == ARAN_FLAVOUR_KKYLIN;
   if (kk) kkylin_pass(s, 0);
+  else if (R < 0) m2m_levels<T>(s, tb, mult, t.nlevels - 2, 0, st);
   else {
-    DirOffsets D = offsets<T>(p, 1);
-    size_t sm = ((2 * nl + 15) & ~15) + (size_t)8 * 3 * nm * sizeof(cplx<T>) + 64;
-    smem_opt_in(k_m2m_rotate<T>, sm);
-    for (int d = t.nlevels - 2; d >= 0; --d) {
-      if (t.level_internal[d] == 0) continue;
-      int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
-      k_m2m_rotate<T><<<cnt, 256, sm, st>>>(
-          cnt, off, t.child.ptr, t.begin.ptr, t.end.ptr, p, tb.dir_m2m.ptr, D, tb.vm.ptr,
-          tb.lm.ptr, mult);
-      ACHECK(cudaGetLastError());
-      s->launches++;
-    }
+    // FP32 up to the children of depth-R parents, widened, then FP64; the
+    // FP64 multipoles of depths <= R go back to FP32 for the semifar M2P
+    m2m_levels<T>(s, tb, mult, t.nlevels - 2, R + 1, st);
+    convert<true, false>(s, (int64_t)n_root_src * nm * 2, multb.ptr, s->mult64.ptr, st);
+    m2m_levels<double>(s, s->t64, mult64, R, 0, st);
+    convert<false, false>(s, (int64_t)n_root * nm * 2, s->mult64.ptr, multb.ptr, st);
   }
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2M + 1], st));
   // M2L over every node of depth >= 2
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L], st));
   if (kk) kkylin_pass(s, 1);
-  else launch_m2l(s, st);
+  else if (R < 0) launch_m2l(s, sizeof(T) == 8, 0, t.n_parents, st);
+  else {
+    launch_m2l(s, true, 0, n_root_parents, st);
+    launch_m2l(s, false, n_root_parents, t.n_parents - n_root_parents, st);
+  }
   launch_semifar_p2l(s, st);
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L + 1], st));
-  // L2L, from depth 3 (depth 0-1 locals are zero: no far pairs above depth 2)
+  // L2L
   ACHECK(cudaEventRecord(s->ev[2 * Stage::L2L], st));
   if (kk) kkylin_pass(s, 2);
+  else if (R < 0) l2l_levels<T>(s, tb, loc, 3, t.nlevels - 1, st);
   else {
-    DirOffsets D = offsets<T>(p, 2);
-    const int WPB = 4;
-    size_t sm = ((2 * nl + 15) & ~15) + (size_t)WPB * 2 * nl * sizeof(cplx<T>) + 64;
-    smem_opt_in(k_l2l_rotate<T>, sm);
-    for (int d = 3; d < t.nlevels; ++d) {
-      int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
-      k_l2l_rotate<T><<<ceil_div(cnt, WPB), WPB * 32, sm, st>>>(
-          cnt, off, t.parent.ptr, t.child.ptr, t.begin.ptr, t.end.ptr, p, tb.dir_l2l.ptr, D,
-          tb.vl.ptr, tb.lm.ptr, loc);
-      ACHECK(cudaGetLastError());
-      s->launches++;
-    }
+    // the FP32 locals of depths <= R hold only semifar P2L terms: added to
+    // the FP64 ones, carried down in FP64, narrowed back for the deeper levels
+    convert<true, true>(s, (int64_t)n_root * nl * 2, locb.ptr, s->loc64.ptr, st);
+    l2l_levels<double>(s, s->t64, loc64, 3, R, st);
+    convert<false, false>(s, (int64_t)n_root * nl * 2, s->loc64.ptr, locb.ptr, st);
+    l2l_levels<T>(s, tb, loc, R + 1, t.nlevels - 1, st);
   }
   ACHECK(cudaEventRecord(s->ev[2 * Stage::L2L + 1], st));
   // L2P after the near field has written the accumulators

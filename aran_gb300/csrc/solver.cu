@@ -4,6 +4,7 @@
 // (aran/aransolver3d.c:1135-1202) plus the per-point insertion that precedes
 // it: every stage runs on the device, the host only sequences launches.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -15,9 +16,21 @@ static thread_local std::string g_last_error;
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 
+int consumer_wait_polls() {
+  const char *v = getenv("ARAN_DEBUG_WAIT_POLLS");
+  if (!v || !*v) return 1 << 20;
+  long k = strtol(v, nullptr, 10);
+  return k < 0 ? 0 : (k > (1 << 20) ? (1 << 20) : (int)k);
+}
+
 void scatter_outputs(AranGpuSolver3d *s, double *pot, double *fld);
 
 namespace {
+
+// mixed solvers of order >= kRootFp64Order start with FP64 expansions at
+// depths <= kRootFp64Depth (at most 584 nodes take FP64 M2L: depths 2-3)
+constexpr int kRootFp64Order = 16;
+constexpr int kRootFp64Depth = 3;
 
 int check_config(const AranGpuConfig3d *c) {
   if (!c) return fail(ARAN_ERR_INVALID, "config is NULL");
@@ -73,6 +86,11 @@ int aran_gpu_solver3d_create(const AranGpuConfig3d *cfg, AranGpuSolver3d **out) 
     if (s->scale_e < ext) s->scale_e *= 2;
     build_tables(s);
     if (cfg->flavour == ARAN_FLAVOUR_KKYLIN) build_kkylin_tables(s);
+    if (cfg->precision == ARAN_PRECISION_MIXED && cfg->order >= kRootFp64Order &&
+        cfg->flavour != ARAN_FLAVOUR_KKYLIN) {
+      s->root64_depth = kRootFp64Depth;
+      build_tables_fp64(s);
+    }
     s->err_dev.reserve(4);
     ACHECK(cudaMemset(s->err_dev.ptr, 0, sizeof(int)));
   } catch (const CudaError &ce) {
@@ -171,7 +189,8 @@ int aran_gpu_solver3d_solve(AranGpuSolver3d *s, int64_t n, const double *xyz, co
     {
       int derr = 0;
       ACHECK(cudaMemcpy(&derr, s->err_dev.ptr, sizeof(int), cudaMemcpyDeviceToHost));
-      if (derr) return fail(ARAN_ERR_TIMEOUT, "a bounded device-side wait gave up (M2L table copy)");
+      if (derr & kErrTimeout)
+        return fail(ARAN_ERR_TIMEOUT, "a bounded device-side wait gave up (M2L table copy)");
     }
     // stage times
     auto el = [&](int a0, int a1) {
@@ -193,6 +212,12 @@ int aran_gpu_solver3d_solve(AranGpuSolver3d *s, int64_t n, const double *xyz, co
     s->ms[11] = el(2 * Stage::D2H, 2 * Stage::D2H + 1);
   } catch (const CudaError &ce) {
     return from_cuda(ce);
+  } catch (const InputError &ie) {
+    // stopped after the key pass: drain the stream, no output was written
+    cudaStreamSynchronize(s->s0);
+    cudaStreamSynchronize(s->s1);
+    s->have_tree = false;
+    return fail(ARAN_ERR_INVALID, ie.msg);
   }
   return ARAN_OK;
 }
@@ -312,5 +337,20 @@ int aran_gpu_solver3d_timings(AranGpuSolver3d *s, double ms[16]) {
 }
 
 int64_t aran_gpu_solver3d_launches(AranGpuSolver3d *s) { return s ? s->launches : -1; }
+
+int aran_gpu_solver3d_set_fp64_root_depth(AranGpuSolver3d *s, int depth) {
+  if (!s) return fail(ARAN_ERR_INVALID, "solver is NULL");
+  if (s->cfg.precision != ARAN_PRECISION_MIXED)
+    return fail(ARAN_ERR_INVALID, "FP64 root levels apply to mixed-precision solvers");
+  if (depth < -1 || depth > kKeyBits) return fail(ARAN_ERR_INVALID, "depth must be in [-1, 21]");
+  try {
+    ACHECK(cudaSetDevice(s->device));
+    if (depth >= 0 && s->cfg.flavour != ARAN_FLAVOUR_KKYLIN) build_tables_fp64(s);
+  } catch (const CudaError &ce) {
+    return from_cuda(ce);
+  }
+  s->root64_depth = depth;
+  return ARAN_OK;
+}
 
 }  // extern "C"

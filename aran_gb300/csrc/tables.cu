@@ -335,4 +335,8 @@ void build_tables(AranGpuSolver3d *s) {
   else build_tables_t<double>(s, s->t64, s->s0);
 }
 
+void build_tables_fp64(AranGpuSolver3d *s) {
+  if (s->t64.p != s->cfg.order) build_tables_t<double>(s, s->t64, s->s0);
+}
+
 }  // namespace aran

@@ -24,14 +24,18 @@ namespace aran {
 
 namespace {
 
-__global__ void k_keys(int64_t n, const double *__restrict__ xyz, double lbx, double lby,
-                       double lbz, double scx, double scy, double scz,
-                       uint64_t *__restrict__ keys, int *__restrict__ idx) {
+// Morton keys of the particles; a non-finite coordinate or charge sets
+// kErrNonFinite in the error word (the solve then stops before any output)
+__global__ void k_keys(int64_t n, const double *__restrict__ xyz, const double *__restrict__ q,
+                       double lbx, double lby, double lbz, double scx, double scy, double scz,
+                       uint64_t *__restrict__ keys, int *__restrict__ idx, int *__restrict__ err) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  uint64_t qx = (uint64_t)quantise(xyz[3 * i], lbx, scx);
-  uint64_t qy = (uint64_t)quantise(xyz[3 * i + 1], lby, scy);
-  uint64_t qz = (uint64_t)quantise(xyz[3 * i + 2], lbz, scz);
+  const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+  if (!(isfinite(x) && isfinite(y) && isfinite(z) && isfinite(q[i]))) atomicOr(err, kErrNonFinite);
+  uint64_t qx = (uint64_t)quantise(x, lbx, scx);
+  uint64_t qy = (uint64_t)quantise(y, lby, scy);
+  uint64_t qz = (uint64_t)quantise(z, lbz, scz);
   keys[i] = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
   idx[i] = (int)i;
 }
@@ -482,8 +486,8 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
   s->keys_out.reserve(n);
   s->idx_in.reserve(n);
   s->perm.reserve(n);
-  k_keys<<<ceil_div(n, TB), TB, 0, st>>>(n, d_xyz, c.lb[0], c.lb[1], c.lb[2], sc[0], sc[1], sc[2],
-                                          s->keys_in.ptr, s->idx_in.ptr);
+  k_keys<<<ceil_div(n, TB), TB, 0, st>>>(n, d_xyz, d_q, c.lb[0], c.lb[1], c.lb[2], sc[0], sc[1],
+                                          sc[2], s->keys_in.ptr, s->idx_in.ptr, s->err_dev.ptr);
   s->launches++;
   size_t bytes = 0;
   ACHECK(cub::DeviceRadixSort::SortPairs(nullptr, bytes, s->keys_in.ptr, s->keys_out.ptr,
@@ -514,7 +518,7 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
   int off = 0, cnt = 1;
   DBuf<int> &flags = s->scan_tmp;
   int d = 0;
-  int hostbuf[2];
+  int hostbuf[3] = {0, 0, 0};
   while (cnt > 0) {
     t.level_off.push_back(off + cnt);
     flags.reserve(2 * (size_t)cnt + 2);
@@ -525,7 +529,9 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
     exclusive_scan(s, flags.ptr, pos, cnt, st);
     ACHECK(cudaMemcpyAsync(&hostbuf[0], pos + cnt - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     ACHECK(cudaMemcpyAsync(&hostbuf[1], flags.ptr + cnt - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (d == 0) ACHECK(cudaMemcpyAsync(&hostbuf[2], s->err_dev.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
     ACHECK(cudaStreamSynchronize(st));
+    if (hostbuf[2] & kErrNonFinite) throw InputError{"a particle coordinate or charge is NaN or infinite"};
     int ninternal = hostbuf[0] + hostbuf[1];
     t.level_internal.push_back(ninternal);
     int child_off = off + cnt;

@@ -115,15 +115,29 @@ int aran_gpu_solver3d_timings (AranGpuSolver3d *s, double ms[16]);
 /* Number of GPU kernel launches issued by the last solve. */
 int64_t aran_gpu_solver3d_launches (AranGpuSolver3d *s);
 
+/* Mixed precision only: nodes of depth <= depth keep FP64 expansions, so
+ * M2M into them and M2L and L2L at them run in FP64 (the coarse levels,
+ * whose translations span the widest range of powers of the distance at
+ * high order: aran/aransphericalseriesd-translate.c:609-676).  -1 turns it
+ * off.  A mixed solver starts with depth 3 when its order is >= 16 and -1
+ * below; the kkylin flavour ignores it.  No counterpart in the reference
+ * (all FP64 there).  ARAN_ERR_INVALID outside [-1, 21] or on an FP64 solver. */
+int aran_gpu_solver3d_set_fp64_root_depth (AranGpuSolver3d *s, int depth);
+
 /* Allocation-free Newton near field: every pair of n <= 131072 particles
  * (potential, and field when d_field is not NULL, with the same rules as the
  * solver's single-leaf P2P), FP64, device pointers, AoS xyz.  No counterpart
  * in the reference: it exists for callers that may not allocate device
- * memory during a call.  Its scratch is a static 4 MiB device array held on
- * every GPU that loads the library until exit; the first call on a device
- * looks up that array's address and should precede any stream capture; calls
- * share the array, so calls that overlap on the GPU race.  Returns
- * ARAN_ERR_INVALID for n outside [1, 131072]. */
+ * memory during a call (a host that owns all device memory, or a loop that
+ * must not meet cudaMalloc's implicit synchronisation).  Its scratch is a
+ * static 4 MiB device array of the library's device code, placed on a GPU
+ * when that code is loaded there (lazily, at the first call on the device,
+ * unless CUDA_MODULE_LOADING=EAGER) and kept until exit: make one warm-up
+ * call per device before the no-allocation region and before any stream
+ * capture.  The kernels run on, and the call synchronises, the legacy
+ * default stream: finish writing d_xyz and d_q first.  Calls share the
+ * array, so calls that overlap on the GPU race.  Returns ARAN_ERR_INVALID
+ * for n outside [1, 131072]. */
 int aran_gpu_p2p_direct_noalloc (int64_t n, const double *d_xyz,
                                  const double *d_q, double *d_pot,
                                  double *d_field);

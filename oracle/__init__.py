@@ -83,6 +83,8 @@ def lib():
         L.or_wigner.argtypes = [C.c_double] * 3 + [C.c_int, dp]
         L.or_solve.restype = C.c_int
         L.or_solve.argtypes = [C.c_void_p, dp, dp, dp, dp, i64p]
+        L.or_solve_threaded.restype = C.c_int
+        L.or_solve_threaded.argtypes = [C.c_void_p, dp, dp, dp, dp, i64p, C.c_int]
         L.or_tree_lists.restype = C.c_int
         L.or_tree_lists.argtypes = [C.c_void_p, dp, i64p, u64p, i32p, i32p, u8p,
                                     i64p, u64p, i64p, u64p, i32p]
@@ -216,9 +218,12 @@ def harmonics(l, theta, phi):
 
 # ------------------------------------------------------------------- solver
 def solve(xyz, q, *, order, maxbox, flavour="rotate", field=False,
-          lb=(0.0, 0.0, 0.0), ub=(1.0, 1.0, 1.0), max_depth=21, semifar_threshold=0):
+          lb=(0.0, 0.0, 0.0), ub=(1.0, 1.0, 1.0), max_depth=21, semifar_threshold=0,
+          nthreads=1):
     """Full CPU FMM solve; returns (potential or field, stats dict).
-    semifar_threshold > 0 turns on P2L/M2P for nodes holding more points."""
+    semifar_threshold > 0 turns on P2L/M2P for nodes holding more points;
+    nthreads != 1 spreads the per-node/per-leaf work over host threads (0:
+    all cores) with the same results."""
     xyz = np.ascontiguousarray(xyz, np.float64)
     q = np.ascontiguousarray(q, np.float64)
     n = len(q)
@@ -226,8 +231,12 @@ def solve(xyz, q, *, order, maxbox, flavour="rotate", field=False,
     pot = np.zeros(n)
     fld = np.zeros((n, 3))
     st = np.zeros(NSTATS, dtype=np.int64)
-    rc = lib().or_solve(C.byref(cfg), _dp(xyz), _dp(q), _dp(pot), _dp(fld),
-                        st.ctypes.data_as(C.POINTER(C.c_int64)))
+    stp = st.ctypes.data_as(C.POINTER(C.c_int64))
+    if nthreads == 1:
+        rc = lib().or_solve(C.byref(cfg), _dp(xyz), _dp(q), _dp(pot), _dp(fld), stp)
+    else:
+        rc = lib().or_solve_threaded(C.byref(cfg), _dp(xyz), _dp(q), _dp(pot), _dp(fld), stp,
+                                     int(nthreads))
     if rc != 0:
         raise RuntimeError("oracle solve failed")
     return (fld if field else pot), dict(zip(STAT_NAMES, st.tolist()))

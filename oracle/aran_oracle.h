@@ -94,6 +94,17 @@ typedef struct
 int or_solve (const OrSolveConfig *cfg, const double *xyz, const double *q,
               double *pot, double *field, int64_t stats[OR_NSTATS]);
 
+/* The same solve with the per-node and per-leaf work spread over nthreads
+ * host threads (<= 0: the host core count).  Every target (node local,
+ * particle) receives its terms in the order of the single-threaded solve;
+ * results agree to rounding (angle triples within 1e-9 share one cached
+ * rotation, built by whichever call asked first).  A near pair is evaluated
+ * from both of its leaves (the single-threaded solve updates both sides at
+ * once).  Semifar solves run single-threaded. */
+int or_solve_threaded (const OrSolveConfig *cfg, const double *xyz,
+                       const double *q, double *pot, double *field,
+                       int64_t stats[OR_NSTATS], int nthreads);
+
 /* Tree/list description for bit-exact parity with the device tree.
  * Node id = (1 << 3*depth) | morton_key(depth).  Returns counts; arrays may
  * be NULL to query sizes.  Far pairs are unordered (a<b by id), near pairs

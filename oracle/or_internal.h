@@ -44,5 +44,10 @@ void or_translate_series (int flavour, const OrSeries *src, const double xs[3],
 void or_to_local_series (int flavour, const OrSeries *src, const double xs[3],
                          OrSeries *dst, const double xd[3]);
 void or_wigner_cache_clear (void);
+/* several threads are about to share the rotation cache: cleared, entries
+ * built to at least degree lmax from now on (unshare: back to one thread) */
+void or_wigner_cache_share (int lmax);
+void or_wigner_cache_unshare (void);
+void or_series_init (void);
 
 #endif

@@ -67,6 +67,11 @@ static void tables_init (void)
   g_ready = 1;
 }
 
+void or_series_init (void)
+{
+  tables_init ();
+}
+
 double or_beta (int l)
 {
   tables_init ();

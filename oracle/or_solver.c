@@ -394,9 +394,14 @@ static void p2p_pair (SolveCtx *s, int i, int j)
   double r = sqrt (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
   if (!s->cfg->field)
     {
-      double inv_r = 1. / r;
-      s->acc[i] += inv_r * qj;
-      s->acc[j] += inv_r * qi;
+      /* coincident distinct points: the reference divides by zero
+       * (tests/newtonpot3.c:72); here, as on the GPU, the pair is skipped */
+      if (r > 0.)
+        {
+          double inv_r = 1. / r;
+          s->acc[i] += inv_r * qj;
+          s->acc[j] += inv_r * qi;
+        }
     }
   else if (r > 1.e-5)
     {
@@ -617,6 +622,368 @@ int or_solve (const OrSolveConfig *cfg, const double *xyz, const double *q,
   return 0;
 }
 
+/* ------------------------------------------------------- threaded solve */
+typedef struct
+{
+  void (*fn) (void *ctx, int i);
+  void *ctx;
+  int n, chunk;
+  int next;
+} ParFor;
+
+static void *par_worker (void *arg)
+{
+  ParFor *p = (ParFor *) arg;
+  for (;;)
+    {
+      int i0 = __atomic_fetch_add (&p->next, p->chunk, __ATOMIC_RELAXED), i;
+      if (i0 >= p->n)
+        break;
+      for (i = i0; i < p->n && i < i0 + p->chunk; i++)
+        p->fn (p->ctx, i);
+    }
+  return NULL;
+}
+
+/* fn (ctx, i) for i in [0, n), dynamically scheduled over nthreads threads */
+static void par_for (int n, int nthreads, int chunk, void (*fn) (void *, int), void *ctx)
+{
+  ParFor p = { fn, ctx, n, chunk > 0 ? chunk : 1, 0 };
+  pthread_t th[256];
+  int k, nt = nthreads < 256 ? nthreads : 256;
+  if (n <= 0)
+    return;
+  if (nt > (n + p.chunk - 1) / p.chunk)
+    nt = (n + p.chunk - 1) / p.chunk;
+  for (k = 1; k < nt; k++)
+    pthread_create (&th[k], NULL, par_worker, &p);
+  par_worker (&p);
+  for (k = 1; k < nt; k++)
+    pthread_join (th[k], NULL);
+}
+
+typedef struct
+{
+  SolveCtx *s;
+  int lvl_begin;
+  int *far_off, *far_src;     /* per target node: sources in traversal order */
+  int *near_off, *near_src;   /* per target leaf: source leaves in traversal order */
+  int64_t nfar, capfar, nnear, capnear;
+  int *farp, *nearp;          /* collected pairs (a, b) */
+} ThrCtx;
+
+static void push2 (int **arr, int64_t *n, int64_t *cap, int a, int b)
+{
+  if (*n == *cap)
+    {
+      *cap = *cap ? 2 * *cap : 4096;
+      *arr = (int *) realloc (*arr, (size_t) *cap * 2 * sizeof (int));
+    }
+  (*arr)[2 * *n] = a;
+  (*arr)[2 * *n + 1] = b;
+  (*n)++;
+}
+
+static void th_far (void *ctx, int a, int b)
+{
+  ThrCtx *c = (ThrCtx *) ctx;
+  push2 (&c->farp, &c->nfar, &c->capfar, a, b);
+  c->s->stats[4] += 2;
+}
+
+static void th_near (void *ctx, int a, int b)
+{
+  ThrCtx *c = (ThrCtx *) ctx;
+  const OrNode *A = &c->s->t->nodes[a], *B = &c->s->t->nodes[b];
+  push2 (&c->nearp, &c->nnear, &c->capnear, a, b);
+  c->s->stats[1] += a == b ? (int64_t) cnt (A) * (cnt (A) + 1) / 2
+    : (int64_t) cnt (A) * cnt (B);
+}
+
+/* per-target CSR of directed pairs: (a, b) gives b the source a and, unless
+ * a == b, a the source b; the order within a target is the pair order */
+static void csr_targets (int nn, const int *pairs, int64_t np, int **off_out, int **src_out)
+{
+  int *off = (int *) calloc ((size_t) nn + 1, sizeof (int));
+  int *fill = (int *) malloc ((size_t) nn * sizeof (int));
+  int *src;
+  int64_t k;
+  int i;
+  for (k = 0; k < np; k++)
+    {
+      off[pairs[2 * k + 1] + 1]++;
+      if (pairs[2 * k] != pairs[2 * k + 1])
+        off[pairs[2 * k] + 1]++;
+    }
+  for (i = 0; i < nn; i++)
+    off[i + 1] += off[i];
+  src = (int *) malloc ((size_t) (off[nn] + 1) * sizeof (int));
+  memcpy (fill, off, (size_t) nn * sizeof (int));
+  for (k = 0; k < np; k++)
+    {
+      int a = pairs[2 * k], b = pairs[2 * k + 1];
+      src[fill[b]++] = a;
+      if (a != b)
+        src[fill[a]++] = b;
+    }
+  free (fill);
+  *off_out = off;
+  *src_out = src;
+}
+
+static void th_p2m (void *ctx, int nb)
+{
+  SolveCtx *s = ((ThrCtx *) ctx)->s;
+  const OrNode *nd = &s->t->nodes[nb];
+  int i;
+  if (!nd->leaf)
+    return;
+  for (i = nd->begin; i < nd->end; i++)
+    {
+      int o = s->t->perm[i];
+      or_p2m_series (s->xyz + 3 * o, s->q[o], nd->center, &s->mult[nb]);
+    }
+}
+
+/* M2M into one parent: its children in child order, as up() adds them */
+static void th_m2m (void *ctx, int k)
+{
+  ThrCtx *c = (ThrCtx *) ctx;
+  SolveCtx *s = c->s;
+  int nb = c->lvl_begin + k, ch;
+  const OrNode *nd = &s->t->nodes[nb];
+  if (nd->leaf)
+    return;
+  for (ch = 0; ch < 8; ch++)
+    {
+      const OrNode *cn = &s->t->nodes[nd->child[ch]];
+      if (cnt (cn) != 0)
+        or_translate_series (s->cfg->flavour, &s->mult[nd->child[ch]], cn->center,
+                             &s->mult[nb], nd->center);
+    }
+}
+
+static void th_m2l (void *ctx, int nb)
+{
+  ThrCtx *c = (ThrCtx *) ctx;
+  SolveCtx *s = c->s;
+  const OrNode *B = &s->t->nodes[nb];
+  int k;
+  for (k = c->far_off[nb]; k < c->far_off[nb + 1]; k++)
+    {
+      int a = c->far_src[k];
+      or_to_local_series (s->cfg->flavour, &s->mult[a], s->t->nodes[a].center,
+                          &s->loc[nb], B->center);
+    }
+}
+
+/* target side of p2p_pair for every particle of one leaf */
+static void th_p2p (void *ctx, int nb)
+{
+  ThrCtx *c = (ThrCtx *) ctx;
+  SolveCtx *s = c->s;
+  const OrNode *T = &s->t->nodes[nb];
+  int i, k, j;
+  for (i = T->begin; i < T->end; i++)
+    {
+      const double *xi = s->xyz + 3 * s->t->perm[i];
+      for (k = c->near_off[nb]; k < c->near_off[nb + 1]; k++)
+        {
+          const OrNode *S = &s->t->nodes[c->near_src[k]];
+          for (j = S->begin; j < S->end; j++)
+            {
+              const double *xj;
+              double d[3], r, qj;
+              if (j == i)
+                continue;
+              xj = s->xyz + 3 * s->t->perm[j];
+              qj = s->q[s->t->perm[j]];
+              d[0] = xi[0] - xj[0];
+              d[1] = xi[1] - xj[1];
+              d[2] = xi[2] - xj[2];
+              r = sqrt (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+              if (!s->cfg->field)
+                {
+                  if (r > 0.)
+                    s->acc[i] += (1. / r) * qj;
+                }
+              else if (r > 1.e-5)
+                {
+                  double inv_r = 1. / r, inv_r3 = inv_r * inv_r * inv_r;
+                  s->fld[3 * i] += d[0] * (-inv_r3 * qj);
+                  s->fld[3 * i + 1] += d[1] * (-inv_r3 * qj);
+                  s->fld[3 * i + 2] += d[2] * (-inv_r3 * qj);
+                }
+            }
+        }
+    }
+}
+
+static void th_l2l (void *ctx, int k)
+{
+  ThrCtx *c = (ThrCtx *) ctx;
+  SolveCtx *s = c->s;
+  int nb = c->lvl_begin + k;
+  const OrNode *nd = &s->t->nodes[nb];
+  if (cnt (nd) != 0 && nd->father >= 0)
+    {
+      const OrNode *f = &s->t->nodes[nd->father];
+      or_translate_series (s->cfg->flavour, &s->loc[nd->father], f->center, &s->loc[nb],
+                           nd->center);
+    }
+}
+
+static void th_l2p (void *ctx, int nb)
+{
+  SolveCtx *s = ((ThrCtx *) ctx)->s;
+  const OrNode *nd = &s->t->nodes[nb];
+  int i;
+  if (!nd->leaf)
+    return;
+  for (i = nd->begin; i < nd->end; i++)
+    {
+      int o = s->t->perm[i];
+      const double *x = s->xyz + 3 * o;
+      double rel[3] = { x[0] - nd->center[0], x[1] - nd->center[1], x[2] - nd->center[2] };
+      if (s->cfg->field)
+        {
+          double g[3];
+          or_gradient_xyz (&s->loc[nb], rel, g);
+          s->fld[3 * i] += g[0];
+          s->fld[3 * i + 1] += g[1];
+          s->fld[3 * i + 2] += g[2];
+        }
+      else
+        {
+          double r, cost, sint, cosp, sinp;
+          or_to_spherical_internal (rel, &r, &cost, &sint, &cosp, &sinp);
+          s->acc[i] += creal (or_evaluate_internal (&s->loc[nb], r, cost, sint, cosp, sinp));
+        }
+    }
+}
+
+int or_solve_threaded (const OrSolveConfig *cfg, const double *xyz, const double *q,
+                       double *pot, double *field, int64_t stats[OR_NSTATS], int nthreads)
+{
+  OrTree t;
+  SolveCtx s;
+  ThrCtx c;
+  Traversal tv;
+  int i, d, p = cfg->order, nlev = 0;
+  int ms = or_series_size (0, p), ls = or_series_size (p, 0);
+  int *lvl;
+  double complex *mstore, *lstore;
+
+  if (nthreads <= 0)
+    nthreads = (int) sysconf (_SC_NPROCESSORS_ONLN);
+  if (nthreads <= 1 || cfg->semifar_threshold > 0)
+    return or_solve (cfg, xyz, q, pot, field, stats);
+  if (cfg->n <= 0 || p <= 0)
+    return -1;
+  tree_build (&t, cfg, xyz);
+  memset (stats, 0, OR_NSTATS * sizeof (int64_t));
+  memset (&c, 0, sizeof (c));
+  s.cfg = cfg;
+  s.t = &t;
+  s.xyz = xyz;
+  s.q = q;
+  s.stats = stats;
+  s.acc = (double *) calloc ((size_t) cfg->n, sizeof (double));
+  s.fld = (double *) calloc ((size_t) cfg->n * 3, sizeof (double));
+  s.mult = (OrSeries *) malloc (t.nn * sizeof (OrSeries));
+  s.loc = (OrSeries *) malloc (t.nn * sizeof (OrSeries));
+  mstore = (double complex *) calloc ((size_t) t.nn * ms, sizeof (double complex));
+  lstore = (double complex *) calloc ((size_t) t.nn * ls, sizeof (double complex));
+  for (i = 0; i < t.nn; i++)
+    {
+      s.mult[i].posdeg = 0;
+      s.mult[i].negdeg = p;
+      s.mult[i].c = mstore + (size_t) i * ms;
+      s.loc[i].posdeg = p;
+      s.loc[i].negdeg = 0;
+      s.loc[i].c = lstore + (size_t) i * ls;
+    }
+  c.s = &s;
+  /* level ranges: the tree is built level by level */
+  lvl = (int *) malloc ((size_t) (t.nn + 2) * sizeof (int));
+  lvl[0] = 0;
+  for (i = 0; i < t.nn; i++)
+    if (t.nodes[i].depth != nlev)
+      lvl[++nlev] = i;
+  lvl[++nlev] = t.nn;
+  /* shared read-only tables from here on */
+  or_series_init ();
+  or_wigner_cache_share (p + 1);
+
+  stats[0] = t.nn;
+  stats[2] = cfg->n;
+  stats[6] = cfg->n;
+  for (i = 0; i < t.nn; i++)
+    if (cnt (&t.nodes[i]) != 0 && t.nodes[i].father >= 0)
+      {
+        stats[3]++;
+        stats[5]++;
+      }
+  /* up: P2M at the leaves, then M2M level by level, deepest parents first */
+  par_for (t.nn, nthreads, 64, th_p2m, &c);
+  for (d = nlev - 2; d >= 0; d--)
+    {
+      c.lvl_begin = lvl[d];
+      par_for (lvl[d + 1] - lvl[d], nthreads, 8, th_m2m, &c);
+    }
+  /* near/far pairs in traversal order, then every target's sources */
+  tv.far = th_far;
+  tv.near = th_near;
+  tv.semifar = NULL;
+  tv.threshold = 0;
+  tv.ctx = &c;
+  tv.t = &t;
+  pair_traverse (&tv, 0, 0);
+  csr_targets (t.nn, c.farp, c.nfar, &c.far_off, &c.far_src);
+  csr_targets (t.nn, c.nearp, c.nnear, &c.near_off, &c.near_src);
+  par_for (t.nn, nthreads, 16, th_m2l, &c);
+  par_for (t.nn, nthreads, 16, th_p2p, &c);
+  /* down: L2L level by level, then L2P at the leaves */
+  for (d = 1; d < nlev; d++)
+    {
+      c.lvl_begin = lvl[d];
+      par_for (lvl[d + 1] - lvl[d], nthreads, 32, th_l2l, &c);
+    }
+  par_for (t.nn, nthreads, 64, th_l2p, &c);
+  or_wigner_cache_unshare ();
+
+  for (i = 0; i < cfg->n; i++)
+    {
+      int o = t.perm[i];
+      if (cfg->field)
+        {
+          if (field)
+            {
+              field[3 * o] = s.fld[3 * i];
+              field[3 * o + 1] = s.fld[3 * i + 1];
+              field[3 * o + 2] = s.fld[3 * i + 2];
+            }
+        }
+      else if (pot)
+        pot[o] = s.acc[i];
+    }
+  free (lvl);
+  free (c.farp);
+  free (c.nearp);
+  free (c.far_off);
+  free (c.far_src);
+  free (c.near_off);
+  free (c.near_src);
+  free (s.acc);
+  free (s.fld);
+  free (s.mult);
+  free (s.loc);
+  free (mstore);
+  free (lstore);
+  tree_free (&t);
+  return 0;
+}
+
 /* ----------------------------------------------------------- tree lists */
 typedef struct
 {
@@ -743,6 +1110,8 @@ static void *direct_worker (void *arg)
           d[1] = xi[1] - xk[1];
           d[2] = xi[2] - xk[2];
           r = sqrt (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+          if (r == 0.)
+            continue;           /* coincident distinct points: skipped */
           nsum (&ps, &pc, j->q[k] / r);
           if (r > 1.e-5)
             {

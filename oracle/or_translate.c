@@ -5,7 +5,9 @@
  */
 #include "or_internal.h"
 
+#include <pthread.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -177,9 +179,17 @@ static void wigner_require (OrWigner *aw, int lmax)
 static struct
 {
   int used;
+  int ready;          /* entry complete (published with release order) */
   int64_t k[3];
   OrWigner w;
 } g_wc[WCACHE];
+
+/* While several threads share the cache (or_wigner_cache_share), entries are
+ * built under g_wc_mu to at least degree g_wc_floor and never change or go
+ * away afterwards, so complete entries are read without the lock. */
+static pthread_mutex_t g_wc_mu = PTHREAD_MUTEX_INITIALIZER;
+static int g_wc_shared = 0;
+static int g_wc_floor = 0;
 
 void or_wigner_cache_clear (void)
 {
@@ -189,15 +199,39 @@ void or_wigner_cache_clear (void)
       {
         free (g_wc[i].w.t);
         g_wc[i].used = 0;
+        g_wc[i].ready = 0;
       }
 }
 
-static OrWigner *wigner_lookup (double a, double b, double g)
+void or_wigner_cache_share (int lmax)
 {
-  int64_t k[3] = { llround (a * 1e9), llround (b * 1e9), llround (g * 1e9) };
-  uint64_t h = (uint64_t) k[0] * 0x9E3779B97F4A7C15ull ^
+  or_wigner_cache_clear ();
+  g_wc_floor = lmax;
+  g_wc_shared = 1;
+}
+
+void or_wigner_cache_unshare (void)
+{
+  g_wc_shared = 0;
+  g_wc_floor = 0;
+}
+
+static void wc_key (double a, double b, double g, int64_t k[3], int *slot)
+{
+  uint64_t h;
+  k[0] = llround (a * 1e9);
+  k[1] = llround (b * 1e9);
+  k[2] = llround (g * 1e9);
+  h = (uint64_t) k[0] * 0x9E3779B97F4A7C15ull ^
     (uint64_t) k[1] * 0xC2B2AE3D27D4EB4Full ^ (uint64_t) k[2] * 0x165667B19E3779F9ull;
-  int i, slot = (int) (h % WCACHE);
+  *slot = (int) (h % WCACHE);
+}
+
+static int wigner_lookup (double a, double b, double g)
+{
+  int64_t k[3];
+  int i, slot;
+  wc_key (a, b, g, k, &slot);
   for (i = 0; i < WCACHE; i++)
     {
       int s = (slot + i) % WCACHE;
@@ -210,14 +244,52 @@ static OrWigner *wigner_lookup (double a, double b, double g)
           g_wc[s].w.gamma = g;
           g_wc[s].w.lmax = -1;
           g_wc[s].w.t = NULL;
-          return &g_wc[s].w;
+          return s;
         }
       if (memcmp (g_wc[s].k, k, sizeof (k)) == 0)
-        return &g_wc[s].w;
+        return s;
+    }
+  if (g_wc_shared)
+    {
+      fprintf (stderr, "oracle: Wigner cache full while shared\n");
+      abort ();
     }
   /* cache full: start over */
   or_wigner_cache_clear ();
   return wigner_lookup (a, b, g);
+}
+
+/* the rotation of angles (a, b, g) up to degree lmax: aran_wigner_repo_lookup
+ * + aran_wigner_require (aran/aranwignerrepo.c:57-82, aran/aranwigner.c:256-313) */
+static const OrWigner *wigner_get (double a, double b, double g, int lmax)
+{
+  int s;
+  if (g_wc_shared)
+    {
+      int64_t k[3];
+      int i, slot;
+      wc_key (a, b, g, k, &slot);
+      for (i = 0; i < WCACHE; i++)
+        {
+          int e = (slot + i) % WCACHE;
+          if (!__atomic_load_n (&g_wc[e].ready, __ATOMIC_ACQUIRE))
+            break;
+          if (memcmp (g_wc[e].k, k, sizeof (k)) == 0 && g_wc[e].w.lmax >= lmax)
+            return &g_wc[e].w;
+        }
+      pthread_mutex_lock (&g_wc_mu);
+    }
+  s = wigner_lookup (a, b, g);
+  if (g_wc_shared && g_wc[s].ready && g_wc[s].w.lmax < lmax)
+    {
+      fprintf (stderr, "oracle: shared Wigner entry below the requested degree\n");
+      abort ();
+    }
+  wigner_require (&g_wc[s].w, lmax > g_wc_floor ? lmax : g_wc_floor);
+  __atomic_store_n (&g_wc[s].ready, 1, __ATOMIC_RELEASE);
+  if (g_wc_shared)
+    pthread_mutex_unlock (&g_wc_mu);
+  return &g_wc[s].w;
 }
 
 void or_wigner (double alpha, double beta, double gamma, int lmax,
@@ -267,8 +339,7 @@ static void rotate_series (const OrSeries *src, double a, double b, double g,
 {
   int nd = imin (dst->negdeg, src->negdeg);
   int pd = imin (dst->posdeg, src->posdeg);
-  OrWigner *aw = wigner_lookup (a, b, g);
-  wigner_require (aw, imax (pd + 1, nd));
+  const OrWigner *aw = wigner_get (a, b, g, imax (pd + 1, nd));
   buffer_rotate (aw, src->posdeg, or_pos (src, 0, 0), or_pos (dst, 0, 0));
   if (src->negdeg > 0)
     buffer_rotate (aw, src->negdeg - 1, or_neg (src, 0, 0),
@@ -281,8 +352,7 @@ static void rotate_inverse_series (const OrSeries *src, double a, double b,
 {
   int nd = imin (dst->negdeg, src->negdeg);
   int pd = imin (dst->posdeg, src->posdeg);
-  OrWigner *aw = wigner_lookup (-g, -b, -a);
-  wigner_require (aw, imax (pd + 1, nd));
+  const OrWigner *aw = wigner_get (-g, -b, -a, imax (pd + 1, nd));
   buffer_rotate (aw, pd, or_pos (src, 0, 0), or_pos (dst, 0, 0));
   if (nd > 0)
     buffer_rotate (aw, nd - 1, or_neg (src, 0, 0), or_neg (dst, 0, 0));

@@ -1,0 +1,175 @@
+"""Mixed precision per order, FP64 root levels, and input/failure handling.
+
+* Accuracy of the headline workload's distribution (Plummer, a = 0.05, r <= 1,
+  box [-1,1]^3, q ~ U[0,1], leaf 64) at the three orders of the clustered
+  configuration, p = 8, 12, 16: mixed and FP64 results against the FP64
+  direct sum on a target subset.  At p = 12 the mixed potential must be
+  within 1e-6 (rel-L2), the accuracy the throughput metric is quoted at; p = 8
+  is truncation-limited (the FP64 path has the same error) and p = 16 is
+  limited by FP32 arithmetic.
+* FP64 root levels of the mixed path (aran_gpu_solver3d_set_fp64_root_depth):
+  every depth split gives the same operators, so results stay within the
+  mixed tolerance of the oracle, and moving all translations to FP64 brings
+  the mixed result closer to the FP64 one.
+* Coincident distinct particles: skipped by every P2P (FP64, mixed, oracle);
+  the reference's potential kernel divides by zero there.
+* NaN/Inf coordinates or charges: ARAN_ERR_INVALID before any output.
+* A bounded device wait that gives up (forced by ARAN_DEBUG_WAIT_POLLS=0, a
+  consumer poll limit of zero; the copies already issued are still waited
+  for): ARAN_ERR_TIMEOUT, and the solver keeps working.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from aran_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+MIXED_TOL = 3e-6
+FP64_TOL = 1e-12
+BOX = ((-1.0, -1.0, -1.0), (1.0, 1.0, 1.0))
+
+# rel-L2 bounds against the FP64 direct sum per order (potential, field),
+# Plummer 200k, leaf 64; measured on GB300 (mixed): p=8 1.4e-6 / 2.2e-5,
+# p=12 2.8e-7 / 7.0e-7, p=16 2.3e-7 / 2.8e-7
+ORDER_BOUNDS = {8: (3e-6, 4e-5), 12: (1e-6, 1.5e-6), 16: (5e-7, 5e-7)}
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def plummer200k(oracle):
+    x, q = W.plummer(200_000, 3)
+    tgt = np.random.default_rng(5).choice(len(q), 4000, replace=False)
+    rp, rf = oracle.direct(x, q, targets=tgt)
+    return x, q, tgt, rp, rf
+
+
+@pytest.mark.parametrize("p", [8, 12, 16])
+def test_plummer_orders_vs_direct_sum(aran, plummer200k, p):
+    x, q, tgt, rp, rf = plummer200k
+    out = {}
+    for prec in ("mixed", "fp64"):
+        with aran.Solver3d(*BOX, maxbox=64, order=p, field=True, precision=prec) as s:
+            out[prec] = s.solve(x, q)
+    bp, bf = ORDER_BOUNDS[p]
+    pot, fld = out["mixed"]
+    assert rel_l2(pot[tgt], rp) < bp
+    assert rel_l2(fld[tgt], rf) < bf
+    # the FP64 path is at least as accurate, and mixed stays near it
+    assert rel_l2(out["fp64"][0][tgt], rp) < bp
+    assert rel_l2(pot, out["fp64"][0]) < 5e-7
+    assert rel_l2(fld, out["fp64"][1]) < 5e-7
+
+
+@pytest.mark.parametrize("p,depths", [(16, (-1, 2, 3, 21)), (12, (3, 5)), (8, (4,))])
+def test_fp64_root_levels_match_oracle(aran, oracle, p, depths):
+    """Any split between FP64 root levels and FP32 below applies the same
+    operators: within the mixed tolerance of the oracle's FP64 solve.  With
+    every level in FP64 (depth 21) only P2M, L2P and P2P stay in FP32, and the
+    result moves closer to the FP64 GPU path than with no FP64 levels."""
+    x, q = W.plummer(30000, 17)
+    kw = dict(maxbox=32, order=p, field=True)
+    opot, _ = oracle.solve(x, q, order=p, maxbox=32, field=False, lb=BOX[0], ub=BOX[1])
+    ofld, _ = oracle.solve(x, q, order=p, maxbox=32, field=True, lb=BOX[0], ub=BOX[1])
+    with aran.Solver3d(*BOX, precision="fp64", **kw) as s:
+        pot64, fld64 = s.solve(x, q)
+    assert rel_l2(pot64, opot) < FP64_TOL
+    errs = {}
+    for d in depths:
+        with aran.Solver3d(*BOX, precision="mixed", fp64_root_depth=d, **kw) as s:
+            pot, fld = s.solve(x, q)
+        assert rel_l2(pot, opot) < MIXED_TOL, d
+        assert rel_l2(fld, ofld) < MIXED_TOL, d
+        errs[d] = rel_l2(pot, pot64)
+    if -1 in errs and 21 in errs:
+        assert errs[21] < errs[-1]
+
+
+def test_fp64_root_depth_argument_checks(aran):
+    with aran.Solver3d(*BOX, maxbox=32, order=8, precision="fp64") as s:
+        with pytest.raises(aran.AranError) as ei:
+            aran._check(aran.load().aran_gpu_solver3d_set_fp64_root_depth(s._h, 3))
+        assert ei.value.code == -1
+    with aran.Solver3d(*BOX, maxbox=32, order=8, precision="mixed") as s:
+        for bad in (-2, 22):
+            with pytest.raises(aran.AranError):
+                aran._check(aran.load().aran_gpu_solver3d_set_fp64_root_depth(s._h, bad))
+
+
+def duplicated_points(n=6000, ndup=400, seed=21):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(0.0, 1.0, (n, 3))
+    q = rng.uniform(-1.0, 1.0, n)
+    src = rng.choice(n - ndup, ndup, replace=False)
+    x[n - ndup:] = x[src]                      # exact copies of other points
+    x[n - 2] = x[n - 1]                        # and a pair of copies of one point
+    return x, q
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_coincident_points_skipped(aran, oracle, precision, tol):
+    x, q = duplicated_points()
+    with aran.Solver3d(maxbox=16, order=8, field=False, precision=precision) as s:
+        pot, _ = s.solve(x, q)
+    assert np.all(np.isfinite(pot))
+    opot, _ = oracle.solve(x, q, order=8, maxbox=16, field=False)
+    assert np.all(np.isfinite(opot))
+    assert rel_l2(pot, opot) < tol
+    rp, _ = oracle.direct(x, q)
+    assert rel_l2(pot, rp) < 1e-4          # p = 8 truncation
+    with aran.Solver3d(maxbox=16, order=8, field=True, precision=precision) as s:
+        _, fld = s.solve(x, q)
+    ofld, _ = oracle.solve(x, q, order=8, maxbox=16, field=True)
+    assert np.all(np.isfinite(fld))
+    assert rel_l2(fld, ofld) < tol
+
+
+@pytest.mark.parametrize("what", ["x-nan", "y-inf", "q-nan", "q-neginf"])
+def test_nonfinite_input_rejected(aran, oracle, what):
+    x, q = W.uniform(5000, 23)
+    bad_x, bad_q = x.copy(), q.copy()
+    if what == "x-nan":
+        bad_x[1234, 0] = np.nan
+    elif what == "y-inf":
+        bad_x[17, 1] = np.inf
+    elif what == "q-nan":
+        bad_q[4999] = np.nan
+    else:
+        bad_q[0] = -np.inf
+    L = aran.load()
+    with aran.Solver3d(maxbox=32, order=6, field=True, precision="mixed") as s:
+        pot = np.full(len(q), 7.0)
+        fld = np.full((len(q), 3), 7.0)
+        dp = lambda a: a.ctypes.data_as(C.c_void_p)
+        rc = L.aran_gpu_solver3d_solve(s._h, len(q), dp(bad_x), dp(bad_q), dp(pot), dp(fld),
+                                       aran.MEM_HOST)
+        assert rc == -1
+        assert b"NaN or infinite" in L.aran_gpu_last_error()
+        assert np.all(pot == 7.0) and np.all(fld == 7.0)   # outputs untouched
+        # the solver keeps working
+        pot, fld = s.solve(x, q)
+    opot, _ = oracle.solve(x, q, order=6, maxbox=32, field=False)
+    assert rel_l2(pot, opot) < MIXED_TOL
+
+
+@pytest.mark.parametrize("order,kernel", [(12, "lanes"), (12, "sibling"), (10, "sibling")])
+def test_bounded_wait_timeout(aran, oracle, monkeypatch, order, kernel):
+    """The M2L consumers' wait for an offset table is bounded; with a poll limit
+    of zero it gives up at once: the solve returns ARAN_ERR_TIMEOUT (after the
+    copies in flight have landed), and the next solve is correct."""
+    x, q = W.uniform(20000, 24)
+    monkeypatch.setenv("ARAN_M2L_KERNEL", kernel)
+    with aran.Solver3d(maxbox=32, order=order, field=True, precision="mixed") as s:
+        monkeypatch.setenv("ARAN_DEBUG_WAIT_POLLS", "0")
+        with pytest.raises(aran.AranError) as ei:
+            s.solve(x, q)
+        assert ei.value.code == -5
+        monkeypatch.delenv("ARAN_DEBUG_WAIT_POLLS")
+        pot, fld = s.solve(x, q)
+    opot, _ = oracle.solve(x, q, order=order, maxbox=32, field=False)
+    assert rel_l2(pot, opot) < MIXED_TOL

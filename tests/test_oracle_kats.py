@@ -466,3 +466,20 @@ def test_semifar_keeps_the_accuracy(oracle):
     assert st1["p2l"] > 0 and st1["p2l"] == st1["m2p"] and st0["p2l"] == 0
     assert st1["p2p"] < st0["p2p"]
     assert e1 < 2 * e0 + 1e-9
+
+
+@pytest.mark.parametrize("flavour", ["rotate", "kkylin"])
+@pytest.mark.parametrize("field", [False, True])
+def test_threaded_solve_equals_serial(oracle, flavour, field):
+    """The threaded oracle solve (the CPU baseline's) gives every target its
+    terms in the single-threaded order: same counters, results equal to
+    rounding, also with coincident points."""
+    from aran_gb300 import workloads as W
+    x, q = W.plummer(6000, 8)
+    x[5990:] = x[:10]
+    kw = dict(order=8, maxbox=16, field=field, flavour=flavour, lb=(-1, -1, -1), ub=(1, 1, 1))
+    a, sa = oracle.solve(x, q, **kw)
+    b, sb = oracle.solve(x, q, nthreads=4, **kw)
+    assert sa == sb
+    assert np.all(np.isfinite(b))
+    assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(a)
