@@ -22,7 +22,7 @@ MEM_HOST, MEM_DEVICE = 0, 1
 STAT_NAMES = ("zero", "p2p", "p2m", "m2m", "m2l", "l2l", "l2p", "p2l", "m2p",
               "p2p_remote", "m2l_remote")
 STAGE_NAMES = ("total", "sort", "tree", "lists", "p2m", "m2m", "m2l", "l2l", "l2p",
-               "p2p", "h2d", "d2h")
+               "p2p", "h2d", "d2h", "semifar_p2l", "semifar_m2p")
 
 # exported symbols of include/aran_gpu.h
 EXPORTS = (
@@ -35,7 +35,8 @@ EXPORTS = (
     "aran_gpu_server_cancel", "aran_gpu_server_destroy",
     "aran_gpu_solver2d_create", "aran_gpu_solver2d_destroy", "aran_gpu_solver2d_solve",
     "aran_gpu_solver2d_get_stats", "aran_gpu_solver2d_timings", "aran_gpu_solver2d_tree_info",
-    "aran_gpu_solver2d_launches",
+    "aran_gpu_solver2d_launches", "aran_gpu_solver3d_set_fp64_root_depth",
+    "aran_gpu_plan_for_tolerance", "aran_gpu_solver3d_set_leaf_predicate",
 )
 
 
@@ -57,14 +58,24 @@ class Config2d(C.Structure):
     _fields_ = [("maxbox", C.c_int), ("order", C.c_int), ("max_depth", C.c_int)]
 
 
+class NodeView(C.Structure):
+    """AranGpuNodeView: a node about to be split, as a leaf predicate sees it."""
+    _fields_ = [("center", C.c_double * 3), ("lbound", C.c_double * 3),
+                ("ubound", C.c_double * 3), ("point_count", C.c_int64), ("depth", C.c_int)]
+
+
+LEAF_PREDICATE = C.CFUNCTYPE(C.c_int, C.POINTER(NodeView), C.c_void_p)
+
+
 class Request3d(C.Structure):
     _fields_ = [("cfg", Config3d), ("n", C.c_int64), ("xyz", C.c_void_p), ("q", C.c_void_p),
-                ("pot", C.c_void_p), ("field", C.c_void_p)]
+                ("pot", C.c_void_p), ("field", C.c_void_p), ("tolerance", C.c_double)]
 
 
 class RequestInfo(C.Structure):
     _fields_ = [("status", C.c_int), ("submit_s", C.c_double), ("start_s", C.c_double),
-                ("end_s", C.c_double), ("slot", C.c_int), ("footprint_bytes", C.c_int64)]
+                ("end_s", C.c_double), ("slot", C.c_int), ("footprint_bytes", C.c_int64),
+                ("order", C.c_int), ("precision", C.c_int)]
 
 
 _lib = None
@@ -102,12 +113,16 @@ def load(build_if_missing: bool = True):
     L.aran_gpu_solver3d_timings.restype = C.c_int
     L.aran_gpu_solver3d_launches.argtypes = [vp]
     L.aran_gpu_solver3d_launches.restype = C.c_int64
+    L.aran_gpu_solver3d_set_leaf_predicate.argtypes = [vp, vp, vp]
+    L.aran_gpu_solver3d_set_leaf_predicate.restype = C.c_int
     L.aran_gpu_solver3d_set_fp64_root_depth.argtypes = [vp, C.c_int]
     L.aran_gpu_solver3d_set_fp64_root_depth.restype = C.c_int
     L.aran_gpu_p2p_direct_noalloc.argtypes = [C.c_int64, vp, vp, vp, vp]
     L.aran_gpu_p2p_direct_noalloc.restype = C.c_int
     L.aran_gpu_footprint_bytes.argtypes = [C.POINTER(Config3d), C.c_int64]
     L.aran_gpu_footprint_bytes.restype = C.c_int64
+    L.aran_gpu_plan_for_tolerance.argtypes = [C.c_double, C.POINTER(Config3d)]
+    L.aran_gpu_plan_for_tolerance.restype = C.c_double
     L.aran_gpu_server_create.argtypes = [C.c_int, C.c_double, C.POINTER(vp)]
     L.aran_gpu_server_create.restype = C.c_int
     L.aran_gpu_server_submit.argtypes = [vp, C.POINTER(Request3d), C.POINTER(C.c_int64)]
@@ -161,6 +176,16 @@ def make_config(lbound=(0.0, 0.0, 0.0), ubound=(1.0, 1.0, 1.0), *, maxbox=64, or
     return cfg
 
 
+def plan_for_tolerance(tol: float, order: int = 0) -> tuple[int, str, float]:
+    """(order, precision, estimated error) the request loop picks for a
+    requested relative L2 potential error (order > 0: only the precision)."""
+    cfg = make_config(order=order)
+    est = load().aran_gpu_plan_for_tolerance(float(tol), C.byref(cfg))
+    if est < 0:
+        raise AranError(-1, load().aran_gpu_last_error().decode())
+    return cfg.order, ("mixed" if cfg.precision == PRECISIONS["mixed"] else "fp64"), est
+
+
 def footprint_bytes(n: int, **cfg_kw) -> int:
     """Estimated device memory of one solve (the server's admission unit)."""
     return int(load().aran_gpu_footprint_bytes(C.byref(make_config(**cfg_kw)), int(n)))
@@ -181,7 +206,10 @@ class Server:
         self._h = h
         self._live = {}
 
-    def submit(self, xyz, q, **cfg_kw) -> int:
+    def submit(self, xyz, q, tolerance=0.0, **cfg_kw) -> int:
+        """Queues a solve; ``tolerance`` > 0 lets the server pick the
+        precision (and the order, given ``order=0``) for that relative L2
+        potential error."""
         xyz = np.ascontiguousarray(xyz, dtype=np.float64)
         q = np.ascontiguousarray(q, dtype=np.float64)
         n = len(q)
@@ -189,7 +217,7 @@ class Server:
         pot = np.empty(n)
         fld = np.empty((n, 3)) if cfg.field else None
         req = Request3d(cfg, n, xyz.ctypes.data, q.ctypes.data, pot.ctypes.data,
-                        fld.ctypes.data if fld is not None else None)
+                        fld.ctypes.data if fld is not None else None, float(tolerance))
         t = C.c_int64()
         _check(load().aran_gpu_server_submit(self._h, C.byref(req), C.byref(t)))
         self._live[t.value] = (xyz, q, pot, fld)
@@ -202,7 +230,9 @@ class Server:
             raise AranError(rc, load().aran_gpu_last_error().decode())
         xyz, q, pot, fld = self._live.pop(int(ticket))
         d = {"status": info.status, "submit_s": info.submit_s, "start_s": info.start_s,
-             "end_s": info.end_s, "slot": info.slot, "footprint_bytes": info.footprint_bytes}
+             "end_s": info.end_s, "slot": info.slot, "footprint_bytes": info.footprint_bytes,
+             "order": info.order,
+             "precision": "mixed" if info.precision == PRECISIONS["mixed"] else "fp64"}
         _check(rc)
         return pot, fld, d
 
@@ -256,6 +286,13 @@ class Solver3d:
         self._h = h
         if fp64_root_depth is not None:
             _check(L.aran_gpu_solver3d_set_fp64_root_depth(h, int(fp64_root_depth)))
+
+    def set_leaf_predicate(self, fn=None):
+        """Nodes about to be split for which fn(NodeView) is true stay leaves
+        (virtual leaves); None clears it."""
+        self._leaf_cb = LEAF_PREDICATE(lambda v, _d: int(bool(fn(v.contents)))) if fn else None
+        _check(load().aran_gpu_solver3d_set_leaf_predicate(
+            self._h, C.cast(self._leaf_cb, C.c_void_p) if fn else None, None))
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

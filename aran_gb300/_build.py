@@ -14,7 +14,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(ROOT, "_build", "aran_gpu")
 LIB = os.path.join(HERE, "libaran_gpu.so")
-SOURCES = ["tables.cu", "tree.cu", "passes.cu", "p2p.cu", "m2l.cu", "m2l_lanes.cu", "kkylin.cu", "noalloc.cu", "server.cu", "solver.cu", "compat.cu", "solver2d.cu", "compat2d.cu", "semifar.cu", "series3d.cu"]
+SOURCES = ["tables.cu", "tree.cu", "passes.cu", "p2p.cu", "m2l.cu", "m2l_lanes.cu", "kkylin.cu",
+           "noalloc.cu", "server.cu", "solver.cu", "compat.cu", "solver2d.cu", "compat2d.cu",
+           "semifar.cu", "series3d.cu", "profiledb.cpp"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
@@ -23,7 +25,7 @@ FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
 
 
 def _deps() -> list[str]:
-    out = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh"))]
+    out = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".cpp"))]
     for sub in ("", "aran", "vsg"):
         d = os.path.join(ROOT, "include", sub)
         out += [os.path.join(d, f) for f in os.listdir(d) if f.endswith(".h")]
@@ -49,7 +51,7 @@ def build(force: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(_compile, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -162,7 +162,8 @@ struct KkTables {
 };
 
 struct Stage {
-  enum { TOTAL, SORT, TREE, LISTS, P2M, M2M, M2L, L2L, L2P, P2P, H2D, D2H, NSTAGE };
+  enum { TOTAL, SORT, TREE, LISTS, P2M, M2M, M2L, L2L, L2P, P2P, H2D, D2H, SEMI_P2L, SEMI_M2P,
+         NSTAGE };
 };
 
 }  // namespace aran
@@ -200,10 +201,17 @@ struct AranGpuSolver3d {
   // mixed precision: nodes of depth <= root64_depth keep FP64 expansions
   // (M2M into them, M2L and L2L at them in FP64); -1 = none
   int root64_depth = -1;
+  // host predicate keeping nodes about to be split as leaves (virtual leaves)
+  AranGpuLeafPredicate leaf_pred = nullptr;
+  void *leaf_pred_data = nullptr;
 };
 
 namespace aran {
 
+// solver.cu: the tree of n host particles without lists or passes (for
+// traversals of the tree); the solver's last solve results stay valid only
+// if the same particles are given
+void build_tree_only(AranGpuSolver3d *s, int64_t n, const double *xyz, const double *q);
 // tree.cu
 void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double *d_q);
 void build_lists(AranGpuSolver3d *s);

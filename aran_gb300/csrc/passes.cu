@@ -696,7 +696,9 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
     launch_m2l(s, true, 0, n_root_parents, st);
     launch_m2l(s, false, n_root_parents, t.n_parents - n_root_parents, st);
   }
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::SEMI_P2L], st));
   launch_semifar_p2l(s, st);
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::SEMI_P2L + 1], st));
   ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L + 1], st));
   // L2L
   ACHECK(cudaEventRecord(s->ev[2 * Stage::L2L], st));
@@ -734,7 +736,9 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
     ACHECK(cudaGetLastError());
     s->launches++;
   }
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::SEMI_M2P], st));
   launch_semifar_m2p(s, st);
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::SEMI_M2P + 1], st));
   ACHECK(cudaEventRecord(s->ev[2 * Stage::L2P + 1], st));
 }
 

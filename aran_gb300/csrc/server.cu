@@ -46,6 +46,46 @@ struct ConfigKey {
 
 }  // namespace
 
+// relative L2 error of the potential against the FP64 direct sum by order
+// (index p, 0 = not measured), the worst of uniform draws in [0,1]^3 with
+// charges U[-1,1] and Plummer draws with charges U[0,1], 2e4 and 3e5
+// particles, leaf capacity 64, 3,000 targets, measured on GB300; orders
+// between measured ones take the next lower measured order's error
+constexpr int kPlanMaxOrder = 30;
+const double kErrFp64[kPlanMaxOrder + 1] = {
+    0, 0, 0, 0, 2.4e-3, 0, 2.7e-4, 0, 3.8e-5, 0, 6.8e-6, 0, 1.4e-6, 0, 2.7e-7, 0, 6.4e-8,
+    0, 1.6e-8, 0, 5.8e-9};
+const double kErrMixed[kPlanMaxOrder + 1] = {
+    0, 0, 0, 0, 2.4e-3, 0, 2.7e-4, 0, 3.8e-5, 0, 6.8e-6, 0, 1.4e-6, 0, 5.4e-7, 0, 3.7e-7,
+    0, 3.7e-7, 0, 3.7e-7};
+
+double table_error(const double *tab, int p) {
+  for (int k = p < kPlanMaxOrder ? p : kPlanMaxOrder; k >= 1; --k)
+    if (tab[k] > 0) return tab[k];
+  return 1.0;
+}
+
+double plan_for_tolerance(double tol, AranGpuConfig3d *cfg) {
+  const double want = 0.5 * tol;
+  if (cfg->order > 0) {
+    double em = table_error(kErrMixed, cfg->order);
+    cfg->precision = em <= want ? ARAN_PRECISION_MIXED : ARAN_PRECISION_FP64;
+    return cfg->precision == ARAN_PRECISION_MIXED ? em : table_error(kErrFp64, cfg->order);
+  }
+  for (int prec : {ARAN_PRECISION_MIXED, ARAN_PRECISION_FP64}) {
+    const double *tab = prec == ARAN_PRECISION_MIXED ? kErrMixed : kErrFp64;
+    for (int p = 1; p <= kPlanMaxOrder; ++p)
+      if (tab[p] > 0 && tab[p] <= want) {
+        cfg->order = p;
+        cfg->precision = prec;
+        return tab[p];
+      }
+  }
+  cfg->order = kPlanMaxOrder;
+  cfg->precision = ARAN_PRECISION_FP64;
+  return table_error(kErrFp64, kPlanMaxOrder);
+}
+
 int64_t footprint_bytes(const AranGpuConfig3d *c, int64_t n) {
   const int p = c->order;
   const int64_t real = c->precision == ARAN_PRECISION_MIXED ? 4 : 8;
@@ -153,6 +193,14 @@ int64_t aran_gpu_footprint_bytes(const AranGpuConfig3d *cfg, int64_t n) {
   return footprint_bytes(cfg, n);
 }
 
+double aran_gpu_plan_for_tolerance(double tol, AranGpuConfig3d *cfg) {
+  if (!cfg || !(tol > 0)) {
+    set_error("plan_for_tolerance needs tol > 0 and a config");
+    return -1.0;
+  }
+  return plan_for_tolerance(tol, cfg);
+}
+
 int aran_gpu_server_create(int nslots, double hbm_budget_bytes, AranGpuServer **out) {
   if (!out) {
     set_error("out is NULL");
@@ -190,7 +238,14 @@ int aran_gpu_server_submit(AranGpuServer *sv, const AranGpuRequest3d *req, int64
     set_error("request needs n >= 1, xyz, q and an output");
     return ARAN_ERR_INVALID;
   }
-  int64_t fp = footprint_bytes(&req->cfg, req->n);
+  AranGpuRequest3d r = *req;
+  if (r.tolerance > 0) plan_for_tolerance(r.tolerance, &r.cfg);
+  if (r.cfg.order < 1 || r.cfg.order > kMaxOrder) {
+    set_error("request order must be in [1, " + std::to_string(kMaxOrder) +
+              "] (or 0 with a tolerance)");
+    return ARAN_ERR_INVALID;
+  }
+  int64_t fp = footprint_bytes(&r.cfg, r.n);
   std::lock_guard<std::mutex> lk(sv->mu);
   if (fp > sv->budget) {
     set_error("request footprint " + std::to_string(fp) + " B exceeds the HBM budget " +
@@ -199,7 +254,7 @@ int aran_gpu_server_submit(AranGpuServer *sv, const AranGpuRequest3d *req, int64
   }
   auto job = std::make_unique<Job>();
   job->ticket = sv->next_ticket++;
-  job->req = *req;
+  job->req = r;
   job->footprint = fp;
   job->t_submit = now_s(sv);
   *ticket = job->ticket;
@@ -235,6 +290,8 @@ int aran_gpu_server_wait(AranGpuServer *sv, int64_t ticket, double timeout_s,
     info->end_s = j->t_end;
     info->slot = j->slot;
     info->footprint_bytes = j->footprint;
+    info->order = j->req.cfg.order;
+    info->precision = j->req.cfg.precision;
   }
   int st = j->status;
   if (st != ARAN_OK) set_error(j->error);

@@ -25,6 +25,20 @@ int consumer_wait_polls() {
 
 void scatter_outputs(AranGpuSolver3d *s, double *pot, double *fld);
 
+void build_tree_only(AranGpuSolver3d *s, int64_t n, const double *xyz, const double *q) {
+  ACHECK(cudaSetDevice(s->device));
+  cudaStream_t st = s->s0;
+  ACHECK(cudaMemsetAsync(s->err_dev.ptr, 0, sizeof(int), st));
+  s->io_xyz.reserve(3 * n);
+  s->io_q.reserve(n);
+  ACHECK(cudaMemcpyAsync(s->io_xyz.ptr, xyz, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+  ACHECK(cudaMemcpyAsync(s->io_q.ptr, q, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::SORT], st));
+  build_tree(s, n, s->io_xyz.ptr, s->io_q.ptr);
+  ACHECK(cudaStreamSynchronize(st));
+  s->have_tree = false;   // no lists: counters and list queries need a solve
+}
+
 namespace {
 
 // mixed solvers of order >= kRootFp64Order start with FP64 expansions at
@@ -210,6 +224,8 @@ int aran_gpu_solver3d_solve(AranGpuSolver3d *s, int64_t n, const double *xyz, co
     s->ms[9] = el(2 * Stage::P2P, 2 * Stage::P2P + 1);
     s->ms[10] = el(2 * Stage::H2D, 2 * Stage::H2D + 1);
     s->ms[11] = el(2 * Stage::D2H, 2 * Stage::D2H + 1);
+    s->ms[12] = el(2 * Stage::SEMI_P2L, 2 * Stage::SEMI_P2L + 1);
+    s->ms[13] = el(2 * Stage::SEMI_M2P, 2 * Stage::SEMI_M2P + 1);
   } catch (const CudaError &ce) {
     return from_cuda(ce);
   } catch (const InputError &ie) {
@@ -337,6 +353,14 @@ int aran_gpu_solver3d_timings(AranGpuSolver3d *s, double ms[16]) {
 }
 
 int64_t aran_gpu_solver3d_launches(AranGpuSolver3d *s) { return s ? s->launches : -1; }
+
+int aran_gpu_solver3d_set_leaf_predicate(AranGpuSolver3d *s, AranGpuLeafPredicate pred,
+                                         void *user_data) {
+  if (!s) return fail(ARAN_ERR_INVALID, "solver is NULL");
+  s->leaf_pred = pred;
+  s->leaf_pred_data = pred ? user_data : nullptr;
+  return ARAN_OK;
+}
 
 int aran_gpu_solver3d_set_fp64_root_depth(AranGpuSolver3d *s, int depth) {
   if (!s) return fail(ARAN_ERR_INVALID, "solver is NULL");

@@ -471,6 +471,47 @@ void grow_nodes(DevTree &t, size_t need, size_t keep, cudaStream_t st) {
   t.center.grow_keep(3 * need, 3 * keep, st);
 }
 
+// the nodes of one level about to be split are shown to the host leaf
+// predicate; those it keeps as leaves lose their flag
+void apply_leaf_predicate(AranGpuSolver3d *s, int off, int cnt, int d, int *d_flags,
+                          cudaStream_t st) {
+  const DevTree &t = s->tree;
+  const AranGpuConfig3d &c = s->cfg;
+  std::vector<int> fl(cnt), b(cnt), e(cnt), ijk(3 * (size_t)cnt);
+  ACHECK(cudaMemcpyAsync(fl.data(), d_flags, cnt * sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaMemcpyAsync(b.data(), t.begin.ptr + off, cnt * sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaMemcpyAsync(e.data(), t.end.ptr + off, cnt * sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaMemcpyAsync(ijk.data(), t.ijk.ptr + 3 * (size_t)off, 3 * cnt * sizeof(int),
+                         cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaStreamSynchronize(st));
+  bool changed = false;
+  for (int i = 0; i < cnt; ++i) {
+    if (!fl[i]) continue;
+    AranGpuNodeView v;
+    for (int a = 0; a < 3; ++a) {
+      // the cell by halving the root box, as the node centres are made
+      double lo = c.lb[a], hi = c.ub[a];
+      for (int bit = d - 1; bit >= 0; --bit) {
+        const double mid = (lo + hi) * 0.5;
+        if ((ijk[3 * (size_t)i + a] >> bit) & 1) lo = mid;
+        else hi = mid;
+      }
+      v.lbound[a] = lo;
+      v.ubound[a] = hi;
+      v.center[a] = (lo + hi) * 0.5;
+    }
+    v.point_count = e[i] - b[i];
+    v.depth = d;
+    if (s->leaf_pred(&v, s->leaf_pred_data)) {
+      fl[i] = 0;
+      changed = true;
+    }
+  }
+  if (changed)
+    ACHECK(cudaMemcpyAsync(d_flags, fl.data(), cnt * sizeof(int), cudaMemcpyHostToDevice, st));
+  ACHECK(cudaStreamSynchronize(st));
+}
+
 }  // namespace
 
 void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double *d_q) {
@@ -526,6 +567,7 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
     k_flag_internal<<<ceil_div(cnt, TB), TB, 0, st>>>(cnt, off, t.begin.ptr, t.end.ptr, c.maxbox,
                                                        d, maxd, flags.ptr);
     s->launches++;
+    if (s->leaf_pred) apply_leaf_predicate(s, off, cnt, d, flags.ptr, st);
     exclusive_scan(s, flags.ptr, pos, cnt, st);
     ACHECK(cudaMemcpyAsync(&hostbuf[0], pos + cnt - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     ACHECK(cudaMemcpyAsync(&hostbuf[1], flags.ptr + cnt - 1, sizeof(int), cudaMemcpyDeviceToHost, st));

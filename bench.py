@@ -13,10 +13,16 @@ bulk, FP64 tables/centres/final sums).  The same line reports the plain FP64
 GPU path on the same input (``fp64``), the error of the mixed path against
 it and against an FP64 direct sum on a target subset.
 
+The same line carries the clustered configuration at the other two orders
+(``orders``: p = 8 and 16, mixed and FP64, with their errors), the served
+request stream (tolerance-driven plans, p50/p99 over an arrival-rate sweep,
+per-request errors), the batched systems and the CPU baseline.
+
 ``--impl reference`` times the reference algorithm on the host cores: the
 C restatement of LibAran's solver in oracle/ (the reference itself needs
-glib and libvsg, which are not available), one independent process per core
-on bounded samples of the same workload.
+glib and libvsg, which are not available), full solves of the same
+4M-particle workload with the per-node and per-leaf work spread over every
+host thread.
 
 Multi-GPU: one process per GPU (torchrun); each rank solves its own
 replica (the path does not shard: independent solves, no collective on the
@@ -48,6 +54,17 @@ WORKLOADS = {
     "uniform1m": ("uniform", 1_000_000, 12, 64, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0),
                   "N=1,000,000 uniform in [0,1]^3, q~U[-1,1], p=12, leaf 64, field"),
 }
+
+
+def m2l_flops_rotate(p: int) -> int:
+    """Algorithmic flops of one rotate-flavour M2L by the operator's own
+    definition: 4 [A(p-1) + B(p) + A(p)], A(L) = (L+1)(L+2)(4L+3)/6 the
+    multiply-adds of a real Wigner-d block applied to complex coefficients
+    (aransphericalseriesd-rotate.c:34-80), B(p) = p(p+1)(p+2)/3 those of the
+    vertical translation (aransphericalseriesd-translate.c:647-675); 13,988 at
+    p = 12."""
+    a = lambda L: (L + 1) * (L + 2) * (4 * L + 3) // 6
+    return 4 * (a(p - 1) + p * (p + 1) * (p + 2) // 3 + a(p))
 
 
 def m2l_flops(p: int) -> int:
@@ -128,10 +145,14 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ serving
+TOLERANCES = (1e-4, 1e-6, 1e-9)
+
+
 def serving_stream(nreq: int, rate: float, seed: int = 5):
     """Poisson arrivals of 3D potential+field solves: N log-uniform in
-    [1e3, 2e6], requested tolerance 1e-4/1e-6/1e-9 -> p = 6/10/16, half
-    uniform in [0,1]^3, half Plummer in [-1,1]^3."""
+    [1e3, 2e6], a requested relative potential error drawn from 1e-4 / 1e-6
+    / 1e-9 (the request loop picks order and precision for it), half uniform
+    in [0,1]^3, half Plummer in [-1,1]^3, leaf 64."""
     import numpy as np
     from aran_gb300 import workloads as W
     rng = np.random.default_rng(seed)
@@ -139,45 +160,115 @@ def serving_stream(nreq: int, rate: float, seed: int = 5):
     reqs = []
     for i in range(nreq):
         n = int(np.exp(rng.uniform(np.log(1e3), np.log(2e6))))
-        p = (6, 10, 16)[int(rng.integers(0, 3))]
+        tol = TOLERANCES[int(rng.integers(0, 3))]
         if rng.uniform() < 0.5:
             x, q = W.uniform(n, 1000 + i)
             lb, ub = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)
         else:
             x, q = W.plummer(n, 1000 + i)
             lb, ub = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
-        reqs.append((float(arrivals[i]), x, q, dict(lbound=lb, ubound=ub, maxbox=64, order=p,
-                                                     field=True)))
+        reqs.append(dict(arrival=float(arrivals[i]), x=x, q=q, tol=tol,
+                         kw=dict(lbound=lb, ubound=ub, maxbox=64, field=True)))
     return reqs
 
 
-def run_serving(reqs, precision: str, nslots: int = 4, budget: float = 150e9) -> dict:
+def run_serving(reqs, rate_scale: float = 1.0, plain_fp64: bool = False, nslots: int = 4,
+                budget: float = 150e9, keep: bool = False) -> dict:
+    """Replays the stream (arrival times / rate_scale; 0 = all at once).
+    Default: every request carries its tolerance and the request loop plans
+    order and precision.  plain_fp64: the same orders, every request FP64."""
     import numpy as np
     import aran_gb300 as A
+    plans = {tol: A.plan_for_tolerance(tol) for tol in TOLERANCES}
+
+    def args_of(r):
+        order, prec, _ = plans[r["tol"]]
+        if plain_fp64:
+            return dict(order=order, precision="fp64", tolerance=0.0, **r["kw"])
+        return dict(order=0, tolerance=r["tol"], **r["kw"])
+
     with A.Server(nslots=nslots, hbm_budget_bytes=budget) as sv:
         # one warm request per configuration so table builds stay out of the stream
         seen = set()
-        for _, x, q, kw in reqs:
-            key = (kw["order"], kw["lbound"])
+        for r in reqs:
+            a = args_of(r)
+            key = (plans[r["tol"]][:2], r["kw"]["lbound"])
             if key not in seen:
                 seen.add(key)
-                sv.wait(sv.submit(x[:2000], q[:2000], precision=precision, **kw))
+                sv.wait(sv.submit(r["x"][:2000], r["q"][:2000], **a))
         t0 = time.perf_counter()
         tickets = []
-        for arr, x, q, kw in reqs:
-            dt = arr - (time.perf_counter() - t0)
-            if dt > 0:
-                time.sleep(dt)
-            tickets.append(sv.submit(x, q, precision=precision, **kw))
-        infos = [sv.wait(t)[2] for t in tickets]
+        for r in reqs:
+            if rate_scale > 0:
+                dt = r["arrival"] / rate_scale - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+            tickets.append(sv.submit(r["x"], r["q"], **args_of(r)))
+        outs = [sv.wait(t) for t in tickets]
+    infos = [o[2] for o in outs]
     lat = np.array([i["end_s"] - i["submit_s"] for i in infos])
     span = max(i["end_s"] for i in infos) - min(i["submit_s"] for i in infos)
-    npart = sum(len(r[2]) for r in reqs)
-    return {"precision": precision, "requests": len(reqs),
-            "p50_ms": float(np.percentile(lat, 50) * 1e3),
-            "p99_ms": float(np.percentile(lat, 99) * 1e3),
-            "throughput": npart / span, "unit": UNIT,
-            "mean_queue_ms": float(np.mean([i["start_s"] - i["submit_s"] for i in infos]) * 1e3)}
+    npart = sum(len(r["q"]) for r in reqs)
+    res = {"mode": "plain FP64" if plain_fp64 else "tolerance plan", "requests": len(reqs),
+           "p50_ms": float(np.percentile(lat, 50) * 1e3),
+           "p99_ms": float(np.percentile(lat, 99) * 1e3),
+           "throughput": npart / span, "unit": UNIT,
+           "mean_queue_ms": float(np.mean([i["start_s"] - i["submit_s"] for i in infos]) * 1e3)}
+    if keep:
+        res["_outs"] = outs
+    return res
+
+
+def serving_errors(reqs, outs, targets: int = 200) -> dict:
+    """Per request: relative L2 and largest per-particle relative error
+    |phi - phi_ref| / max(|phi|, |phi_ref|) (tests/newtonpot3.c:678-715) of
+    the potential on a target sample against the FP64 direct sum, grouped by
+    requested tolerance."""
+    import numpy as np
+    import oracle
+    by = {}
+    for r, (pot, fld, info) in zip(reqs, outs):
+        n = len(r["q"])
+        tgt = np.random.default_rng(n).choice(n, min(n, targets), replace=False)
+        rp, _ = oracle.direct(r["x"], r["q"], targets=tgt)
+        l2 = float(np.linalg.norm(pot[tgt] - rp) / np.linalg.norm(rp))
+        mx = float((np.abs(pot[tgt] - rp) / np.maximum(np.abs(pot[tgt]), np.abs(rp))).max())
+        d = by.setdefault(f"{r['tol']:g}", {"requests": 0, "met": 0, "worst_rel_l2": 0.0,
+                                            "worst_max_rel": 0.0, "plans": set()})
+        d["requests"] += 1
+        d["met"] += int(l2 <= r["tol"])
+        d["worst_rel_l2"] = max(d["worst_rel_l2"], l2)
+        d["worst_max_rel"] = max(d["worst_max_rel"], mx)
+        d["plans"].add(f"p={info['order']} {info['precision']}")
+    for d in by.values():
+        d["plans"] = sorted(d["plans"])
+    return by
+
+
+def run_serving_suite(nreq: int, rate: float) -> dict:
+    """The served stream at the base rate (tolerance plans, with per-request
+    errors, and plain FP64 at the same orders), then the planned stream at
+    rates x4, x16 and all at once (saturation)."""
+    import aran_gb300 as A
+    reqs = serving_stream(nreq, rate)
+    base = run_serving(reqs, keep=True)
+    outs = base.pop("_outs")
+    out = {"stream": (f"{nreq} Poisson arrivals, N log-uniform [1e3, 2e6], requested relative "
+                      "potential error 1e-4 / 1e-6 / 1e-9, half uniform / half Plummer, leaf 64, "
+                      "potential + field, 4 slots, 150 GB HBM admission budget"),
+           "plans": {f"{t:g}": {"order": o, "precision": pr, "table_error": e}
+                     for t, (o, pr, e) in ((t, A.plan_for_tolerance(t)) for t in TOLERANCES)},
+           "base_rate_per_s": rate, "planned": base,
+           "errors": serving_errors(reqs, outs)}
+    del outs
+    out["plain_fp64"] = run_serving(reqs, plain_fp64=True)
+    sweep = []
+    for k in (4.0, 16.0, 0.0):
+        r = run_serving(reqs, rate_scale=k)
+        r["rate_per_s"] = rate * k if k > 0 else "all at once"
+        sweep.append(r)
+    out["rate_sweep"] = sweep
+    return out
 
 
 # ------------------------------------------------------------------ batched
@@ -254,70 +345,93 @@ def run_batched_2d(nsys: int, steps: int, order: int = 20, maxbox: int = 32) -> 
     return out
 
 
-def run_batched_3d(nsys: int, precision: str = "mixed", nslots: int = 4) -> dict:
+def run_batched_3d(nsys: int, nslots: int = 4, check_systems: int = 8) -> dict:
     """Config 4, 3D part: every system a request of the request loop, all
-    submitted at once; throughput = particles / (last end - first submit)."""
+    submitted at once (mixed precision at the system's order; FP64 root levels
+    where the order asks for them); throughput = particles / (last end - first
+    submit); a sample of systems checked against the FP64 direct sum."""
     import numpy as np
     import aran_gb300 as A
+    import oracle
     from aran_gb300 import workloads as W
     systems = W.batch3d(nsys)
     kw = dict(lbound=(0.0, 0.0, 0.0), ubound=(1.0, 1.0, 1.0), maxbox=64, field=True,
-              precision=precision)
+              precision="mixed")
     with A.Server(nslots=nslots, hbm_budget_bytes=150e9) as sv:
         for p in (4, 8, 12):   # resident solvers per order in every slot
             for t in [sv.submit(systems[0][0][:2000], systems[0][1][:2000], order=p, **kw)
                       for _ in range(nslots)]:
                 sv.wait(t)
         tickets = [sv.submit(x, q, order=p, **kw) for x, q, p in systems]
-        infos = [sv.wait(t)[2] for t in tickets]
+        outs = [sv.wait(t) for t in tickets]
+    infos = [o[2] for o in outs]
     span = max(i["end_s"] for i in infos) - min(i["submit_s"] for i in infos)
     npart = sum(len(s[1]) for s in systems)
-    return {"systems": nsys, "particles": npart, "precision": precision, "slots": nslots,
-            "description": (f"the first {nsys} draws of the config-4 3D stream (2,048 "
-                            "systems): N log-uniform in [1e3, 2e5], uniform in [0,1]^3 or 1-8 "
-                            "Gaussian blobs, p in {4, 8, 12}, leaf 64, potential + field, "
-                            "host arrays in and out"),
-            "value": npart / span, "unit": UNIT, "wall_s": span}
+    worst = {}
+    for i in np.random.default_rng(4).choice(nsys, check_systems, replace=False):
+        x, q, p = systems[i]
+        tgt = np.random.default_rng(i).choice(len(q), min(len(q), 300), replace=False)
+        rp, _ = oracle.direct(x, q, targets=tgt)
+        e = float(np.linalg.norm(outs[i][0][tgt] - rp) / np.linalg.norm(rp))
+        worst[f"p={p}"] = max(worst.get(f"p={p}", 0.0), e)
+    return {"systems": nsys, "particles": npart, "precision": "mixed", "slots": nslots,
+            "description": (f"{nsys} systems of the config-4 3D stream: N log-uniform in "
+                            "[1e3, 2e5], uniform in [0,1]^3 or 1-8 Gaussian blobs, p in "
+                            "{4, 8, 12}, leaf 64, potential + field, host arrays in and out"),
+            "value": npart / span, "unit": UNIT, "wall_s": span, "systems_per_s": nsys / span,
+            "accuracy": {"checked_systems": check_systems, "targets_each": 300,
+                         "worst_rel_l2_vs_direct_by_order": worst}}
 
 
 # ------------------------------------------------------------- CPU baseline
-def _cpu_job(args):
-    name, n_sample, seed = args
-    import numpy as np
-    import oracle
-    from aran_gb300 import workloads as W
-    gen, n, p, maxbox, lb, ub, desc = WORKLOADS[name]
-    x, q = getattr(W, gen)(n_sample, 100 + seed)
-    t0 = time.perf_counter()
-    oracle.solve(x, q, order=p, maxbox=maxbox, flavour="rotate", field=True, lb=lb, ub=ub)
-    return n_sample, time.perf_counter() - t0
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
-def cpu_baseline(name: str, n_sample: int, procs: int, rounds: int = 1) -> dict:
-    """Times the oracle port of the reference solver: `procs` independent
-    single-threaded processes (the reference has no threading), each solving
-    its own n_sample-particle draw of the workload distribution."""
+def cpu_baseline(x, q, name: str, max_solves: int = 1, budget_s: float = 0.0) -> dict:
+    """Times the oracle port of the reference solver on the whole workload
+    (same particles, order, leaf size, flavour, field): full solves with the
+    per-node and per-leaf work spread over every host thread, max_solves of
+    them or as many as fit in budget_s (at least one).  Also reports the
+    particles per CPU-second (the one-core equivalent)."""
     import oracle
     oracle.build()
-    ctx = mp.get_context("spawn")
-    total_n, t0 = 0, time.perf_counter()
-    with ctx.Pool(procs) as pool:
-        for r in range(rounds):
-            for n_done, _ in pool.map(_cpu_job, [(name, n_sample, r * procs + i) for i in range(procs)]):
-                total_n += n_done
-    el = time.perf_counter() - t0
-    return {"value": total_n / el, "unit": UNIT, "cores": procs, "kind": "port",
-            "sample": f"{procs} processes x {rounds} round(s), each a full solve of its own "
-                      f"{n_sample}-particle draw of the workload distribution "
-                      f"(same p, leaf size, flavour, field); {el:.1f} s wall"}
+    gen, n, p, maxbox, lb, ub, desc = WORKLOADS[name]
+    threads = os.cpu_count() or 1
+    walls, cpus = [], []
+    while len(walls) < max(1, max_solves):
+        c0, t0 = time.process_time(), time.perf_counter()
+        oracle.solve(x, q, order=p, maxbox=maxbox, flavour="rotate", field=True, lb=lb, ub=ub,
+                     nthreads=threads)
+        walls.append(time.perf_counter() - t0)
+        cpus.append(time.process_time() - c0)
+        if budget_s > 0 and sum(walls) + walls[-1] > budget_s:
+            break
+    wall = sum(walls)
+    return {"value": len(walls) * len(q) / wall, "unit": UNIT, "cores": threads, "kind": "port",
+            "solves": len(walls), "s_per_solve": wall / len(walls),
+            "per_core_value": len(walls) * len(q) / sum(cpus),
+            "cpu_model": cpu_model(),
+            "sample": (f"the whole workload ({len(q)} particles, same p, leaf size, flavour, "
+                       f"field): {len(walls)} full solve(s) by the C restatement of the "
+                       f"reference solver, per-node/per-leaf work over {threads} host threads "
+                       f"({wall / len(walls):.1f} s wall, {sum(cpus) / len(cpus):.0f} CPU-s "
+                       "per solve); per_core_value = particles per CPU-second")}
 
 
 # ----------------------------------------------------------------- GPU arm
-# DRAM bytes of the FP32 M2L launch per tree node: ncu capture of
-# k_m2l_lanes<12> on uniform1m (37449 nodes), dram__bytes_read.sum +
-# dram__bytes_write.sum = 26.004224 MB + 0.010496 MB
-# (profiles/m2l_lanes_uniform1m_p12_mixed.md)
-M2L_DRAM_BYTES_PER_NODE = (26.004224e6 + 0.010496e6) / 37449
+# DRAM bytes of one k_m2l_lanes<12> launch on plummer4m (233,161 nodes,
+# 38,977,626 M2L): ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum
+# on one launch of that workload (-k regex:k_m2l_lanes -s 1 -c 1,
+# --clock-control none), read + write
+M2L_DRAM_BYTES_PLUMMER4M = None
 
 
 def run_gpu(args):
@@ -382,18 +496,23 @@ def run_gpu(args):
         stage[0]["_wall_s"] = wall
         return el, stage, launches
 
-    results = {}
+    def mean_stages(stages):
+        return {k: round(statistics.mean(d[k] for d in stages), 4) for k in stages[0]
+                if not k.startswith("_")}
+
+    def run_order(order, precision, steps, warmup):
+        """(seconds per step, stage ms, potential, field) of one configuration."""
+        with A.Solver3d(lb, ub, maxbox=maxbox, order=order, flavour="rotate", field=True,
+                        precision=precision) as s_:
+            for _ in range(warmup):
+                solve_dev(s_)
+            el_, st_, _ = timed(s_, solve_dev, steps, f"order{order}_{precision}")
+            return (el_ / steps, mean_stages(st_), pot.cpu().numpy().copy(),
+                    fld.cpu().numpy().copy())
+
     # plain FP64 path on the same input (reference point of the metric)
-    with A.Solver3d(lb, ub, maxbox=maxbox, order=p, flavour="rotate", field=True,
-                    precision="fp64") as s64:
-        for _ in range(max(1, min(args.warmup, 2))):
-            solve_dev(s64)
-        el64, st64, _ = timed(s64, solve_dev, max(1, args.fp64_steps), "timed_fp64")
-        pot64 = pot.cpu().numpy().copy()
-        fld64 = fld.cpu().numpy().copy()
-        results["fp64_s_per_step"] = el64 / max(1, args.fp64_steps)
-        st64[0].pop("_wall_s")
-        results["fp64_stage_ms"] = {k: round(statistics.mean(d[k] for d in st64), 3) for k in st64[0]}
+    fp64_s, fp64_stages, pot64, fld64 = run_order(p, "fp64", max(1, args.fp64_steps),
+                                                  max(1, min(args.warmup, 2)))
 
     s = A.Solver3d(lb, ub, maxbox=maxbox, order=p, flavour="rotate", field=True,
                    precision=args.precision)
@@ -426,6 +545,18 @@ def run_gpu(args):
     wall_e2e = st_e2e[0].pop("_wall_s")
     s.close()
 
+    # the clustered configuration at its other orders (mixed and FP64)
+    orders = {}
+    if rank == 0 and args.orders:
+        for po in [int(v) for v in args.orders.split(",") if v]:
+            ms_, stm_, pm_, fm_ = run_order(po, "mixed", max(1, min(args.steps, 5)), 2)
+            m64_, st64_, p64_, f64_ = run_order(po, "fp64", 1, 1)
+            orders[po] = {"mixed": {"value": n / ms_, "unit": UNIT, "ms_per_step": 1e3 * ms_,
+                                    "stage_ms": stm_},
+                          "fp64": {"value": n / m64_, "unit": UNIT, "ms_per_step": 1e3 * m64_},
+                          "speedup_vs_fp64_gpu": m64_ / ms_,
+                          "_arrays": (pm_, fm_, p64_, f64_)}
+
     if rank != 0:
         if dist is not None:
             dist.barrier()
@@ -433,10 +564,12 @@ def run_gpu(args):
         return
 
     # accuracy: mixed vs FP64 GPU path, both vs FP64 direct sum on a subset
+    # of targets (the same subset for every order)
     def rl2(a, b):
         return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
     acc = {"pot_vs_fp64_gpu": rl2(potm, pot64), "field_vs_fp64_gpu": rl2(fldm, fld64)}
+    rp = rf = tgt = None
     if args.direct_targets > 0:
         import oracle
         tgt = np.random.default_rng(5).choice(n, args.direct_targets, replace=False)
@@ -445,51 +578,75 @@ def run_gpu(args):
                     "pot_vs_direct": rl2(potm[tgt], rp), "field_vs_direct": rl2(fldm[tgt], rf),
                     "fp64_pot_vs_direct": rl2(pot64[tgt], rp),
                     "fp64_field_vs_direct": rl2(fld64[tgt], rf)})
+    for po, d in orders.items():
+        pm_, fm_, p64_, f64_ = d.pop("_arrays")
+        a = {"pot_vs_fp64_gpu": rl2(pm_, p64_), "field_vs_fp64_gpu": rl2(fm_, f64_)}
+        if tgt is not None:
+            a.update({"pot_vs_direct": rl2(pm_[tgt], rp), "field_vs_direct": rl2(fm_[tgt], rf),
+                      "fp64_pot_vs_direct": rl2(p64_[tgt], rp),
+                      "fp64_field_vs_direct": rl2(f64_[tgt], rf)})
+        d["accuracy"] = a
+    orders[p] = {"mixed": {"value": n * args.steps / el, "unit": UNIT,
+                           "ms_per_step": 1e3 * el / args.steps},
+                 "fp64": {"value": n / fp64_s, "unit": UNIT, "ms_per_step": 1e3 * fp64_s},
+                 "speedup_vs_fp64_gpu": fp64_s / (el / args.steps),
+                 "accuracy": "see accuracy"}
 
     ms_step = 1e3 * el / args.steps
     value = world * n * args.steps / el
     wall_s = stages[0].pop("_wall_s")
-    stage_ms = {k: round(statistics.mean(d[k] for d in stages), 4) for k in stages[0]}
-    # roofline of the dominant kernel (M2L): algorithmic flops per launch over
-    # its CUDA-event duration (recorded on the launching stream by the library)
-    flops = info["far"] * m2l_flops(p)
+    stage_ms = mean_stages(stages)
+    # roofline of the dominant kernel (M2L): algorithmic flops per launch (the
+    # operator's definition, F(p) per directed M2L) over its CUDA-event
+    # duration recorded on the launching stream by the library
     m2l_s = stage_ms["m2l"] * 1e-3
+    flops = info["far"] * m2l_flops_rotate(p)
+    flops_applied = info["far"] * m2l_flops(p)
+    props = torch.cuda.get_device_properties(local)
+    sms = props.multi_processor_count
     smax = clk.get("sm_max_mhz") or 2070.0
-    fp32_peak = 152 * 128 * 2 * smax * 1e6 / 1e12
+    fp32_peak = sms * 128 * 2 * smax * 1e6 / 1e12
     achieved = flops / m2l_s / 1e12
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
-    # algorithmic bytes of the M2L launch: every far source multipole and every
-    # written local once (FP32 complex), at the HBM roofline
-    alg_bytes = (info["far"] * (p * (p + 1) // 2) + info["nodes"] * ((p + 1) * (p + 2) // 2)) * 8
+    # algorithmic bytes of the launch: every node's multipole read and local
+    # written once (FP32 complex), x2 as counted for expansions
+    real = 4 if args.precision == "mixed" else 8
+    alg_bytes = info["nodes"] * (p * (p + 1) // 2 + (p + 1) * (p + 2) // 2) * 2 * real * 2
+    traffic = args.m2l_traffic
+    if traffic is None and args.workload == "plummer4m" and p == 12 and args.precision == "mixed":
+        traffic = M2L_DRAM_BYTES_PLUMMER4M
     roof = {
-        "kernel": ("k_m2l_sibling<float> (rotate M2L, all levels, one launch)"
+        "kernel": ("k_m2l_sibling (rotate M2L, all levels, one launch)"
                    if os.environ.get("ARAN_M2L_KERNEL") == "sibling" or p not in (8, 12)
                    or args.precision != "mixed" else
                    f"k_m2l_lanes<{p}> (rotate M2L, FP32 lane pairs, all levels, one launch)"),
         "bound": "fp32",
         "achieved": round(achieved, 3), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
         "frac": round(achieved / fp32_peak, 4),
-        "peak_source": ("FP32 CUDA-core peak 152 SMs x 128 lanes x 2 flop x max SM clock; "
-                        "MEASURED_PEAKS.json holds only HBM and bf16-tensor peaks, and this "
+        "traffic": traffic,
+        "peak_source": (f"FP32 CUDA-core peak: {sms} SMs (device property) x 128 FP32 lanes x 2 "
+                        f"flop x {smax:.0f} MHz (max SM clock sampled by nvidia-smi); "
+                        "MEASURED_PEAKS.json holds only HBM and bf16-tensor peaks and this "
                         "kernel runs on the FP32 pipes"),
-        "flops_per_launch": flops, "m2l_per_launch": info["far"],
-        "flops_per_m2l": m2l_flops(p),
-        "hbm_view": {"bytes_per_launch": alg_bytes,
-                     "achieved_gbs": round(alg_bytes / m2l_s / 1e9, 1),
-                     "peak_gbs": peaks.get("hbm_gbs", 6803.8),
-                     "frac": round(alg_bytes / m2l_s / 1e9 / peaks.get("hbm_gbs", 6803.8), 4)},
-        # DRAM bytes per launch: ncu capture of this kernel on uniform1m,
-        # 694 B per tree node, scaled by this tree's node count
-        "traffic": (args.m2l_traffic if args.m2l_traffic is not None
-                    else round(M2L_DRAM_BYTES_PER_NODE * info["nodes"])),
-        "traffic_source": ("--m2l-traffic" if args.m2l_traffic is not None else
-                           "ncu dram__bytes_read.sum+write.sum of the uniform1m launch, "
-                           "scaled by node count"),
+        "flops_per_m2l": m2l_flops_rotate(p), "m2l_per_launch": info["far"],
+        "flops_per_launch": flops,
+        "as_applied": {"flops_per_m2l": m2l_flops(p), "flops_per_launch": flops_applied,
+                       "achieved": round(flops_applied / m2l_s / 1e12, 3),
+                       "frac": round(flops_applied / m2l_s / 1e12 / fp32_peak, 4)},
+        "algorithmic_bytes": {"bytes_per_launch": alg_bytes,
+                              "definition": "nodes x (multipole + local coefficients) x 8 B "
+                                            "(FP32 complex) x 2",
+                              "achieved_gbs": round(alg_bytes / m2l_s / 1e9, 1),
+                              "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on "
+                           "this workload" if traffic is not None else "not captured"),
         "bf16_tensor_peak_tflops": peaks.get("bf16_tflops"),
+        "tensor_frac": (round(achieved / peaks["bf16_tflops"], 4)
+                        if peaks.get("bf16_tflops") else None),
     }
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -504,11 +661,11 @@ def run_gpu(args):
                    "timing": ("CUDA events on the solver's launching stream around each solve, "
                               "summed over the timed steps; max over ranks"),
                    "wall_ms_per_step": 1e3 * wall_s / args.steps},
-        "fp64": {"value": world * n / results["fp64_s_per_step"], "unit": UNIT,
-                 "ms_per_step": 1e3 * results["fp64_s_per_step"],
-                 "stage_ms": results["fp64_stage_ms"]},
-        "speedup_vs_fp64_gpu": (value / world) / (n / results["fp64_s_per_step"]),
+        "fp64": {"value": world * n / fp64_s, "unit": UNIT, "ms_per_step": 1e3 * fp64_s,
+                 "stage_ms": fp64_stages},
+        "speedup_vs_fp64_gpu": fp64_s / (el / args.steps),
         "accuracy": acc,
+        "orders": {str(k): orders[k] for k in sorted(orders)},
         "stage_ms": stage_ms,
         "tree": info, "stats": stats,
         "roofline": roof,
@@ -521,14 +678,7 @@ def run_gpu(args):
         "gpu_launches": launches,
     }
     if args.serving_requests > 0:
-        reqs = serving_stream(args.serving_requests, args.serving_rate)
-        line["serving"] = {
-            "stream": (f"{args.serving_requests} Poisson arrivals at {args.serving_rate}/s, N "
-                       "log-uniform [1e3, 2e6], p in {6,10,16}, half uniform / half Plummer, "
-                       "4 slots, 150 GB HBM admission budget"),
-            "mixed": run_serving(reqs, "mixed"),
-            "fp64": run_serving(reqs, "fp64"),
-        }
+        line["serving"] = run_serving_suite(args.serving_requests, args.serving_rate)
     if args.batched_2d_systems > 0 or args.batched_3d_systems > 0:
         line["batched"] = {}
         if args.batched_2d_systems > 0:
@@ -536,8 +686,7 @@ def run_gpu(args):
         if args.batched_3d_systems > 0:
             line["batched"]["3d"] = run_batched_3d(args.batched_3d_systems)
     if args.cpu_baseline:
-        procs = args.cpu_procs or os.cpu_count() or 1
-        line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_sample, procs)
+        line["cpu_baseline"] = cpu_baseline(x, q, args.workload, max_solves=1)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
@@ -549,16 +698,18 @@ def run_reference(args):
     if rank != 0:
         return
     gen, n, p, maxbox, lb, ub, desc = WORKLOADS[args.workload]
-    procs = args.cpu_procs or os.cpu_count() or 1
-    for _ in range(args.warmup if args.ref_warmup else 0):
-        cpu_baseline(args.workload, max(2000, args.cpu_sample // 10), procs)
-    res = cpu_baseline(args.workload, args.cpu_sample, procs, rounds=args.steps)
+    x, q = make_workload(args.workload)
+    res = cpu_baseline(x, q, args.workload, max_solves=args.steps, budget_s=args.ref_budget_s)
     line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": UNIT,
-            "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "description": desc, "order": p,
-                       "maxbox": maxbox, "flavour": "rotate", "precision": "fp64 (reference)"},
+            "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": res["solves"],
+            "warmup": 0, "ms_per_step": 1e3 * res["s_per_solve"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "description": desc, "n_per_gpu": n,
+                       "order": p, "maxbox": maxbox, "flavour": "rotate",
+                       "precision": "fp64 (reference algorithm)",
+                       "steps_requested": args.steps,
+                       "steps_note": ("full solves of the whole workload until --steps of them "
+                                      f"or {args.ref_budget_s:.0f} s of wall time")},
             "cpu_baseline": res,
             "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -574,17 +725,18 @@ def main():
     ap.add_argument("--workload", default="plummer4m", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--direct-targets", type=int, default=1000)
+    ap.add_argument("--orders", default="8,16",
+                    help="other orders of the workload to run (mixed and FP64), comma-separated")
+    ap.add_argument("--direct-targets", type=int, default=10000)
     ap.add_argument("--cpu-baseline", type=int, default=1)
-    ap.add_argument("--cpu-sample", type=int, default=20000)
-    ap.add_argument("--cpu-procs", type=int, default=0)
-    ap.add_argument("--ref-warmup", type=int, default=0)
+    ap.add_argument("--ref-budget-s", type=float, default=150.0,
+                    help="--impl reference: wall-time budget for full CPU solves")
     ap.add_argument("--serving-requests", type=int, default=48)
     ap.add_argument("--serving-rate", type=float, default=16.0)
     ap.add_argument("--batched-2d-systems", type=int, default=512)
-    ap.add_argument("--batched-3d-systems", type=int, default=512)
+    ap.add_argument("--batched-3d-systems", type=int, default=2048)
     ap.add_argument("--m2l-traffic", type=float, default=None,
-                    help="dram bytes per M2L launch from an ncu capture (profiles/)")
+                    help="DRAM bytes of one M2L launch from an ncu capture of this workload")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -46,4 +46,13 @@ struct _GSList
 
 typedef void (*GFunc) (gpointer data, gpointer user_data);
 
+/* orders of a tree traversal (glib's GTraverseType) */
+typedef enum
+{
+  G_IN_ORDER,
+  G_PRE_ORDER,
+  G_POST_ORDER,
+  G_LEVEL_ORDER
+} GTraverseType;
+
 #endif

@@ -80,8 +80,63 @@ gboolean aran_solver3d_remove_point (AranSolver3d *solver, VsgPoint3 point);
 void aran_solver3d_foreach_point (AranSolver3d *solver, GFunc func, gpointer user_data);
 void aran_solver3d_solve (AranSolver3d *solver);
 /* the semifar threshold used when set_functions_full was given 0
- * (aran/aransolver3d.c:1090-1127); G_MAXUINT without p2l/m2p */
+ * (aran/aransolver3d.c:1090-1127): (p2l + m2p) / p2p of the operator costs
+ * set by aran_solver3d_db_profile_operators or _profile_operators; G_MAXUINT
+ * without p2l/m2p or without costs */
 guint aran_solver3d_optimal_semifar_threshold (AranSolver3d *solver);
+
+/* aran/aransolver3d.c:663-685; like the reference, *p2p is not written */
+void aran_solver3d_get_functions_full (AranSolver3d *solver, AranParticle2ParticleFunc3d *p2p,
+                                       AranParticle2MultipoleFunc3d *p2m,
+                                       AranMultipole2MultipoleFunc3d *m2m,
+                                       AranMultipole2LocalFunc3d *m2l, AranLocal2LocalFunc3d *l2l,
+                                       AranLocal2ParticleFunc3d *l2p, AranParticle2LocalFunc3d *p2l,
+                                       AranMultipole2ParticleFunc3d *m2p,
+                                       guint *semifar_threshold);
+/* operator costs of the registered callbacks from the profile database
+ * (aran_profile_db_address_eval at `order`, p2p at 0; as the reference,
+ * aran/aransolver3d.c:687-740, the l2p cost is looked up under the p2p
+ * address), printed to stderr */
+void aran_solver3d_db_profile_operators (AranSolver3d *solver, gdouble order);
+/* operator costs measured on the GPU (aran/aransolver3d.c:742-770 times
+ * the callbacks on the host): a calibration solve of the solver's
+ * configuration with semifar interactions on, each stage's CUDA-event time
+ * divided by its operation count (p2p per directed pair, p2m/l2p per
+ * particle, m2m/l2l per node, m2l per translation, p2l/m2p per particle).
+ * point_init, p1 and p2 are accepted for source compatibility and unused. */
+void aran_solver3d_profile_operators (AranSolver3d *solver, AranParticleInitFunc3d point_init,
+                                      gpointer p1, gpointer p2);
+/* serial: the same as aran_solver3d_insert_point; TRUE */
+gboolean aran_solver3d_insert_point_local (AranSolver3d *solver, VsgPoint3 point);
+/* a point whose position (the VsgVector3d at the start of the point) lies
+ * within the tolerance (aran_solver3d_set_tolerance; 0: the same position)
+ * of the selector's, or NULL (aran/aransolver3d.c:1024-1030) */
+VsgPoint3 aran_solver3d_find_point (AranSolver3d *solver, VsgPoint3 selector);
+/* func on every point for which locfunc (selector, point) returns
+ * VSG_RLOC3_MASK, in tree order (aran/aransolver3d.c:1077-1088) */
+void aran_solver3d_foreach_point_custom (AranSolver3d *solver, VsgRegion3 selector,
+                                         VsgRegion3Point3LocFunc locfunc, GFunc func,
+                                         gpointer user_data);
+/* func on every node of the tree of the inserted points, in the given order
+ * (G_IN_ORDER: first child, node, other children, as glib's n-ary trees)
+ * (aran/aransolver3d.c:1057-1066).  The tree is the one the GPU builds;
+ * user_data is the node's development (after a solve with the same points:
+ * its multipole and local expansions, else zero); point_list holds a leaf's
+ * points.  The node infos live for the duration of the call. */
+void aran_solver3d_traverse (AranSolver3d *solver, GTraverseType order, VsgPRTree3dFunc func,
+                             gpointer user_data);
+/* children visited in Hilbert-curve order (J. Skilling's transpose
+ * algorithm) or in the default octant order x + 2y + 4z by
+ * aran_solver3d_traverse and foreach_point_custom; solve results do not
+ * depend on it (aran/aransolver3d.c:1204-1217) */
+void aran_solver3d_set_children_order_hilbert (AranSolver3d *solver);
+void aran_solver3d_set_children_order_default (AranSolver3d *solver);
+/* virtual leaves (aran/aransolver3d.c:1272-1279): a node about to be split
+ * stays a leaf of the near/far interactions when isleaf (node_info,
+ * user_data) is TRUE; node_info carries center, bounds, point_count and
+ * depth.  See aran_gpu_solver3d_set_leaf_predicate. */
+void aran_solver3d_set_nf_isleaf (AranSolver3d *solver, VsgPRTree3dNFIsleafFunc isleaf,
+                                  gpointer user_data);
 
 /* Additive: where the Newton data sits in the caller's point struct
  * (position: VsgVector3d at pos_offset, charge: gdouble at charge_offset,

@@ -108,12 +108,39 @@ int aran_gpu_solver3d_expansions (AranGpuSolver3d *s, double *mult,
                                   double *local);
 
 /* Stage times of the last solve in ms (CUDA events on the solve stream):
- * [0] total, [1] keys+sort, [2] tree, [3] lists, [4] p2m, [5] m2m, [6] m2l,
- * [7] l2l, [8] l2p, [9] p2p (its own stream), [10] h2d, [11] d2h. */
+ * [0] total, [1] keys+sort, [2] tree, [3] lists, [4] p2m, [5] m2m, [6] m2l
+ * (semifar P2L included), [7] l2l, [8] l2p (semifar M2P included), [9] p2p
+ * (its own stream), [10] h2d, [11] d2h, [12] semifar p2l, [13] semifar m2p. */
 int aran_gpu_solver3d_timings (AranGpuSolver3d *s, double ms[16]);
 
 /* Number of GPU kernel launches issued by the last solve. */
 int64_t aran_gpu_solver3d_launches (AranGpuSolver3d *s);
+
+/* The view of a tree node a leaf predicate receives. */
+typedef struct
+{
+  double center[3];
+  double lbound[3];
+  double ubound[3];
+  int64_t point_count;   /* particles below the node */
+  int depth;
+} AranGpuNodeView;
+
+/* Returns non-zero when a node that holds more than maxbox particles is to be
+ * a leaf all the same (a "virtual leaf": its particles take P2P as one leaf
+ * and no M2L runs below it). */
+typedef int (*AranGpuLeafPredicate) (const AranGpuNodeView *node, void *user_data);
+
+/* Sets (pred != NULL) or clears the leaf predicate: while the tree of a solve
+ * is subdivided level by level, every node about to be split is shown to
+ * pred and stays a leaf when it answers non-zero.  Replaces the near/far
+ * traversal's is-leaf callback of aran_solver3d_set_nf_isleaf
+ * (aran/aransolver3d.c:1272-1279, libvsg's vsg_prtree3d_set_nf_isleaf): the
+ * reference keeps the nodes below a virtual leaf for its up and down passes,
+ * here they are not made, which changes only the rounding (M2M and L2L are
+ * exact on truncated expansions) and the zero/m2m/l2l counters. */
+int aran_gpu_solver3d_set_leaf_predicate (AranGpuSolver3d *s, AranGpuLeafPredicate pred,
+                                          void *user_data);
 
 /* Mixed precision only: nodes of depth <= depth keep FP64 expansions, so
  * M2M into them and M2L and L2L at them run in FP64 (the coarse levels,
@@ -154,6 +181,10 @@ typedef struct
   const double *q;     /* host, n */
   double *pot;         /* host, n (or NULL) */
   double *field;       /* host, 3n (or NULL) */
+  double tolerance;    /* > 0: requested relative L2 error of the potential
+                          against the direct sum; the server then picks
+                          cfg.precision, and cfg.order too when it is 0
+                          (aran_gpu_plan_for_tolerance).  <= 0: cfg as given */
 } AranGpuRequest3d;
 
 typedef struct
@@ -164,7 +195,18 @@ typedef struct
   double end_s;
   int slot;
   int64_t footprint_bytes;
+  int order;           /* order and precision the request ran at */
+  int precision;
 } AranGpuRequestInfo;
+
+/* Picks the cheapest (order, precision) whose relative L2 potential error
+ * against the FP64 direct sum, measured on GB300 over uniform and Plummer
+ * draws of 2e4-3e5 particles at leaf capacity 64, is at most tol / 2:
+ * mixed precision wherever it reaches that, FP64 otherwise.  cfg->order > 0
+ * keeps the order and picks only the precision.  Returns the table's error
+ * estimate for the pick (tolerances below what order 30 in FP64 reaches get
+ * order 30, FP64, and an estimate above tol / 2). */
+double aran_gpu_plan_for_tolerance (double tol, AranGpuConfig3d *cfg);
 
 typedef struct AranGpuServer AranGpuServer;
 

@@ -40,7 +40,23 @@ struct _VsgPRTree3dNodeInfo
   guint id;
 };
 
+/* Serial trees share no node with another process. */
+#define VSG_PRTREE3D_NODE_INFO_IS_SHARED(node_info) (FALSE)
+
+/* Octant mask: bit o set when a region reaches octant o (x + 2y + 4z, a bit
+ * set on the upper side) around a point; all eight bits: the region
+ * surrounds the point. */
+typedef guint8 vsgrloc3;
+#define VSG_RLOC3_MASK ((vsgrloc3) 0xff)
+
 typedef gint (*VsgPoint3dLocFunc) (const VsgPoint3 candidate, const VsgVector3d *center);
+/* where a region lies around a point, as an octant mask */
+typedef vsgrloc3 (*VsgRegion3Point3LocFunc) (const VsgRegion3 region, const VsgPoint3 point);
+/* node visitor of aran_solver3d_traverse */
+typedef void (*VsgPRTree3dFunc) (const VsgPRTree3dNodeInfo *node_info, gpointer user_data);
+/* near/far traversal's is-leaf callback (aran_solver3d_set_nf_isleaf) */
+typedef gboolean (*VsgPRTree3dNFIsleafFunc) (const VsgPRTree3dNodeInfo *node_info,
+                                             gpointer user_data);
 typedef gdouble (*VsgPoint3dDistFunc) (const VsgPoint3 one, const VsgPoint3 other);
 typedef gint (*VsgRegion3dLocFunc) (const VsgRegion3 region, const VsgVector3d *center);
 

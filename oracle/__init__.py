@@ -83,6 +83,8 @@ def lib():
         L.or_wigner.argtypes = [C.c_double] * 3 + [C.c_int, dp]
         L.or_solve.restype = C.c_int
         L.or_solve.argtypes = [C.c_void_p, dp, dp, dp, dp, i64p]
+        L.or_set_leaf_predicate.restype = None
+        L.or_set_leaf_predicate.argtypes = [C.c_void_p, C.c_void_p]
         L.or_solve_threaded.restype = C.c_int
         L.or_solve_threaded.argtypes = [C.c_void_p, dp, dp, dp, dp, i64p, C.c_int]
         L.or_tree_lists.restype = C.c_int
@@ -102,6 +104,30 @@ def lib():
         L.or2_direct.argtypes = [C.c_int, dp, dp, C.c_int, i32p, dp]
         _lib = L
     return _lib
+
+
+class NodeView(C.Structure):
+    """OrNodeView: a node about to be split, as a leaf predicate sees it."""
+    _fields_ = [("center", C.c_double * 3), ("lbound", C.c_double * 3),
+                ("ubound", C.c_double * 3), ("point_count", C.c_int64), ("depth", C.c_int)]
+
+
+LEAF_PREDICATE = C.CFUNCTYPE(C.c_int, C.POINTER(NodeView), C.c_void_p)
+
+
+class leaf_predicate:
+    """Context manager: tree builds inside it keep as leaves the nodes for
+    which fn(node_view) is true (virtual leaves)."""
+
+    def __init__(self, fn):
+        self._cb = LEAF_PREDICATE(lambda v, _d: int(bool(fn(v.contents))))
+
+    def __enter__(self):
+        lib().or_set_leaf_predicate(C.cast(self._cb, C.c_void_p), None)
+        return self
+
+    def __exit__(self, *a):
+        lib().or_set_leaf_predicate(None, None)
 
 
 class SolveConfig(C.Structure):

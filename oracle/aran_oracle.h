@@ -90,6 +90,24 @@ typedef struct
  * m2p, p2p_remote, m2l_remote. */
 #define OR_NSTATS 11
 
+/* A node about to be split, as a leaf predicate sees it. */
+typedef struct
+{
+  double center[3];
+  double lbound[3];
+  double ubound[3];
+  int64_t point_count;
+  int depth;
+} OrNodeView;
+
+/* Non-zero keeps the node as a leaf ("virtual leaf" of the near/far
+ * traversal, aran_solver3d_set_nf_isleaf, aran/aransolver3d.c:1272-1279). */
+typedef int (*OrLeafPredicate) (const OrNodeView *node, void *user_data);
+
+/* Sets (or clears, with NULL) the leaf predicate of every later tree build;
+ * process-global, for the tests. */
+void or_set_leaf_predicate (OrLeafPredicate pred, void *user_data);
+
 /* Builds the tree, runs the solve, writes potential (n) or field (3n). */
 int or_solve (const OrSolveConfig *cfg, const double *xyz, const double *q,
               double *pot, double *field, int64_t stats[OR_NSTATS]);

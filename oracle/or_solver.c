@@ -138,6 +138,42 @@ static int push_node (OrTree *t)
   return t->nn++;
 }
 
+static OrLeafPredicate g_leaf_pred = NULL;
+static void *g_leaf_data = NULL;
+
+void or_set_leaf_predicate (OrLeafPredicate pred, void *user_data)
+{
+  g_leaf_pred = pred;
+  g_leaf_data = user_data;
+}
+
+/* a node the predicate keeps as a leaf; its cell by halving the root box */
+static int virtual_leaf (const OrSolveConfig *cfg, const OrNode *nd)
+{
+  OrNodeView v;
+  int a, b;
+  if (!g_leaf_pred)
+    return 0;
+  for (a = 0; a < 3; a++)
+    {
+      double lo = cfg->lb[a], hi = cfg->ub[a];
+      for (b = nd->depth - 1; b >= 0; b--)
+        {
+          double mid = (lo + hi) * 0.5;
+          if ((nd->ijk[a] >> b) & 1)
+            lo = mid;
+          else
+            hi = mid;
+        }
+      v.lbound[a] = lo;
+      v.ubound[a] = hi;
+      v.center[a] = (lo + hi) * 0.5;
+    }
+  v.point_count = nd->end - nd->begin;
+  v.depth = nd->depth;
+  return g_leaf_pred (&v, g_leaf_data) != 0;
+}
+
 static void tree_build (OrTree *t, const OrSolveConfig *cfg,
                         const double *xyz)
 {
@@ -186,7 +222,7 @@ static void tree_build (OrTree *t, const OrSolveConfig *cfg,
         {
           OrNode *nd = &t->nodes[nb];
           int c, pos;
-          if (nd->end - nd->begin <= cfg->maxbox || d >= maxd)
+          if (nd->end - nd->begin <= cfg->maxbox || d >= maxd || virtual_leaf (cfg, nd))
             {
               nd->leaf = 1;
               for (c = 0; c < 8; c++)

@@ -154,3 +154,80 @@ def test_cauchy_program(exe2d, n, order, maxbox, dist, tol):
     assert v["p2l"] < 1e-9, out
     assert v["host_calls"] == 0
     assert v["p2m"] == n and v["l2p"] == n and v["p2p"] > 0
+
+
+API_SRC = os.path.join(ROOT, "tests", "c", "solver_api.c")
+
+PROFILE_INI = """# profile database of the API test
+[aran-profile]
+aran_development3d_m2l_rotate=1e-7;2e-7;3e-8;
+samples-aran_development3d_m2l_rotate=5:5e-06;6:6e-06;
+aran_development3d_p2l=4e-6;
+aran_development3d_m2pv=2e-6;
+[other]
+aran_development3d_m2l_rotate=9;
+"""
+
+
+@pytest.fixture(scope="module")
+def api_exe(tmp_path_factory):
+    return compile_c(tmp_path_factory, API_SRC, "solver_api")
+
+
+def test_solver_api_host(api_exe, tmp_path):
+    """get_functions_full (p2p left unwritten, as the reference), find_point
+    with and without a tolerance, insert_point_local, the profile database
+    read from $ARAN_PROFILE_DB: no GPU needed."""
+    ini = tmp_path / "profiledb.ini"
+    ini.write_text(PROFILE_INI)
+    env = dict(os.environ, ARAN_PROFILE_DB=str(ini))
+    r = subprocess.run([api_exe, "host"], capture_output=True, text=True, timeout=120, env=env)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
+    # the costs db_profile_operators printed (aran/aransolver3d.c:731-738 format)
+    assert re.search(r"db_m2l_time 0x[0-9a-f]+ = 6e-06", r.stderr), r.stderr
+    assert re.search(r"db_p2l_time 0x[0-9a-f]+ = 4e-06", r.stderr), r.stderr
+
+
+@pytest.mark.gpu
+def test_solver_api_gpu(api_exe):
+    """traverse in the four orders on the GPU tree, Hilbert children order,
+    foreach_point_custom, virtual leaves (set_nf_isleaf) against the tree of
+    the equivalent leaf capacity, GPU-timed operator costs."""
+    r = subprocess.run([api_exe, "gpu"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
+
+
+REF_PROFILE_DB = "/root/reference/tests/profiledb-test.ini"
+
+
+@pytest.mark.skipif(not os.path.exists(REF_PROFILE_DB), reason="reference tree not mounted")
+def test_reference_profile_db_fixture():
+    """The reference's own fixture read by the C library with the lookups of
+    its tests/profiledb.c:79-134: by name and by operator address the same
+    entry, both evaluate to a number at 1; an unknown address gives NaN."""
+    import ctypes as C
+    import math
+    import aran_gb300
+    L = C.CDLL(aran_gb300.load()._name)
+    L.aran_profile_db_read_file.argtypes = [C.c_char_p, C.c_char_p]
+    L.aran_profile_db_get_by_name.argtypes = [C.c_char_p]
+    L.aran_profile_db_get_by_name.restype = C.c_void_p
+    L.aran_profile_db_get_by_address.argtypes = [C.c_void_p]
+    L.aran_profile_db_get_by_address.restype = C.c_void_p
+    L.aran_profile_db_name_eval.argtypes = [C.c_char_p, C.c_double]
+    L.aran_profile_db_name_eval.restype = C.c_double
+    L.aran_profile_db_address_eval.argtypes = [C.c_void_p, C.c_double]
+    L.aran_profile_db_address_eval.restype = C.c_double
+    L.aran_profile_db_set_verbose(0)
+    assert L.aran_profile_db_read_file(REF_PROFILE_DB.encode(), None) == 1
+    for name in ("aran_development2d_m2m", "aran_development2d_m2l", "aran_development2d_l2l",
+                 "aran_development3d_m2m", "aran_development3d_m2l", "aran_development3d_l2l"):
+        addr = C.cast(getattr(L, name), C.c_void_p).value
+        p1 = L.aran_profile_db_get_by_name(name.encode())
+        p2 = L.aran_profile_db_get_by_address(addr)
+        assert p1 is not None and p1 == p2, name
+        x = L.aran_profile_db_name_eval(name.encode(), 1.0)
+        assert not math.isnan(x), name
+        assert L.aran_profile_db_address_eval(addr, 1.0) == x, name
+    bad = C.c_int(0)
+    assert math.isnan(L.aran_profile_db_address_eval(C.addressof(bad), 1.0))
