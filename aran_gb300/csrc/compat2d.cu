@@ -10,7 +10,9 @@
 // same order (aranlaurentseriesd.c:47-73,311-452; arandevelopment2d.c:167-221).
 // aran_solver2d_solve runs the forest solver of solver2d.cu on one system.
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <cstdio>
 #include <complex>
 #include <cstdlib>
 #include <cstring>
@@ -20,6 +22,7 @@
 
 #include "internal.cuh"
 
+#include <aran/aranprofiledb.h>
 #include <aran/aransolver2d.h>
 
 struct _AranLaurentSeriesd {
@@ -54,6 +57,14 @@ struct _AranSolver2d {
   AranGpuConfig2d gpu_cfg;
   int64_t stats[11] = {};
   guint depth = 0;
+  // virtual leaves, children order, operator costs (< 0: unknown), and
+  // whether the last solve ran on exactly the current points
+  VsgPRTree2dNFIsleafFunc nf_isleaf = nullptr;
+  gpointer nf_isleaf_data = nullptr;
+  bool hilbert = false;
+  double p2p_time = -1, p2m_time = -1, p2l_time = -1, l2p_time = -1, m2p_time = -1,
+         m2m_time = -1, m2l_time = -1, l2l_time = -1;
+  bool solved_current = false;
 };
 
 namespace aran {
@@ -439,6 +450,84 @@ gcomplex128 aran_development2d_l2p(const VsgPRTree2dNodeInfo *devel_node, AranDe
 }
 
 // ---- 2D solver (aran/aransolver2d.c) ----
+namespace {
+
+int leaf_pred2(const AranGpuNodeView *v, void *data) {
+  AranSolver2d *s = (AranSolver2d *)data;
+  VsgPRTree2dNodeInfo info;
+  std::memset(&info, 0, sizeof(info));
+  info.center = {v->center[0], v->center[1]};
+  info.lbound = {v->lbound[0], v->lbound[1]};
+  info.ubound = {v->ubound[0], v->ubound[1]};
+  info.point_count = (guint)v->point_count;
+  info.depth = (guint)v->depth;
+  return s->nf_isleaf(&info, s->nf_isleaf_data) ? 1 : 0;
+}
+
+// the GPU solver of the solver's order and leaf capacity, with its
+// virtual-leaf predicate
+int gpu_solver2(AranSolver2d *solver) {
+  AranGpuConfig2d cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.maxbox = (int)solver->tree->maxbox;
+  cfg.order = solver->devel->multipole->negdeg;
+  cfg.max_depth = 0;
+  if (!solver->gpu || std::memcmp(&cfg, &solver->gpu_cfg, sizeof(cfg)) != 0) {
+    if (solver->gpu) aran_gpu_solver2d_destroy(solver->gpu);
+    solver->gpu = nullptr;
+    solver->solved_current = false;
+    int rc = aran_gpu_solver2d_create(&cfg, &solver->gpu);
+    if (rc != ARAN_OK) return rc;
+    solver->gpu_cfg = cfg;
+  }
+  return aran_gpu_solver2d_set_leaf_predicate(solver->gpu, solver->nf_isleaf ? leaf_pred2 : nullptr,
+                                              solver);
+}
+
+void gather2(AranSolver2d *solver, size_t off_pos, size_t off_q, std::vector<double> &xy,
+             std::vector<double> &q) {
+  const size_t n = solver->points.size();
+  xy.resize(2 * n);
+  q.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    const char *pt = (const char *)solver->points[i];
+    const VsgVector2d *v = (const VsgVector2d *)(pt + off_pos);
+    xy[2 * i] = v->x;
+    xy[2 * i + 1] = v->y;
+    q[i] = off_q == (size_t)-1 ? 0.0 : *(const double *)(pt + off_q);
+  }
+}
+
+// Hilbert index of cell (x, y) of a 2^bits grid (J. Skilling's transpose
+// algorithm, AIP Conf. Proc. 707 (2004) 381, for two axes)
+uint64_t hilbert2(uint32_t x, uint32_t y, int bits) {
+  uint32_t X[2] = {x, y};
+  const uint32_t M = 1u << (bits - 1);
+  for (uint32_t Q = M; Q > 1; Q >>= 1) {
+    const uint32_t P = Q - 1;
+    for (int i = 0; i < 2; ++i) {
+      if (X[i] & Q) X[0] ^= P;
+      else {
+        const uint32_t t = (X[0] ^ X[i]) & P;
+        X[0] ^= t;
+        X[i] ^= t;
+      }
+    }
+  }
+  X[1] ^= X[0];
+  uint32_t t = 0;
+  for (uint32_t Q = M; Q > 1; Q >>= 1)
+    if (X[1] & Q) t ^= Q - 1;
+  X[0] ^= t;
+  X[1] ^= t;
+  uint64_t h = 0;
+  for (int b = bits - 1; b >= 0; --b)
+    for (int i = 0; i < 2; ++i) h = (h << 1) | ((X[i] >> b) & 1u);
+  return h;
+}
+
+}  // namespace
+
 AranSolver2d *aran_solver2d_new(VsgPRTree2d *prtree, GType devel_type, gpointer devel,
                                 AranZeroFunc zero) {
   AranSolver2d *s = new AranSolver2d();
@@ -533,7 +622,15 @@ guint aran_solver2d_point_count(const AranSolver2d *solver) {
 }
 
 void aran_solver2d_insert_point(AranSolver2d *solver, VsgPoint2 point) {
-  if (solver && point) solver->points.push_back(point);
+  if (!solver || !point) return;
+  solver->points.push_back(point);
+  solver->solved_current = false;
+}
+
+gboolean aran_solver2d_insert_point_local(AranSolver2d *solver, VsgPoint2 point) {
+  if (!solver || !point) return FALSE;
+  aran_solver2d_insert_point(solver, point);
+  return TRUE;
 }
 
 gboolean aran_solver2d_remove_point(AranSolver2d *solver, VsgPoint2 point) {
@@ -541,6 +638,7 @@ gboolean aran_solver2d_remove_point(AranSolver2d *solver, VsgPoint2 point) {
   for (size_t i = 0; i < solver->points.size(); ++i)
     if (solver->points[i] == point) {
       solver->points.erase(solver->points.begin() + i);
+      solver->solved_current = false;
       return TRUE;
     }
   return FALSE;
@@ -578,31 +676,16 @@ int aran_solver2d_solve_try(AranSolver2d *solver) {
                 "aran_solver2d_solve: m2m/m2l/l2l must be aran_development2d_m2m/m2l/l2l");
   const int64_t n = (int64_t)solver->points.size();
   if (n == 0) return ARAN_OK;
-  AranGpuConfig2d cfg;
-  std::memset(&cfg, 0, sizeof(cfg));
-  cfg.maxbox = (int)solver->tree->maxbox;
-  cfg.order = solver->devel->multipole->negdeg;
-  cfg.max_depth = 0;
-  if (!solver->gpu || std::memcmp(&cfg, &solver->gpu_cfg, sizeof(cfg)) != 0) {
-    if (solver->gpu) aran_gpu_solver2d_destroy(solver->gpu);
-    solver->gpu = nullptr;
-    int rc = aran_gpu_solver2d_create(&cfg, &solver->gpu);
-    if (rc != ARAN_OK) return rc;
-    solver->gpu_cfg = cfg;
-  }
-  std::vector<double> xy(2 * n), q(n), acc(2 * n);
-  for (int64_t i = 0; i < n; ++i) {
-    const char *pt = (const char *)solver->points[i];
-    const VsgVector2d *v = (const VsgVector2d *)(pt + solver->off_pos);
-    xy[2 * i] = v->x;
-    xy[2 * i + 1] = v->y;
-    q[i] = *(const double *)(pt + solver->off_q);
-  }
+  int rc = gpu_solver2(solver);
+  if (rc != ARAN_OK) return rc;
+  std::vector<double> xy, q, acc(2 * n);
+  gather2(solver, solver->off_pos, solver->off_q, xy, q);
   int64_t offs[2] = {0, n};
   double box[4] = {solver->tree->lb.x, solver->tree->lb.y, solver->tree->ub.x, solver->tree->ub.y};
-  int rc = aran_gpu_solver2d_solve(solver->gpu, 1, offs, box, xy.data(), q.data(), acc.data(),
-                                   ARAN_MEM_HOST);
+  rc = aran_gpu_solver2d_solve(solver->gpu, 1, offs, box, xy.data(), q.data(), acc.data(),
+                               ARAN_MEM_HOST);
   if (rc != ARAN_OK) return rc;
+  solver->solved_current = true;
   for (int64_t i = 0; i < n; ++i) {
     double *a = (double *)((char *)solver->points[i] + solver->off_acc);  // gcomplex128: re, im
     a[0] += acc[2 * i];
@@ -617,5 +700,248 @@ int aran_solver2d_solve_try(AranSolver2d *solver) {
 }
 
 void aran_solver2d_solve(AranSolver2d *solver) { (void)aran_solver2d_solve_try(solver); }
+
+void aran_solver2d_get_functions_full(AranSolver2d *solver, AranParticle2ParticleFunc2d *p2p,
+                                      AranParticle2MultipoleFunc2d *p2m,
+                                      AranMultipole2MultipoleFunc2d *m2m,
+                                      AranMultipole2LocalFunc2d *m2l, AranLocal2LocalFunc2d *l2l,
+                                      AranLocal2ParticleFunc2d *l2p,
+                                      AranParticle2LocalFunc2d *p2l,
+                                      AranMultipole2ParticleFunc2d *m2p,
+                                      guint *semifar_threshold) {
+  (void)p2p;   // not written, like the 3D twin (aran/aransolver3d.c:676-684)
+  if (!solver) return;
+  if (p2m) *p2m = solver->p2m;
+  if (m2m) *m2m = solver->m2m;
+  if (m2l) *m2l = solver->m2l;
+  if (l2l) *l2l = solver->l2l;
+  if (l2p) *l2p = solver->l2p;
+  if (p2l) *p2l = solver->p2l;
+  if (m2p) *m2p = solver->m2p;
+  if (semifar_threshold) *semifar_threshold = solver->semifar_threshold;
+}
+
+void aran_solver2d_db_profile_operators(AranSolver2d *solver, gdouble order) {
+  if (!solver) return;
+  if (solver->p2p) solver->p2p_time = aran_profile_db_address_eval((gpointer)solver->p2p, 0.);
+  if (solver->p2m) solver->p2m_time = aran_profile_db_address_eval((gpointer)solver->p2m, order);
+  if (solver->p2l) solver->p2l_time = aran_profile_db_address_eval((gpointer)solver->p2l, order);
+  if (solver->l2p) solver->l2p_time = aran_profile_db_address_eval((gpointer)solver->p2p, order);
+  if (solver->m2p) solver->m2p_time = aran_profile_db_address_eval((gpointer)solver->m2p, order);
+  if (solver->m2m) solver->m2m_time = aran_profile_db_address_eval((gpointer)solver->m2m, order);
+  if (solver->m2l) solver->m2l_time = aran_profile_db_address_eval((gpointer)solver->m2l, order);
+  if (solver->l2l) solver->l2l_time = aran_profile_db_address_eval((gpointer)solver->l2l, order);
+  std::fprintf(stderr, "db_p2p_time %p = %g\n", (void *)solver->p2p, solver->p2p_time);
+  std::fprintf(stderr, "db_p2m_time %p = %g\n", (void *)solver->p2m, solver->p2m_time);
+  std::fprintf(stderr, "db_p2l_time %p = %g\n", (void *)solver->p2l, solver->p2l_time);
+  std::fprintf(stderr, "db_m2m_time %p = %g\n", (void *)solver->m2m, solver->m2m_time);
+  std::fprintf(stderr, "db_m2l_time %p = %g\n", (void *)solver->m2l, solver->m2l_time);
+  std::fprintf(stderr, "db_l2l_time %p = %g\n", (void *)solver->l2l, solver->l2l_time);
+  std::fprintf(stderr, "db_l2p_time %p = %g\n", (void *)solver->l2p, solver->l2p_time);
+  std::fprintf(stderr, "db_m2p_time %p = %g\n", (void *)solver->m2p, solver->m2p_time);
+}
+
+void aran_solver2d_profile_operators(AranSolver2d *solver, AranParticleInitFunc2d point_init,
+                                     gpointer p1, gpointer p2) {
+  (void)point_init;
+  (void)p1;
+  (void)p2;
+  if (!solver || !solver->devel || solver->devel->multipole->negdeg < 1) return;
+  AranGpuConfig2d cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.maxbox = (int)solver->tree->maxbox < 8 ? 8 : (int)solver->tree->maxbox;
+  cfg.order = solver->devel->multipole->negdeg;
+  const int64_t n = 100000;
+  std::vector<double> xy(2 * n), q(n, 1.0 / n), acc(2 * n);
+  uint64_t st = 0x9E3779B97F4A7C15ull;
+  auto u = [&]() {
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    return (double)(st >> 11) * (1.0 / 9007199254740992.0);
+  };
+  const VsgVector2d lb = solver->tree->lb, ub = solver->tree->ub;
+  for (int64_t i = 0; i < n; ++i) {
+    xy[2 * i] = lb.x + (ub.x - lb.x) * u();
+    xy[2 * i + 1] = lb.y + (ub.y - lb.y) * u();
+  }
+  AranGpuSolver2d *g = nullptr;
+  if (aran_gpu_solver2d_create(&cfg, &g) != ARAN_OK) return;
+  int64_t offs[2] = {0, n}, c[11];
+  double box[4] = {lb.x, lb.y, ub.x, ub.y}, ms[16];
+  bool ok = true;
+  for (int rep = 0; rep < 2 && ok; ++rep)
+    ok = aran_gpu_solver2d_solve(g, 1, offs, box, xy.data(), q.data(), acc.data(),
+                                 ARAN_MEM_HOST) == ARAN_OK;
+  ok = ok && aran_gpu_solver2d_timings(g, ms) == ARAN_OK &&
+       aran_gpu_solver2d_get_stats(g, c) == ARAN_OK;
+  aran_gpu_solver2d_destroy(g);
+  if (!ok) return;
+  auto per = [](double stage_ms, int64_t count) { return count > 0 ? 1e-3 * stage_ms / count : -1.0; };
+  solver->p2p_time = per(ms[9], c[1]);
+  solver->p2m_time = per(ms[4], c[2]);
+  solver->m2m_time = per(ms[5], c[3]);
+  solver->m2l_time = per(ms[6], c[4]);
+  solver->l2l_time = per(ms[7], c[5]);
+  solver->l2p_time = per(ms[8], c[6]);
+}
+
+guint aran_solver2d_optimal_semifar_threshold(AranSolver2d *solver) {
+  if (!solver) return G_MAXUINT;
+  if (solver->p2l_time < 0. || solver->m2p_time < 0. || !(solver->p2p_time > 0.))
+    return G_MAXUINT;
+  const double t = (solver->p2l_time + solver->m2p_time) / solver->p2p_time;
+  return t >= (double)G_MAXUINT ? G_MAXUINT : (guint)t;
+}
+
+void aran_solver2d_set_children_order_hilbert(AranSolver2d *solver) {
+  if (solver) solver->hilbert = true;
+}
+
+void aran_solver2d_set_children_order_default(AranSolver2d *solver) {
+  if (solver) solver->hilbert = false;
+}
+
+void aran_solver2d_set_nf_isleaf(AranSolver2d *solver, VsgPRTree2dNFIsleafFunc isleaf,
+                                 gpointer user_data) {
+  if (!solver) return;
+  solver->nf_isleaf = isleaf;
+  solver->nf_isleaf_data = user_data;
+  solver->solved_current = false;
+}
+
+void aran_solver2d_traverse(AranSolver2d *solver, GTraverseType order, VsgPRTree2dFunc func,
+                            gpointer user_data) {
+  if (!solver || !func || solver->points.empty() || !solver->devel) return;
+  if (gpu_solver2(solver) != ARAN_OK) return;
+  aran::Forest2dHost h;
+  const int64_t n = (int64_t)solver->points.size();
+  if (!solver->solved_current) {
+    std::vector<double> xy, q;
+    gather2(solver, 0, (size_t)-1, xy, q);
+    int64_t offs[2] = {0, n};
+    double box[4] = {solver->tree->lb.x, solver->tree->lb.y, solver->tree->ub.x,
+                     solver->tree->ub.y};
+    if (aran::solve2d_impl(solver->gpu, 1, offs, box, xy.data(), q.data(), nullptr,
+                           ARAN_MEM_HOST, true) != ARAN_OK)
+      return;
+  }
+  if (aran::forest2d_to_host(solver->gpu, h, solver->solved_current) != ARAN_OK) return;
+  const int nn = h.nnodes, p = h.p;
+  std::vector<VsgPRTree2dNodeInfo> info(nn);
+  std::vector<GSList> cells(n);
+  std::vector<AranDevelopment2d *> devs(nn, nullptr);
+  for (int i = 0; i < nn; ++i) {
+    VsgPRTree2dNodeInfo &f = info[i];
+    std::memset(&f, 0, sizeof(f));
+    f.center = {h.center[2 * (size_t)i], h.center[2 * (size_t)i + 1]};
+    const double *bx = h.sysbox.data() + 6 * (size_t)h.sys[i];
+    double lo[2], hi[2];
+    for (int a = 0; a < 2; ++a) {
+      lo[a] = bx[a];
+      hi[a] = bx[2 + a];
+      for (int b = h.depth[i] - 1; b >= 0; --b) {
+        const double mid = (lo[a] + hi[a]) * 0.5;
+        if ((h.ij[2 * (size_t)i + a] >> b) & 1) lo[a] = mid;
+        else hi[a] = mid;
+      }
+    }
+    f.lbound = {lo[0], lo[1]};
+    f.ubound = {hi[0], hi[1]};
+    f.point_count = (guint)(h.end[i] - h.begin[i]);
+    f.isleaf = h.child[i] < 0;
+    f.depth = h.depth[i];
+    f.id = (guint)i;
+    f.father_info = h.parent[i] >= 0 ? &info[h.parent[i]] : nullptr;
+    if (f.isleaf && h.end[i] > h.begin[i]) {
+      for (int k = h.begin[i]; k < h.end[i]; ++k) {
+        cells[k].data = solver->points[h.perm[k]];
+        cells[k].next = k + 1 < h.end[i] ? &cells[k + 1] : nullptr;
+      }
+      f.point_list = &cells[h.begin[i]];
+    }
+    // developments aran_development2d_new (0, p): multipole term z^-t and
+    // local term z^k of the node after a solve, zero before
+    AranDevelopment2d *d = aran_development2d_new(0, (guint8)p);
+    if (!h.mult.empty())
+      for (int t = 0; t <= p; ++t) {
+        const size_t k = ((size_t)i * (p + 1) + t) * 2;
+        *aran_laurent_seriesd_get_term(d->multipole, -t) = gcomplex128(h.mult[k], h.mult[k + 1]);
+        *aran_laurent_seriesd_get_term(d->local, t) = gcomplex128(h.loc[k], h.loc[k + 1]);
+      }
+    devs[i] = d;
+    f.user_data = d;
+  }
+  auto kids = [&](int i, int out[4]) {
+    for (int o = 0; o < 4; ++o) out[o] = h.child[i] + o;
+    if (solver->hilbert) {
+      uint64_t key[4];
+      for (int o = 0; o < 4; ++o) {
+        const int c = h.child[i] + o;
+        key[o] = hilbert2((uint32_t)h.ij[2 * (size_t)c], (uint32_t)h.ij[2 * (size_t)c + 1],
+                          h.depth[c]);
+      }
+      std::sort(out, out + 4,
+                [&](int a, int b) { return key[a - h.child[i]] < key[b - h.child[i]]; });
+    }
+  };
+  if (order == G_LEVEL_ORDER) {
+    std::vector<int> level{0}, next;
+    while (!level.empty()) {
+      next.clear();
+      for (int i : level) {
+        func(&info[i], user_data);
+        if (h.child[i] >= 0) {
+          int k[4];
+          kids(i, k);
+          next.insert(next.end(), k, k + 4);
+        }
+      }
+      level.swap(next);
+    }
+  } else {
+    std::vector<std::pair<int, int>> stack{{0, 0}};
+    std::vector<std::array<int, 4>> order_of(nn);
+    while (!stack.empty()) {
+      auto &top = stack.back();
+      const int i = top.first;
+      const bool leaf = h.child[i] < 0;
+      if (top.second == 0) {
+        if (!leaf) kids(i, order_of[i].data());
+        if (order == G_PRE_ORDER || (leaf && order == G_IN_ORDER)) func(&info[i], user_data);
+      }
+      if (leaf || top.second == 4) {
+        if (order == G_POST_ORDER) func(&info[i], user_data);
+        stack.pop_back();
+        continue;
+      }
+      if (order == G_IN_ORDER && top.second == 1) func(&info[i], user_data);
+      const int c = order_of[i][top.second++];
+      stack.push_back({c, 0});
+    }
+  }
+  for (auto *d : devs) aran_development2d_free(d);
+}
+
+void aran_solver2d_foreach_point_custom(AranSolver2d *solver, VsgRegion2 selector,
+                                        VsgRegion2Point2LocFunc locfunc, GFunc func,
+                                        gpointer user_data) {
+  if (!solver || !locfunc || !func) return;
+  struct Ctx {
+    VsgRegion2 sel;
+    VsgRegion2Point2LocFunc loc;
+    GFunc fn;
+    gpointer data;
+  } ctx{selector, locfunc, func, user_data};
+  aran_solver2d_traverse(
+      solver, G_PRE_ORDER,
+      [](const VsgPRTree2dNodeInfo *node, gpointer d) {
+        Ctx *c = (Ctx *)d;
+        if (!node->isleaf) return;
+        for (GSList *l = node->point_list; l; l = l->next)
+          if (c->loc(c->sel, l->data) == VSG_RLOC2_MASK) c->fn(l->data, c->data);
+      },
+      &ctx);
+}
 
 }  // extern "C"

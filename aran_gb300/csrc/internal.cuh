@@ -243,6 +243,19 @@ void copy_expansions(AranGpuSolver3d *s, double *mult, double *local);
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
+// solver2d.cu: a 2D solve, or only its forest (tree_only, acc unused); and a
+// host copy of the last forest (node arrays, permutation, per-node Laurent
+// multipole/local coefficients of the last solve as interleaved complex FP64)
+struct Forest2dHost {
+  int p = 0, nnodes = 0;
+  std::vector<int> begin, end, child, parent, sys, ij, perm;
+  std::vector<uint8_t> depth;
+  std::vector<double> center, sysbox, mult, loc;
+};
+int solve2d_impl(AranGpuSolver2d *s, int nsys, const int64_t *offs, const double *box,
+                 const double *xy, const double *q, double *acc, int mem, bool tree_only);
+int forest2d_to_host(AranGpuSolver2d *s, Forest2dHost &h, bool expansions);
+
 // poll limit of the M2L consumers' waits for a table copy: 2^20, or the
 // value of ARAN_DEBUG_WAIT_POLLS (a test sets it to 0 to make the wait give
 // up; copies already issued are still waited for with the full limit)

@@ -569,6 +569,10 @@ struct AranGpuSolver2d {
   int64_t stats[11] = {};
   double ms[16] = {};
   int64_t launches = 0;
+  // host predicate keeping nodes about to be split as leaves (virtual leaves)
+  AranGpuLeafPredicate leaf_pred = nullptr;
+  void *leaf_pred_data = nullptr;
+  std::vector<double> h_sysbox;   // per system: lbx, lby, ubx, uby, scale x, scale y
 };
 
 namespace aran {
@@ -614,6 +618,46 @@ int read_int(const int *d, cudaStream_t st) {
   return h;
 }
 
+// the nodes of one level about to be split are shown to the host leaf
+// predicate (z components 0); those it keeps as leaves lose their flag
+void leaf_predicate2(AranGpuSolver2d *s, int off, int cnt, int d, cudaStream_t st) {
+  std::vector<int> fl(cnt), b(cnt), e(cnt), ij(2 * (size_t)cnt), sys(cnt);
+  ACHECK(cudaMemcpyAsync(fl.data(), s->flags.ptr, cnt * sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaMemcpyAsync(b.data(), s->begin.ptr + off, cnt * sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaMemcpyAsync(e.data(), s->end.ptr + off, cnt * sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaMemcpyAsync(ij.data(), s->ij.ptr + 2 * (size_t)off, 2 * cnt * sizeof(int),
+                         cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaMemcpyAsync(sys.data(), s->nsys_.ptr + off, cnt * sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaStreamSynchronize(st));
+  bool changed = false;
+  for (int i = 0; i < cnt; ++i) {
+    if (!fl[i]) continue;
+    AranGpuNodeView v;
+    std::memset(&v, 0, sizeof(v));
+    const double *bx = s->h_sysbox.data() + 6 * (size_t)sys[i];
+    for (int a = 0; a < 2; ++a) {
+      double lo = bx[a], hi = bx[2 + a];
+      for (int bit = d - 1; bit >= 0; --bit) {
+        const double mid = (lo + hi) * 0.5;
+        if ((ij[2 * (size_t)i + a] >> bit) & 1) lo = mid;
+        else hi = mid;
+      }
+      v.lbound[a] = lo;
+      v.ubound[a] = hi;
+      v.center[a] = (lo + hi) * 0.5;
+    }
+    v.point_count = e[i] - b[i];
+    v.depth = d;
+    if (s->leaf_pred(&v, s->leaf_pred_data)) {
+      fl[i] = 0;
+      changed = true;
+    }
+  }
+  if (changed)
+    ACHECK(cudaMemcpyAsync(s->flags.ptr, fl.data(), cnt * sizeof(int), cudaMemcpyHostToDevice, st));
+  ACHECK(cudaStreamSynchronize(st));
+}
+
 void build_forest(AranGpuSolver2d *s, int nsys, const double *dxy, const double *dq) {
   cudaStream_t st = s->s0;
   const int TB = 256;
@@ -656,6 +700,7 @@ void build_forest(AranGpuSolver2d *s, int nsys, const double *dxy, const double 
     k2_flag<<<ceil_div(cnt, TB), TB, 0, st>>>(cnt, off, s->begin.ptr, s->end.ptr, s->cfg.maxbox, d,
                                                maxd, s->flags.ptr);
     s->launches++;
+    if (s->leaf_pred) leaf_predicate2(s, off, cnt, d, st);
     ACHECK(cudaMemsetAsync(s->flags.ptr + cnt, 0, sizeof(int), st));
     ex_scan(s, s->flags.ptr, pos, cnt + 1, st);
     int ninternal = read_int(pos + cnt, st);
@@ -921,9 +966,27 @@ void aran_gpu_solver2d_destroy(AranGpuSolver2d *s) {
 
 int aran_gpu_solver2d_solve(AranGpuSolver2d *s, int nsys, const int64_t *offs, const double *box,
                             const double *xy, const double *q, double *acc, int mem) {
+  if (!acc) return fail(ARAN_ERR_INVALID, "NULL argument");
+  return aran::solve2d_impl(s, nsys, offs, box, xy, q, acc, mem, false);
+}
+
+int aran_gpu_solver2d_set_leaf_predicate(AranGpuSolver2d *s, AranGpuLeafPredicate pred,
+                                         void *user_data) {
+  if (!s) return fail(ARAN_ERR_INVALID, "solver is NULL");
+  s->leaf_pred = pred;
+  s->leaf_pred_data = pred ? user_data : nullptr;
+  return ARAN_OK;
+}
+
+}  // extern "C"
+
+namespace aran {
+
+int solve2d_impl(AranGpuSolver2d *s, int nsys, const int64_t *offs, const double *box,
+                 const double *xy, const double *q, double *acc, int mem, bool tree_only) {
   if (!s) return fail(ARAN_ERR_INVALID, "solver is NULL");
   if (nsys < 1 || nsys > (1 << 21)) return fail(ARAN_ERR_INVALID, "nsys must be in [1, 2^21]");
-  if (!offs || !box || !xy || !q || !acc) return fail(ARAN_ERR_INVALID, "NULL argument");
+  if (!offs || !box || !xy || !q) return fail(ARAN_ERR_INVALID, "NULL argument");
   if (mem != ARAN_MEM_HOST && mem != ARAN_MEM_DEVICE) return fail(ARAN_ERR_INVALID, "bad mem kind");
   if (offs[0] != 0) return fail(ARAN_ERR_INVALID, "offs[0] must be 0");
   int empty = 0;
@@ -969,7 +1032,12 @@ int aran_gpu_solver2d_solve(AranGpuSolver2d *s, int nsys, const int64_t *offs, c
     }
     ACHECK(cudaEventRecord(s->ev[2 * Stage::H2D + 1], st));
     ACHECK(cudaEventRecord(s->ev[2 * Stage::SORT], st));
+    s->h_sysbox = sb;
     build_forest(s, nsys, dxy, dq);
+    if (tree_only) {
+      ACHECK(cudaStreamSynchronize(st));
+      return ARAN_OK;
+    }
     build_lists2(s);
     run_passes2(s, dacc);
     ACHECK(cudaEventRecord(s->ev[2 * Stage::D2H], st));
@@ -1012,6 +1080,51 @@ int aran_gpu_solver2d_solve(AranGpuSolver2d *s, int nsys, const int64_t *offs, c
   }
   return ARAN_OK;
 }
+
+int forest2d_to_host(AranGpuSolver2d *s, Forest2dHost &h, bool expansions) {
+  try {
+    ACHECK(cudaSetDevice(s->device));
+    const int nn = s->nnodes;
+    h.p = s->cfg.order;
+    h.nnodes = nn;
+    h.begin.resize(nn);
+    h.end.resize(nn);
+    h.child.resize(nn);
+    h.parent.resize(nn);
+    h.sys.resize(nn);
+    h.ij.resize(2 * (size_t)nn);
+    h.depth.resize(nn);
+    h.center.resize(2 * (size_t)nn);
+    h.perm.resize(s->n);
+    h.sysbox = s->h_sysbox;
+    ACHECK(cudaMemcpy(h.begin.data(), s->begin.ptr, nn * sizeof(int), cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(h.end.data(), s->end.ptr, nn * sizeof(int), cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(h.child.data(), s->child.ptr, nn * sizeof(int), cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(h.parent.data(), s->parent.ptr, nn * sizeof(int), cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(h.sys.data(), s->nsys_.ptr, nn * sizeof(int), cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(h.ij.data(), s->ij.ptr, 2 * (size_t)nn * sizeof(int), cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(h.depth.data(), s->depth.ptr, nn, cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(h.center.data(), s->center.ptr, 2 * (size_t)nn * sizeof(double),
+                      cudaMemcpyDeviceToHost));
+    ACHECK(cudaMemcpy(h.perm.data(), s->perm.ptr, s->n * sizeof(int), cudaMemcpyDeviceToHost));
+    h.mult.clear();
+    h.loc.clear();
+    if (expansions) {
+      const size_t len = (size_t)nn * (h.p + 1) * 2;
+      h.mult.resize(len);
+      h.loc.resize(len);
+      ACHECK(cudaMemcpy(h.mult.data(), s->mult.ptr, len * sizeof(double), cudaMemcpyDeviceToHost));
+      ACHECK(cudaMemcpy(h.loc.data(), s->loc.ptr, len * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+  } catch (const CudaError &ce) {
+    return from_cuda(ce);
+  }
+  return ARAN_OK;
+}
+
+}  // namespace aran
+
+extern "C" {
 
 int aran_gpu_solver2d_get_stats(AranGpuSolver2d *s, int64_t stats[11]) {
   if (!s || !stats) return fail(ARAN_ERR_INVALID, "NULL argument");

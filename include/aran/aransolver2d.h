@@ -69,6 +69,40 @@ gboolean aran_solver2d_remove_point (AranSolver2d *solver, VsgPoint2 point);
 void aran_solver2d_foreach_point (AranSolver2d *solver, GFunc func, gpointer user_data);
 void aran_solver2d_solve (AranSolver2d *solver);
 
+/* The rest of aran/aransolver2d.h (serial), with the meaning of the 3D twins
+ * in aran/aransolver3d.h: get_functions_full leaves *p2p unwritten;
+ * db_profile_operators reads the costs of the registered operators from the
+ * profile database (the l2p cost under the p2p address);
+ * profile_operators times them on the GPU (a calibration solve of 100,000
+ * uniform particles in the tree's box; p2l/m2p stay unknown: the 2D GPU
+ * path has no semifar pass); the optimal semifar threshold is
+ * (p2l + m2p) / p2p of those costs, G_MAXUINT while one is unknown;
+ * foreach_point_custom visits the points for which locfunc returns
+ * VSG_RLOC2_MASK; traverse walks the GPU quadtree (children in quadrant
+ * order x + 2y or along the Hilbert curve); set_nf_isleaf keeps nodes about
+ * to be split as leaves. */
+void aran_solver2d_get_functions_full (AranSolver2d *solver, AranParticle2ParticleFunc2d *p2p,
+                                       AranParticle2MultipoleFunc2d *p2m,
+                                       AranMultipole2MultipoleFunc2d *m2m,
+                                       AranMultipole2LocalFunc2d *m2l, AranLocal2LocalFunc2d *l2l,
+                                       AranLocal2ParticleFunc2d *l2p, AranParticle2LocalFunc2d *p2l,
+                                       AranMultipole2ParticleFunc2d *m2p,
+                                       guint *semifar_threshold);
+void aran_solver2d_db_profile_operators (AranSolver2d *solver, gdouble order);
+void aran_solver2d_profile_operators (AranSolver2d *solver, AranParticleInitFunc2d point_init,
+                                      gpointer p1, gpointer p2);
+guint aran_solver2d_optimal_semifar_threshold (AranSolver2d *solver);
+gboolean aran_solver2d_insert_point_local (AranSolver2d *solver, VsgPoint2 point);
+void aran_solver2d_foreach_point_custom (AranSolver2d *solver, VsgRegion2 selector,
+                                         VsgRegion2Point2LocFunc locfunc, GFunc func,
+                                         gpointer user_data);
+void aran_solver2d_traverse (AranSolver2d *solver, GTraverseType order, VsgPRTree2dFunc func,
+                             gpointer user_data);
+void aran_solver2d_set_children_order_hilbert (AranSolver2d *solver);
+void aran_solver2d_set_children_order_default (AranSolver2d *solver);
+void aran_solver2d_set_nf_isleaf (AranSolver2d *solver, VsgPRTree2dNFIsleafFunc isleaf,
+                                  gpointer user_data);
+
 /* Additive: where the Cauchy-kernel data sits in the caller's point struct
  * (position: VsgVector2d at pos_offset, density: gdouble at
  * density_offset, accumulator: gcomplex128 at accum_offset). */

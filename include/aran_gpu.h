@@ -259,6 +259,11 @@ void aran_gpu_solver2d_destroy (AranGpuSolver2d *s);
 int aran_gpu_solver2d_solve (AranGpuSolver2d *s, int nsys, const int64_t *offs,
                              const double *box, const double *xy, const double *q,
                              double *acc, int mem);
+/* Leaf predicate of the 2D forest (z components of the view are 0): the
+ * twin of aran_gpu_solver3d_set_leaf_predicate for
+ * aran_solver2d_set_nf_isleaf (aran/aransolver2d.c). */
+int aran_gpu_solver2d_set_leaf_predicate (AranGpuSolver2d *s, AranGpuLeafPredicate pred,
+                                          void *user_data);
 /* Call counters of the last solve, summed over its systems, in the order
  * of aran_solver2d_get_stats (aran/aransolver2d.c:868-896). */
 int aran_gpu_solver2d_get_stats (AranGpuSolver2d *s, int64_t stats[11]);

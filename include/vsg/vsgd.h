@@ -102,7 +102,19 @@ struct _VsgPRTree2dNodeInfo
   guint id;
 };
 
+#define VSG_PRTREE2D_NODE_INFO_IS_SHARED(node_info) (FALSE)
+
+/* Quadrant mask: bit o set when a region reaches quadrant o (x + 2y, a bit
+ * set on the upper side) around a point; all four bits: the region
+ * surrounds the point. */
+typedef guint8 vsgrloc2;
+#define VSG_RLOC2_MASK ((vsgrloc2) 0xf)
+
 typedef gint (*VsgPoint2dLocFunc) (const VsgPoint2 candidate, const VsgVector2d *center);
+typedef vsgrloc2 (*VsgRegion2Point2LocFunc) (const VsgRegion2 region, const VsgPoint2 point);
+typedef void (*VsgPRTree2dFunc) (const VsgPRTree2dNodeInfo *node_info, gpointer user_data);
+typedef gboolean (*VsgPRTree2dNFIsleafFunc) (const VsgPRTree2dNodeInfo *node_info,
+                                             gpointer user_data);
 typedef gdouble (*VsgPoint2dDistFunc) (const VsgPoint2 one, const VsgPoint2 other);
 typedef gint (*VsgRegion2dLocFunc) (const VsgRegion2 region, const VsgVector2d *center);
 

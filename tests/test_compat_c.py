@@ -231,3 +231,25 @@ def test_reference_profile_db_fixture():
         assert L.aran_profile_db_address_eval(addr, 1.0) == x, name
     bad = C.c_int(0)
     assert math.isnan(L.aran_profile_db_address_eval(C.addressof(bad), 1.0))
+
+
+API2D_SRC = os.path.join(ROOT, "tests", "c", "solver2d_api.c")
+
+
+@pytest.fixture(scope="module")
+def api2d_exe(tmp_path_factory):
+    return compile_c(tmp_path_factory, API2D_SRC, "solver2d_api")
+
+
+def test_solver2d_api_host(api2d_exe, tmp_path):
+    ini = tmp_path / "profiledb.ini"
+    ini.write_text("[aran-profile]\naran_development2d_m2l=3e-6;\n")
+    env = dict(os.environ, ARAN_PROFILE_DB=str(ini))
+    r = subprocess.run([api2d_exe, "host"], capture_output=True, text=True, timeout=120, env=env)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
+
+
+@pytest.mark.gpu
+def test_solver2d_api_gpu(api2d_exe):
+    r = subprocess.run([api2d_exe, "gpu"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
