@@ -42,6 +42,13 @@ def build(force: bool = False) -> str:
     return _LIB
 
 
+def build_reference(force: bool = False):
+    """Compile the reference's own operator layer (oracle/ref_build.py) when
+    the reference tree is present; None otherwise."""
+    from . import ref_build
+    return ref_build.build(force)
+
+
 _lib = None
 
 
