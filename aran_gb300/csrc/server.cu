@@ -54,7 +54,7 @@ struct ConfigKey {
 constexpr int kPlanMaxOrder = 30;
 const double kErrFp64[kPlanMaxOrder + 1] = {
     0, 0, 0, 0, 2.4e-3, 0, 2.7e-4, 0, 3.8e-5, 0, 6.8e-6, 0, 1.4e-6, 0, 2.7e-7, 0, 6.4e-8,
-    0, 1.6e-8, 0, 5.8e-9};
+    0, 1.6e-8, 0, 5.8e-9, 0, 1.4e-9, 0, 8.6e-10, 0, 1.9e-10, 0, 9.7e-11, 0, 6.5e-11};
 const double kErrMixed[kPlanMaxOrder + 1] = {
     0, 0, 0, 0, 2.4e-3, 0, 2.7e-4, 0, 3.8e-5, 0, 6.8e-6, 0, 1.4e-6, 0, 5.4e-7, 0, 3.7e-7,
     0, 3.7e-7, 0, 3.7e-7};

@@ -430,8 +430,8 @@ def cpu_baseline(x, q, name: str, max_solves: int = 1, budget_s: float = 0.0) ->
 # DRAM bytes of one k_m2l_lanes<12> launch on plummer4m (233,161 nodes,
 # 38,977,626 M2L): ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum
 # on one launch of that workload (-k regex:k_m2l_lanes -s 1 -c 1,
-# --clock-control none), read + write
-M2L_DRAM_BYTES_PLUMMER4M = None
+# --clock-control none): 154,687,232 B read + 128,904,192 B written
+M2L_DRAM_BYTES_PLUMMER4M = 154_687_232 + 128_904_192
 
 
 def run_gpu(args):
