@@ -384,6 +384,56 @@ def run_batched_3d(nsys: int, nslots: int = 4, check_systems: int = 8) -> dict:
 
 
 # ------------------------------------------------------------- CPU baseline
+def run_flavours(steps: int, direct_targets: int) -> dict:
+    """The uniform1m configuration (N=1M uniform, p=12, leaf 64, field) with
+    both M2L flavours (rotate: point-and-shoot, kkylin: the reference's
+    aransphericalseriesd-kkylin.c), mixed and FP64, each against the FP64
+    direct sum on the same target sample."""
+    import numpy as np
+    import torch
+
+    import aran_gb300 as A
+    import oracle
+
+    gen, n, p, maxbox, lb, ub, desc = WORKLOADS["uniform1m"]
+    x, q = make_workload("uniform1m")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    dx = torch.from_numpy(x).to(dev)
+    dq = torch.from_numpy(q).to(dev)
+    pot = torch.empty(n, dtype=torch.float64, device=dev)
+    fld = torch.empty((n, 3), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    tgt = np.random.default_rng(5).choice(n, direct_targets, replace=False)
+    rp, rf = oracle.direct(x, q, targets=tgt)
+
+    def rl2(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    out = {"workload": "uniform1m", "description": desc, "targets": direct_targets}
+    for flavour in ("rotate", "kkylin"):
+        for precision in ("mixed", "fp64"):
+            k = steps if precision == "mixed" else 1
+            with A.Solver3d(lb, ub, maxbox=maxbox, order=p, flavour=flavour, field=True,
+                            precision=precision) as s:
+                for _ in range(2):
+                    s.solve_device(n, dx.data_ptr(), dq.data_ptr(), pot.data_ptr(),
+                                   fld.data_ptr())
+                ms = []
+                for _ in range(k):
+                    flush.fill_(1.0)
+                    torch.cuda.synchronize()
+                    s.solve_device(n, dx.data_ptr(), dq.data_ptr(), pot.data_ptr(),
+                                   fld.data_ptr())
+                    ms.append(s.timings())
+                pm, fm = pot.cpu().numpy(), fld.cpu().numpy()
+            tot = statistics.mean(d["total"] for d in ms)
+            out[f"{flavour}_{precision}"] = {
+                "value": n / (tot * 1e-3), "unit": UNIT, "ms_per_step": tot,
+                "m2l_ms": statistics.mean(d["m2l"] for d in ms),
+                "pot_vs_direct": rl2(pm[tgt], rp), "field_vs_direct": rl2(fm[tgt], rf)}
+    return out
+
+
 def cpu_model() -> str:
     try:
         out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
@@ -677,6 +727,8 @@ def run_gpu(args):
                 "d2h_bytes_per_step": n * 8 + n * 3 * 8},
         "gpu_launches": launches,
     }
+    if args.flavours:
+        line["flavours"] = run_flavours(max(1, min(args.steps, 5)), args.direct_targets or 10000)
     if args.serving_requests > 0:
         line["serving"] = run_serving_suite(args.serving_requests, args.serving_rate)
     if args.batched_2d_systems > 0 or args.batched_3d_systems > 0:
@@ -728,6 +780,8 @@ def main():
     ap.add_argument("--orders", default="8,16",
                     help="other orders of the workload to run (mixed and FP64), comma-separated")
     ap.add_argument("--direct-targets", type=int, default=10000)
+    ap.add_argument("--flavours", type=int, default=1,
+                    help="also time uniform1m at p=12 with the rotate and kkylin M2L")
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--ref-budget-s", type=float, default=150.0,
                     help="--impl reference: wall-time budget for full CPU solves")

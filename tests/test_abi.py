@@ -91,3 +91,24 @@ def test_invalid_configs_rejected_before_device_use():
         with pytest.raises(aran_gb300.AranError) as ei:
             aran_gb300.Solver2d(**kw)
         assert ei.value.code == -1, kw
+
+
+def test_tolerance_plan():
+    """The request loop's tolerance -> (order, precision) plan (host-only)."""
+    import aran_gb300 as A
+    plans = [A.plan_for_tolerance(t) for t in (1e-3, 1e-4, 1e-5, 1e-6, 1e-7, 1e-8, 1e-9, 1e-10)]
+    for tol, (order, prec, est) in zip((1e-3, 1e-4, 1e-5, 1e-6, 1e-7, 1e-8, 1e-9), plans):
+        assert est <= 0.5 * tol and prec in ("mixed", "fp64")
+    # below the table's best error: the highest tabulated order in FP64
+    assert plans[7][:2] == (30, "fp64") and plans[7][2] > 0.5e-10
+    assert plans[1][:2] == (8, "mixed") and plans[3][:2] == (16, "mixed")
+    assert plans[6][:2] == (26, "fp64")
+    # mixed is preferred while its floor allows; tighter plans never lower the order
+    assert [p[1] for p in plans[:4]] == ["mixed"] * 4 and plans[4][1] == "fp64"
+    fp64_orders = [p[0] for p in plans if p[1] == "fp64"]
+    assert fp64_orders == sorted(fp64_orders)
+    # a given order only picks the precision
+    assert A.plan_for_tolerance(1e-4, order=12)[:2] == (12, "mixed")
+    assert A.plan_for_tolerance(1e-8, order=20)[:2] == (20, "fp64")
+    with pytest.raises(A.AranError):
+        A.plan_for_tolerance(0.0)

@@ -133,16 +133,19 @@ def test_orders_fp64(aran, oracle, p):
     assert rel_l2(fld, ofld) < FP64_TOL
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 2e-6), ("mixed", 3e-6)])
-def test_p12_against_direct_sum(aran, oracle, precision, tol):
-    """Accuracy target of the benchmark workloads: p=12 within ~1e-6 of the
-    FP64 direct sum."""
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_p12_against_direct_sum(aran, oracle, precision):
+    """p=12 on a uniform cube against the FP64 direct sum.  Here the
+    truncation error of the expansion itself (the oracle's FP64 solve) is
+    1.43e-6 for the potential and 5.3e-7 for the field, so the potential bound
+    sits just above it and mixed precision may add at most 1.5e-7; the
+    Plummer workloads (test_gpu_precision) meet 1e-6 for the potential."""
     x, q = W.uniform(30000, 2)
     with aran.Solver3d(maxbox=64, order=12, field=True, precision=precision) as s:
         pot, fld = s.solve(x, q)
     rp, rf = oracle.direct(x, q)
-    assert rel_l2(pot, rp) < tol
-    assert rel_l2(fld, rf) < tol
+    assert rel_l2(pot, rp) < (1.5e-6 if precision == "fp64" else 1.6e-6)
+    assert rel_l2(fld, rf) < (6e-7 if precision == "fp64" else 1e-6)
 
 
 def test_single_leaf_is_direct_sum(aran, oracle):

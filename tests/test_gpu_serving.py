@@ -7,7 +7,12 @@
 * admission respects the HBM budget: requests whose footprints do not fit
   together never run at the same time; a request larger than the budget is
   refused at submission;
-* a queued request can be cancelled; the others complete.
+* a queued request can be cancelled; the others complete;
+* every request that gives a tolerance instead of an order meets it: the
+  server picks order and precision from its error table, and each result's
+  potential is within the requested relative L2 error of the FP64 direct sum
+  on a target sample (the reference checks each solve against the direct
+  sum the same way, tests/newtonpot3.c:678-715).
 """
 import numpy as np
 import pytest
@@ -96,3 +101,30 @@ def test_cancel_queued_request(aran):
         assert ei.value.code == -7
         for t in (ts[0], ts[2]):
             assert sv.wait(t)[2]["status"] == 0
+
+
+TOLERANCES = (1e-4, 1e-6, 1e-9)
+
+
+def test_served_results_meet_their_tolerance(aran, oracle):
+    rng = np.random.default_rng(91)
+    reqs = []
+    for i in range(9):
+        n = int(np.exp(rng.uniform(np.log(5000), np.log(60000))))
+        if i % 2:
+            x, q = W.plummer(n, 400 + i)
+            lb, ub = (-1, -1, -1), (1, 1, 1)
+        else:
+            x, q = W.uniform(n, 400 + i)
+            lb, ub = (0, 0, 0), (1, 1, 1)
+        reqs.append((x, q, TOLERANCES[i % 3], dict(lbound=lb, ubound=ub, maxbox=32, field=True)))
+    with aran.Server(nslots=4, hbm_budget_bytes=100e9) as sv:
+        tickets = [sv.submit(x, q, tolerance=tol, **kw) for x, q, tol, kw in reqs]
+        served = [sv.wait(t) for t in tickets]
+    for (x, q, tol, _), (pot, fld, info) in zip(reqs, served):
+        assert info["status"] == 0
+        order, prec, _ = aran.plan_for_tolerance(tol)
+        assert (info["order"], info["precision"]) == (order, prec)
+        tg = np.random.default_rng(len(q)).choice(len(q), size=2000, replace=False)
+        rp, _ = oracle.direct(x, q, targets=tg)
+        assert rel_l2(pot[tg], rp) <= tol, (tol, len(q), order, prec)
