@@ -27,6 +27,7 @@ STAGE_NAMES = ("total", "sort", "tree", "lists", "p2m", "m2m", "m2l", "l2l", "l2
 # exported symbols of include/aran_gpu.h
 EXPORTS = (
     "aran_gpu_solver3d_create", "aran_gpu_solver3d_destroy", "aran_gpu_solver3d_solve",
+    "aran_gpu_solver3d_solve_forest",
     "aran_gpu_solver3d_get_stats", "aran_gpu_solver3d_tree_info",
     "aran_gpu_solver3d_tree_lists", "aran_gpu_solver3d_expansions",
     "aran_gpu_solver3d_timings", "aran_gpu_solver3d_launches", "aran_gpu_last_error",
@@ -101,6 +102,8 @@ def load(build_if_missing: bool = True):
     L.aran_gpu_solver3d_destroy.restype = None
     L.aran_gpu_solver3d_solve.argtypes = [vp, C.c_int64, vp, vp, vp, vp, C.c_int]
     L.aran_gpu_solver3d_solve.restype = C.c_int
+    L.aran_gpu_solver3d_solve_forest.argtypes = [vp, C.c_int, i64p, dp, vp, vp, vp, vp, C.c_int]
+    L.aran_gpu_solver3d_solve_forest.restype = C.c_int
     L.aran_gpu_solver3d_get_stats.argtypes = [vp, i64p]
     L.aran_gpu_solver3d_get_stats.restype = C.c_int
     L.aran_gpu_solver3d_tree_info.argtypes = [vp, i64p]
@@ -332,6 +335,27 @@ class Solver3d:
                                               C.c_void_p(pot_ptr) if pot_ptr else None,
                                               C.c_void_p(field_ptr) if field_ptr else None,
                                               MEM_DEVICE))
+
+    def solve_forest(self, xyz, q, offsets, boxes):
+        """Independent systems in one solve: system k is particles
+        offsets[k]:offsets[k+1] in box boxes[k] = (lbx, lby, lbz, ubx, uby,
+        ubz), every box with the solver's extents.  Returns (potential[n],
+        field[n,3] or None) in input order."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        offs = np.ascontiguousarray(offsets, dtype=np.int64)
+        boxes = np.ascontiguousarray(boxes, dtype=np.float64).reshape(-1, 6)
+        nsys = len(offs) - 1
+        n = len(q)
+        if xyz.shape != (n, 3) or len(boxes) != nsys:
+            raise ValueError("xyz must be (n, 3) and boxes (nsys, 6)")
+        pot = np.empty(n)
+        fld = np.empty((n, 3)) if self.field else None
+        _check(load().aran_gpu_solver3d_solve_forest(
+            self._h, nsys, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+            boxes.ctypes.data_as(C.POINTER(C.c_double)), _ptr(xyz), _ptr(q), _ptr(pot),
+            _ptr(fld), MEM_HOST))
+        return pot, fld
 
     # -- introspection ------------------------------------------------------
     def get_stats(self) -> dict:

@@ -102,6 +102,7 @@ struct DevTree {
   DBuf<int> ijk;                      // 3 per node
   DBuf<uint8_t> depth;
   DBuf<int> begin, end, child, parent;
+  DBuf<int> sys;                      // system (tree of the forest) of the node
   DBuf<double> center;                // 3 per node
   DBuf<int> col;                      // 27 per node
   DBuf<int> ncol;
@@ -204,6 +205,14 @@ struct AranGpuSolver3d {
   // host predicate keeping nodes about to be split as leaves (virtual leaves)
   AranGpuLeafPredicate leaf_pred = nullptr;
   void *leaf_pred_data = nullptr;
+  // systems of the solve (a forest: one octree per system; 1 for a plain
+  // solve): particle offsets (device, nsys + 1) and per system lb[3],
+  // ub[3] and the key scales 2^21 / (ub - lb) (9 doubles, host and device)
+  int nsys = 1;
+  aran::DBuf<int> sys_off;
+  aran::DBuf<double> sys_box;
+  std::vector<int> h_sys_off;
+  std::vector<double> h_sys_box;
 };
 
 namespace aran {

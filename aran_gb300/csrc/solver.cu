@@ -25,6 +25,32 @@ int consumer_wait_polls() {
 
 void scatter_outputs(AranGpuSolver3d *s, double *pot, double *fld);
 
+// uploads the systems of a solve (offs/boxes NULL: one system in the
+// solver's box); skipped when they equal the last solve's
+void set_systems(AranGpuSolver3d *s, int nsys, const int64_t *offs, const double *boxes,
+                 int64_t n) {
+  std::vector<int> off(nsys + 1);
+  std::vector<double> box(9 * (size_t)nsys);
+  for (int k = 0; k <= nsys; ++k) off[k] = offs ? (int)offs[k] : (k ? (int)n : 0);
+  for (int k = 0; k < nsys; ++k)
+    for (int a = 0; a < 3; ++a) {
+      double *b = box.data() + 9 * (size_t)k;
+      b[a] = boxes ? boxes[6 * (size_t)k + a] : s->cfg.lb[a];
+      b[3 + a] = boxes ? boxes[6 * (size_t)k + 3 + a] : s->cfg.ub[a];
+      b[6 + a] = (double)(1 << kKeyBits) / (b[3 + a] - b[a]);
+    }
+  if (nsys == s->nsys && off == s->h_sys_off && box == s->h_sys_box && s->sys_off.ptr) return;
+  s->sys_off.reserve(off.size());
+  s->sys_box.reserve(box.size());
+  s->nsys = nsys;
+  s->h_sys_off = off;
+  s->h_sys_box = box;
+  ACHECK(cudaMemcpyAsync(s->sys_off.ptr, s->h_sys_off.data(), off.size() * sizeof(int),
+                         cudaMemcpyHostToDevice, s->s0));
+  ACHECK(cudaMemcpyAsync(s->sys_box.ptr, s->h_sys_box.data(), box.size() * sizeof(double),
+                         cudaMemcpyHostToDevice, s->s0));
+}
+
 void build_tree_only(AranGpuSolver3d *s, int64_t n, const double *xyz, const double *q) {
   ACHECK(cudaSetDevice(s->device));
   cudaStream_t st = s->s0;
@@ -34,6 +60,7 @@ void build_tree_only(AranGpuSolver3d *s, int64_t n, const double *xyz, const dou
   ACHECK(cudaMemcpyAsync(s->io_xyz.ptr, xyz, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
   ACHECK(cudaMemcpyAsync(s->io_q.ptr, q, n * sizeof(double), cudaMemcpyHostToDevice, st));
   ACHECK(cudaEventRecord(s->ev[2 * Stage::SORT], st));
+  set_systems(s, 1, nullptr, nullptr, n);
   build_tree(s, n, s->io_xyz.ptr, s->io_q.ptr);
   ACHECK(cudaStreamSynchronize(st));
   s->have_tree = false;   // no lists: counters and list queries need a solve
@@ -145,7 +172,8 @@ void aran_gpu_solver3d_destroy(AranGpuSolver3d *s) {
   s->mult64.release(); s->loc64.release(); s->mult32.release(); s->loc32.release();
   s->scan_tmp.release(); s->stats_dev.release(); s->err_dev.release();
   t.leaf_be.release(); t.leaf_chi.release(); t.leaf_clo.release(); t.big_items.release();
-  t.parents.release(); t.big_rng.release();
+  t.parents.release(); t.big_rng.release(); t.sys.release();
+  s->sys_off.release(); s->sys_box.release();
   s->kk64.release();
   s->kk32.release();
   for (auto &ev : s->ev)
@@ -155,18 +183,48 @@ void aran_gpu_solver3d_destroy(AranGpuSolver3d *s) {
   delete s;
 }
 
-int aran_gpu_solver3d_solve(AranGpuSolver3d *s, int64_t n, const double *xyz, const double *q,
-                            double *pot, double *field, int mem) {
+}  // extern "C"
+
+namespace {
+
+int check_systems(const AranGpuSolver3d *s, int nsys, const int64_t *offs, const double *boxes,
+                  int64_t n) {
+  if (nsys < 1) return fail(ARAN_ERR_INVALID, "nsys must be >= 1");
+  if (!offs || !boxes) return fail(ARAN_ERR_INVALID, "offsets and boxes must not be NULL");
+  if (offs[0] != 0 || offs[nsys] != n)
+    return fail(ARAN_ERR_INVALID, "offsets must start at 0 and end at n");
+  for (int k = 0; k < nsys; ++k) {
+    if (offs[k + 1] < offs[k]) return fail(ARAN_ERR_INVALID, "offsets must be non-decreasing");
+    for (int a = 0; a < 3; ++a) {
+      const double lo = boxes[6 * (size_t)k + a], hi = boxes[6 * (size_t)k + 3 + a];
+      if (!std::isfinite(lo) || !std::isfinite(hi) || !(hi > lo))
+        return fail(ARAN_ERR_INVALID, "system " + std::to_string(k) + ": box must satisfy lb < ub (finite)");
+      // the operator tables are made for the solver's box extents
+      if (hi - lo != s->cfg.ub[a] - s->cfg.lb[a])
+        return fail(ARAN_ERR_INVALID, "system " + std::to_string(k) +
+                                          ": box extents must equal the solver's ub - lb");
+    }
+  }
+  return ARAN_OK;
+}
+
+int solve_impl(AranGpuSolver3d *s, int nsys, const int64_t *offs, const double *boxes, int64_t n,
+               const double *xyz, const double *q, double *pot, double *field, int mem) {
   if (!s) return fail(ARAN_ERR_INVALID, "solver is NULL");
   if (n < 1) return fail(ARAN_ERR_INVALID, "n must be >= 1");
   if (n > (int64_t)1 << 30) return fail(ARAN_ERR_INVALID, "n exceeds 2^30 particles");
   if (!xyz || !q) return fail(ARAN_ERR_INVALID, "xyz and q must not be NULL");
   if (mem != ARAN_MEM_HOST && mem != ARAN_MEM_DEVICE) return fail(ARAN_ERR_INVALID, "bad mem kind");
   if (field && !s->cfg.field) return fail(ARAN_ERR_INVALID, "field requested from a potential-only solver");
+  if (offs) {
+    int rc = check_systems(s, nsys, offs, boxes, n);
+    if (rc) return rc;
+  }
   try {
     ACHECK(cudaSetDevice(s->device));
     s->launches = 0;
     cudaStream_t st = s->s0;
+    set_systems(s, offs ? nsys : 1, offs, boxes, n);
     const double *dx = xyz, *dq = q;
     double *dpot = pot, *dfld = field;
     ACHECK(cudaEventRecord(s->ev[2 * Stage::TOTAL], st));
@@ -236,6 +294,23 @@ int aran_gpu_solver3d_solve(AranGpuSolver3d *s, int64_t n, const double *xyz, co
     return fail(ARAN_ERR_INVALID, ie.msg);
   }
   return ARAN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int aran_gpu_solver3d_solve(AranGpuSolver3d *s, int64_t n, const double *xyz, const double *q,
+                            double *pot, double *field, int mem) {
+  return solve_impl(s, 1, nullptr, nullptr, n, xyz, q, pot, field, mem);
+}
+
+int aran_gpu_solver3d_solve_forest(AranGpuSolver3d *s, int nsys, const int64_t *offsets,
+                                   const double *boxes, const double *xyz, const double *q,
+                                   double *pot, double *field, int mem) {
+  if (!offsets) return fail(ARAN_ERR_INVALID, "offsets must not be NULL");
+  if (nsys < 1) return fail(ARAN_ERR_INVALID, "nsys must be >= 1");
+  return solve_impl(s, nsys, offsets, boxes, offsets[nsys], xyz, q, pot, field, mem);
 }
 
 int aran_gpu_solver3d_get_stats(AranGpuSolver3d *s, int64_t stats[11]) {

@@ -16,6 +16,11 @@
 //      range): every colleague of L (a leaf, or an internal node standing for
 //      all leaves below it), plus the leaf colleagues of every ancestor of L
 //      (a coarser leaf adjacent to an ancestor is near everything below it).
+// A solve of several independent systems builds a forest the same way: each
+// system's particles are sorted within its own segment and in its own box,
+// level 0 holds one root per system, and since a root's only colleague is
+// itself no colleague, far or near list ever joins two systems.  Each
+// level's kernels then run over the nodes of all systems at once.
 #include <cub/cub.cuh>
 
 #include "internal.cuh"
@@ -24,18 +29,27 @@ namespace aran {
 
 namespace {
 
-// Morton keys of the particles; a non-finite coordinate or charge sets
-// kErrNonFinite in the error word (the solve then stops before any output)
+// Morton keys of the particles, each in its system's box (sys_box: lb[3],
+// ub[3], scale[3] per system; particles of system k are sys_off[k] ..
+// sys_off[k+1]-1); a non-finite coordinate or charge sets kErrNonFinite in
+// the error word (the solve then stops before any output)
 __global__ void k_keys(int64_t n, const double *__restrict__ xyz, const double *__restrict__ q,
-                       double lbx, double lby, double lbz, double scx, double scy, double scz,
-                       uint64_t *__restrict__ keys, int *__restrict__ idx, int *__restrict__ err) {
+                       int nsys, const int *__restrict__ sys_off,
+                       const double *__restrict__ sys_box, uint64_t *__restrict__ keys,
+                       int *__restrict__ idx, int *__restrict__ err) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  int lo = 0, hi = nsys;   // the last system k with sys_off[k] <= i, in [lo, hi)
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (sys_off[mid] <= i) lo = mid; else hi = mid;
+  }
+  const double *b = sys_box + 9 * lo;
   const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
   if (!(isfinite(x) && isfinite(y) && isfinite(z) && isfinite(q[i]))) atomicOr(err, kErrNonFinite);
-  uint64_t qx = (uint64_t)quantise(x, lbx, scx);
-  uint64_t qy = (uint64_t)quantise(y, lby, scy);
-  uint64_t qz = (uint64_t)quantise(z, lbz, scz);
+  uint64_t qx = (uint64_t)quantise(x, b[0], b[6]);
+  uint64_t qy = (uint64_t)quantise(y, b[1], b[7]);
+  uint64_t qz = (uint64_t)quantise(z, b[2], b[8]);
   keys[i] = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
   idx[i] = (int)i;
 }
@@ -57,22 +71,28 @@ struct NodeArrays {
   uint64_t *key;
   int *ijk;
   uint8_t *depth;
-  int *begin, *end, *child, *parent;
+  int *begin, *end, *child, *parent, *sys;
   double *center;
 };
 
-__global__ void k_root(NodeArrays na, int64_t n, double lbx, double lby, double lbz, double ubx,
-                       double uby, double ubz) {
-  na.key[0] = 0;
-  na.ijk[0] = na.ijk[1] = na.ijk[2] = 0;
-  na.depth[0] = 0;
-  na.begin[0] = 0;
-  na.end[0] = (int)n;
-  na.child[0] = -1;
-  na.parent[0] = -1;
-  na.center[0] = node_center_axis(lbx, ubx, 0, 0);
-  na.center[1] = node_center_axis(lby, uby, 0, 0);
-  na.center[2] = node_center_axis(lbz, ubz, 0, 0);
+// one root per system at depth 0 (roots have no colleagues but themselves,
+// so no list of the forest joins two systems)
+__global__ void k_roots(NodeArrays na, int nsys, const int *__restrict__ sys_off,
+                        const double *__restrict__ sys_box) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nsys) return;
+  const double *b = sys_box + 9 * r;
+  na.key[r] = 0;
+  na.ijk[3 * r] = na.ijk[3 * r + 1] = na.ijk[3 * r + 2] = 0;
+  na.depth[r] = 0;
+  na.begin[r] = sys_off[r];
+  na.end[r] = sys_off[r + 1];
+  na.child[r] = -1;
+  na.parent[r] = -1;
+  na.sys[r] = r;
+  na.center[3 * r] = node_center_axis(b[0], b[3], 0, 0);
+  na.center[3 * r + 1] = node_center_axis(b[1], b[4], 0, 0);
+  na.center[3 * r + 2] = node_center_axis(b[2], b[5], 0, 0);
 }
 
 __global__ void k_flag_internal(int cnt, int off, const int *__restrict__ begin,
@@ -94,8 +114,7 @@ __device__ __forceinline__ int digit_at(const uint64_t *k, int j, int shift) {
 // (the neighbouring lane's result)
 __global__ void k_make_children(int cnt, int off, int child_off, const int *__restrict__ flags,
                                 const int *__restrict__ pos, const uint64_t *__restrict__ skeys,
-                                int d, NodeArrays na, double lbx, double lby, double lbz,
-                                double ubx, double uby, double ubz) {
+                                int d, NodeArrays na, const double *__restrict__ sys_box) {
   const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int i = (int)(g >> 3), c = (int)(g & 7);
   const bool live = i < cnt;
@@ -125,6 +144,8 @@ __global__ void k_make_children(int cnt, int off, int child_off, const int *__re
   const uint64_t pk = na.key[node];
   const int pi = na.ijk[3 * node], pj = na.ijk[3 * node + 1], pk3 = na.ijk[3 * node + 2];
   const int cn = base + c;
+  const int sy = na.sys[node];
+  const double *bx = sys_box + 9 * sy;
   na.key[cn] = (pk << 3) | (uint64_t)c;
   const int ci = (pi << 1) | (c & 1), cj = (pj << 1) | ((c >> 1) & 1), ck = (pk3 << 1) | ((c >> 2) & 1);
   na.ijk[3 * cn] = ci;
@@ -135,9 +156,10 @@ __global__ void k_make_children(int cnt, int off, int child_off, const int *__re
   na.end[cn] = lo;
   na.child[cn] = -1;
   na.parent[cn] = node;
-  na.center[3 * cn] = node_center_axis(lbx, ubx, d + 1, ci);
-  na.center[3 * cn + 1] = node_center_axis(lby, uby, d + 1, cj);
-  na.center[3 * cn + 2] = node_center_axis(lbz, ubz, d + 1, ck);
+  na.sys[cn] = sy;
+  na.center[3 * cn] = node_center_axis(bx[0], bx[3], d + 1, ci);
+  na.center[3 * cn + 1] = node_center_axis(bx[1], bx[4], d + 1, cj);
+  na.center[3 * cn + 2] = node_center_axis(bx[2], bx[5], d + 1, ck);
 }
 
 __device__ __forceinline__ bool adjacent(const int *ijk, int a, int b) {
@@ -456,6 +478,7 @@ NodeArrays arrays(DevTree &t) {
   na.end = t.end.ptr;
   na.child = t.child.ptr;
   na.parent = t.parent.ptr;
+  na.sys = t.sys.ptr;
   na.center = t.center.ptr;
   return na;
 }
@@ -468,6 +491,7 @@ void grow_nodes(DevTree &t, size_t need, size_t keep, cudaStream_t st) {
   t.end.grow_keep(need, keep, st);
   t.child.grow_keep(need, keep, st);
   t.parent.grow_keep(need, keep, st);
+  t.sys.grow_keep(need, keep, st);
   t.center.grow_keep(3 * need, 3 * keep, st);
 }
 
@@ -476,9 +500,9 @@ void grow_nodes(DevTree &t, size_t need, size_t keep, cudaStream_t st) {
 void apply_leaf_predicate(AranGpuSolver3d *s, int off, int cnt, int d, int *d_flags,
                           cudaStream_t st) {
   const DevTree &t = s->tree;
-  const AranGpuConfig3d &c = s->cfg;
-  std::vector<int> fl(cnt), b(cnt), e(cnt), ijk(3 * (size_t)cnt);
+  std::vector<int> fl(cnt), b(cnt), e(cnt), ijk(3 * (size_t)cnt), sy(cnt);
   ACHECK(cudaMemcpyAsync(fl.data(), d_flags, cnt * sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaMemcpyAsync(sy.data(), t.sys.ptr + off, cnt * sizeof(int), cudaMemcpyDeviceToHost, st));
   ACHECK(cudaMemcpyAsync(b.data(), t.begin.ptr + off, cnt * sizeof(int), cudaMemcpyDeviceToHost, st));
   ACHECK(cudaMemcpyAsync(e.data(), t.end.ptr + off, cnt * sizeof(int), cudaMemcpyDeviceToHost, st));
   ACHECK(cudaMemcpyAsync(ijk.data(), t.ijk.ptr + 3 * (size_t)off, 3 * cnt * sizeof(int),
@@ -488,9 +512,10 @@ void apply_leaf_predicate(AranGpuSolver3d *s, int off, int cnt, int d, int *d_fl
   for (int i = 0; i < cnt; ++i) {
     if (!fl[i]) continue;
     AranGpuNodeView v;
+    const double *box = s->h_sys_box.data() + 9 * (size_t)sy[i];
     for (int a = 0; a < 3; ++a) {
-      // the cell by halving the root box, as the node centres are made
-      double lo = c.lb[a], hi = c.ub[a];
+      // the cell by halving the system's box, as the node centres are made
+      double lo = box[a], hi = box[3 + a];
       for (int bit = d - 1; bit >= 0; --bit) {
         const double mid = (lo + hi) * 0.5;
         if ((ijk[3 * (size_t)i + a] >> bit) & 1) lo = mid;
@@ -520,22 +545,33 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
   DevTree &t = s->tree;
   t.n = n;
   const int TB = 256;
-  double sc[3];
-  for (int a = 0; a < 3; ++a) sc[a] = (double)(1 << kKeyBits) / (c.ub[a] - c.lb[a]);
+  const int nsys = s->nsys;
 
   s->keys_in.reserve(n);
   s->keys_out.reserve(n);
   s->idx_in.reserve(n);
   s->perm.reserve(n);
-  k_keys<<<ceil_div(n, TB), TB, 0, st>>>(n, d_xyz, d_q, c.lb[0], c.lb[1], c.lb[2], sc[0], sc[1],
-                                          sc[2], s->keys_in.ptr, s->idx_in.ptr, s->err_dev.ptr);
+  k_keys<<<ceil_div(n, TB), TB, 0, st>>>(n, d_xyz, d_q, nsys, s->sys_off.ptr, s->sys_box.ptr,
+                                          s->keys_in.ptr, s->idx_in.ptr, s->err_dev.ptr);
   s->launches++;
+  // the systems are contiguous in the input: each is sorted in place
   size_t bytes = 0;
-  ACHECK(cub::DeviceRadixSort::SortPairs(nullptr, bytes, s->keys_in.ptr, s->keys_out.ptr,
-                                         s->idx_in.ptr, s->perm.ptr, (int)n, 0, 3 * kKeyBits, st));
-  s->cub_tmp.reserve(bytes);
-  ACHECK(cub::DeviceRadixSort::SortPairs(s->cub_tmp.ptr, bytes, s->keys_in.ptr, s->keys_out.ptr,
-                                         s->idx_in.ptr, s->perm.ptr, (int)n, 0, 3 * kKeyBits, st));
+  if (nsys == 1) {
+    ACHECK(cub::DeviceRadixSort::SortPairs(nullptr, bytes, s->keys_in.ptr, s->keys_out.ptr,
+                                           s->idx_in.ptr, s->perm.ptr, (int)n, 0, 3 * kKeyBits, st));
+    s->cub_tmp.reserve(bytes);
+    ACHECK(cub::DeviceRadixSort::SortPairs(s->cub_tmp.ptr, bytes, s->keys_in.ptr, s->keys_out.ptr,
+                                           s->idx_in.ptr, s->perm.ptr, (int)n, 0, 3 * kKeyBits, st));
+  } else {
+    const int *ob = s->sys_off.ptr, *oe = s->sys_off.ptr + 1;
+    ACHECK(cub::DeviceSegmentedRadixSort::SortPairs(nullptr, bytes, s->keys_in.ptr, s->keys_out.ptr,
+                                                    s->idx_in.ptr, s->perm.ptr, (int)n, nsys,
+                                                    ob, oe, 0, 3 * kKeyBits, st));
+    s->cub_tmp.reserve(bytes);
+    ACHECK(cub::DeviceSegmentedRadixSort::SortPairs(s->cub_tmp.ptr, bytes, s->keys_in.ptr,
+                                                    s->keys_out.ptr, s->idx_in.ptr, s->perm.ptr,
+                                                    (int)n, nsys, ob, oe, 0, 3 * kKeyBits, st));
+  }
   s->launches += 4;
   s->sx.reserve(n);
   s->sy.reserve(n);
@@ -549,14 +585,14 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
   // level-synchronous subdivision
   int maxd = c.max_depth > 0 ? c.max_depth : kKeyBits;
   if (maxd > kKeyBits) maxd = kKeyBits;
-  size_t est = (size_t)(8 * (n / (c.maxbox + 1) + 1) * 2 + 64);
+  size_t est = (size_t)nsys + (size_t)(8 * (n / (c.maxbox + 1) + 1) * 2 + 64);
   grow_nodes(t, est, 0, st);
   t.level_off.assign(1, 0);
   t.level_internal.clear();
   NodeArrays na = arrays(t);
-  k_root<<<1, 1, 0, st>>>(na, n, c.lb[0], c.lb[1], c.lb[2], c.ub[0], c.ub[1], c.ub[2]);
+  k_roots<<<ceil_div(nsys, TB), TB, 0, st>>>(na, nsys, s->sys_off.ptr, s->sys_box.ptr);
   s->launches++;
-  int off = 0, cnt = 1;
+  int off = 0, cnt = nsys;
   DBuf<int> &flags = s->scan_tmp;
   int d = 0;
   int hostbuf[3] = {0, 0, 0};
@@ -583,8 +619,7 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
       na = arrays(t);
     }
     k_make_children<<<ceil_div(8 * (int64_t)cnt, TB), TB, 0, st>>>(cnt, off, child_off, flags.ptr, pos,
-                                                       s->keys_out.ptr, d, na, c.lb[0], c.lb[1],
-                                                       c.lb[2], c.ub[0], c.ub[1], c.ub[2]);
+                                                       s->keys_out.ptr, d, na, s->sys_box.ptr);
     s->launches++;
     off = child_off;
     cnt = 8 * ninternal;

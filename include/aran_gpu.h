@@ -83,6 +83,22 @@ int aran_gpu_solver3d_solve (AranGpuSolver3d *s, int64_t n, const double *xyz,
                              const double *q, double *pot, double *field,
                              int mem);
 
+/* nsys independent systems in one solve (a forest: one octree per system,
+ * each level's kernels run over the nodes of every system at once).
+ * System k holds particles offsets[k] .. offsets[k+1]-1 (offsets: nsys+1
+ * host int64, offsets[0] = 0, non-decreasing; n = offsets[nsys]) in the box
+ * boxes[6k .. 6k+5] = (lbx, lby, lbz, ubx, uby, ubz) (host).  Every box
+ * must have the solver's extents (ub - lb per axis, compared exactly): the
+ * operator tables are made for them; its origin is free.  xyz, q, pot and
+ * field as for aran_gpu_solver3d_solve over the n particles; each system's
+ * results equal those of a solve of that system alone in its box (up to the
+ * order of FP64 additions), and the counters are summed over the systems.
+ * The batched form of calling aran_solver3d_solve once per system
+ * (aran/aransolver3d.c:1135-1202). */
+int aran_gpu_solver3d_solve_forest (AranGpuSolver3d *s, int nsys, const int64_t *offsets,
+                                    const double *boxes, const double *xyz, const double *q,
+                                    double *pot, double *field, int mem);
+
 /* Call counters of the last solve in the order of aran_solver3d_get_stats
  * (aran/aransolver3d.c:566-586): zero, p2p, p2m, m2m, m2l, l2l, l2p, p2l,
  * m2p, p2p_remote, m2l_remote. */
