@@ -349,6 +349,8 @@ class Solver3d:
         n = len(q)
         if xyz.shape != (n, 3) or len(boxes) != nsys:
             raise ValueError("xyz must be (n, 3) and boxes (nsys, 6)")
+        if nsys < 1 or offs[0] != 0 or offs[-1] != n:
+            raise ValueError("offsets must run from 0 to the number of particles")
         pot = np.empty(n)
         fld = np.empty((n, 3)) if self.field else None
         _check(load().aran_gpu_solver3d_solve_forest(

@@ -102,7 +102,7 @@ __host__ __device__ constexpr int m2l_lane_vpre(int p, int m) {
   return m2l_lane_vtail(p) - m2l_lane_vtail(p - m);
 }
 // orders with a lane-parallel M2L kernel
-__host__ __device__ constexpr bool m2l_lane_order(int p) { return p == 8 || p == 12; }
+__host__ __device__ constexpr bool m2l_lane_order(int p) { return p == 4 || p == 8 || p == 12; }
 
 FMM_HD int sq_off(int l) { return (l * (l + 1) * (2 * l + 1)) / 6; }  // sum_{i<l} (i+1)^2
 FMM_HD int sq_size(int L) { return sq_off(L); }

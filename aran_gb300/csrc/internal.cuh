@@ -209,6 +209,11 @@ struct AranGpuSolver3d {
   // solve): particle offsets (device, nsys + 1) and per system lb[3],
   // ub[3] and the key scales 2^21 / (ub - lb) (9 doubles, host and device)
   int nsys = 1;
+  // dense M2L operators of the tensor-core kernel (m2l_tc.cu), made on
+  // first use at order tc_p
+  aran::DBuf<float> tc_tab;
+  aran::DBuf<int8_t> tc_dvec;
+  int tc_p = -1;
   aran::DBuf<int> sys_off;
   aran::DBuf<double> sys_box;
   std::vector<int> h_sys_off;
@@ -239,6 +244,10 @@ void kkylin_pass(AranGpuSolver3d *s, int stage);
 void launch_m2l(AranGpuSolver3d *s, bool fp64, int first, int count, cudaStream_t st);
 bool launch_m2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, const int *parents, int count,
                       const cplx<float> *mult, cplx<float> *loc, cudaStream_t st);
+// m2l_tc.cu: the FP32 M2L on the tensor cores (orders 8 and 12, when
+// ARAN_M2L_KERNEL is "tc"); false leaves it to the other kernels
+bool launch_m2l_tc(AranGpuSolver3d *s, const int *parents, int count, const float *mult,
+                   float *loc, cudaStream_t st);
 // p2p.cu
 constexpr int kBigRange = 2048;   // near ranges above this many particles are chunked
 void build_p2p_work(AranGpuSolver3d *s);

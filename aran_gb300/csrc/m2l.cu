@@ -423,6 +423,9 @@ void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const int *parents, int count
               const cplx<T> *mult, cplx<T> *loc, cudaStream_t st) {
   if (count <= 0) return;
   if constexpr (sizeof(T) == 4) {
+    if (launch_m2l_tc(s, parents, count, reinterpret_cast<const float *>(mult),
+                      reinterpret_cast<float *>(loc), st))
+      return;
     if (launch_m2l_lanes(s, tb, parents, count, mult, loc, st)) return;
   }
   upload_codes(s->device);

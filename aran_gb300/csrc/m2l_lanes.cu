@@ -458,6 +458,7 @@ bool launch_m2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, const int *parent
   const char *pick = getenv("ARAN_M2L_KERNEL");
   if (pick && strcmp(pick, "sibling") == 0) return false;
   switch (p) {
+    case 4: return launch_p<4>(s, tb, parents, count, mult, loc, st);
     case 8: return launch_p<8>(s, tb, parents, count, mult, loc, st);
     case 12: return launch_p<12>(s, tb, parents, count, mult, loc, st);
     default: return false;

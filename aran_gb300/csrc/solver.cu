@@ -173,7 +173,7 @@ void aran_gpu_solver3d_destroy(AranGpuSolver3d *s) {
   s->scan_tmp.release(); s->stats_dev.release(); s->err_dev.release();
   t.leaf_be.release(); t.leaf_chi.release(); t.leaf_clo.release(); t.big_items.release();
   t.parents.release(); t.big_rng.release(); t.sys.release();
-  s->sys_off.release(); s->sys_box.release();
+  s->sys_off.release(); s->sys_box.release(); s->tc_tab.release(); s->tc_dvec.release();
   s->kk64.release();
   s->kk32.release();
   for (auto &ev : s->ev)

@@ -114,7 +114,7 @@ def test_forest_argument_checks(aran):
         o2[3], o2[4] = o2[4], o2[3]        # decreasing
         with pytest.raises(aran.AranError):
             s.solve_forest(x, q, o2, boxes)
-        with pytest.raises(aran.AranError):
+        with pytest.raises(ValueError):        # the C call takes n = offsets[nsys]
             s.solve_forest(x[:-1], q[:-1], offs, boxes)
         # the solver is still usable
         pot, _ = s.solve_forest(x, q, offs, boxes)

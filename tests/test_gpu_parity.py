@@ -95,13 +95,14 @@ def test_mixed_matches_oracle(aran, oracle, case):
 M2L_KERNEL_CASES = [
     ("plummer-p12", lambda n: W.plummer(n, 31), 40000, 32, 12, (-1, -1, -1), (1, 1, 1)),
     ("uniform-p8", lambda n: W.uniform(n, 32), 30000, 16, 8, (0, 0, 0), (1, 1, 1)),
+    ("uniform-p4", lambda n: W.uniform(n, 34), 30000, 16, 4, (0, 0, 0), (1, 1, 1)),
     ("blobs-p12", lambda n: W.blobs(n, 33, nblobs=2), 9000, 8, 12, (0, 0, 0), (1, 1, 1)),
 ]
 
 
 @pytest.mark.parametrize("case", M2L_KERNEL_CASES, ids=[c[0] for c in M2L_KERNEL_CASES])
 def test_mixed_m2l_kernels_agree(aran, oracle, case, monkeypatch):
-    """The FP32 lane-parallel M2L kernel (orders 8 and 12) and the sibling
+    """The FP32 lane-parallel M2L kernel (orders 4, 8 and 12) and the sibling
     kernel (every order; ARAN_M2L_KERNEL=sibling) apply the same tables in
     FP32: both within the mixed tolerance of the oracle, and within 1e-6 of
     each other."""
@@ -120,6 +121,32 @@ def test_mixed_m2l_kernels_agree(aran, oracle, case, monkeypatch):
         assert rel_l2(fld, ofld) < MIXED_TOL, kernel
     assert rel_l2(out["lanes"][0], out["sibling"][0]) < 1e-6
     assert rel_l2(out["lanes"][1], out["sibling"][1]) < 1e-6
+
+
+TC_CASES = [c for c in M2L_KERNEL_CASES if c[4] in (8, 12)]
+
+
+@pytest.mark.parametrize("case", TC_CASES, ids=[c[0] for c in TC_CASES])
+def test_tensor_core_m2l(aran, oracle, case, monkeypatch):
+    """The tcgen05 M2L (ARAN_M2L_KERNEL=tc, orders 8 and 12) applies the same
+    operator as dense TF32 products with a hi/lo split.  Its results stay
+    within 5e-5 of the lane-parallel kernel's; the gap is the truncation of
+    the tensor core's FP32 accumulation over the ~10^4 MMAs chained into one
+    accumulator (halving the chain halves it), not the operator."""
+    name, gen, n, maxbox, p, lb, ub = case
+    x, q = gen(n)
+    out = {}
+    for kernel in ("lanes", "tc"):
+        monkeypatch.setenv("ARAN_M2L_KERNEL", kernel)
+        with aran.Solver3d(lb, ub, maxbox=maxbox, order=p, field=True, precision="mixed") as s:
+            out[kernel] = s.solve(x, q)
+            out[kernel + "_stats"] = s.get_stats()
+    monkeypatch.delenv("ARAN_M2L_KERNEL")
+    assert rel_l2(out["tc"][0], out["lanes"][0]) < 5e-5
+    assert rel_l2(out["tc"][1], out["lanes"][1]) < 5e-5
+    assert out["tc_stats"] == out["lanes_stats"]
+    opot, _ = oracle.solve(x, q, order=p, maxbox=maxbox, field=False, lb=lb, ub=ub)
+    assert rel_l2(out["tc"][0], opot) < 1e-4
 
 
 @pytest.mark.parametrize("p", [1, 2, 4, 6, 16, 20])
