@@ -38,7 +38,10 @@ EXPORTS = (
     "aran_gpu_solver2d_get_stats", "aran_gpu_solver2d_timings", "aran_gpu_solver2d_tree_info",
     "aran_gpu_solver2d_launches", "aran_gpu_solver3d_set_fp64_root_depth",
     "aran_gpu_plan_for_tolerance", "aran_gpu_solver3d_set_leaf_predicate",
+    "aran_gpu_solver3d_set_m2l_kernel", "aran_gpu_autotune3d", "aran_gpu_tune_lookup",
 )
+
+M2L_KERNELS = {"auto": 0, "lanes": 1, "sibling": 2, "tc": 3}
 
 
 class AranError(RuntimeError):
@@ -73,6 +76,17 @@ class Request3d(C.Structure):
                 ("pot", C.c_void_p), ("field", C.c_void_p), ("tolerance", C.c_double)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("maxbox", C.c_int), ("m2l_kernel", C.c_int), ("m2l_nst", C.c_int),
+                ("m2l_g", C.c_int), ("ms", C.c_double), ("candidates", C.c_int)]
+
+
+def _tune_dict(r: "TuneResult") -> dict:
+    inv = {v: k for k, v in M2L_KERNELS.items()}
+    return {"maxbox": r.maxbox, "m2l_kernel": inv.get(r.m2l_kernel, r.m2l_kernel),
+            "m2l_nst": r.m2l_nst, "m2l_g": r.m2l_g, "ms": r.ms, "candidates": r.candidates}
+
+
 class RequestInfo(C.Structure):
     _fields_ = [("status", C.c_int), ("submit_s", C.c_double), ("start_s", C.c_double),
                 ("end_s", C.c_double), ("slot", C.c_int), ("footprint_bytes", C.c_int64),
@@ -104,6 +118,14 @@ def load(build_if_missing: bool = True):
     L.aran_gpu_solver3d_solve.restype = C.c_int
     L.aran_gpu_solver3d_solve_forest.argtypes = [vp, C.c_int, i64p, dp, vp, vp, vp, vp, C.c_int]
     L.aran_gpu_solver3d_solve_forest.restype = C.c_int
+    L.aran_gpu_solver3d_set_m2l_kernel.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    L.aran_gpu_solver3d_set_m2l_kernel.restype = C.c_int
+    L.aran_gpu_autotune3d.argtypes = [C.POINTER(Config3d), C.c_int64, vp, vp, C.c_int,
+                                      C.POINTER(C.c_int), C.c_int, C.c_int, C.c_char_p,
+                                      C.POINTER(TuneResult)]
+    L.aran_gpu_autotune3d.restype = C.c_int
+    L.aran_gpu_tune_lookup.argtypes = [C.c_char_p, C.POINTER(Config3d), C.POINTER(TuneResult)]
+    L.aran_gpu_tune_lookup.restype = C.c_int
     L.aran_gpu_solver3d_get_stats.argtypes = [vp, i64p]
     L.aran_gpu_solver3d_get_stats.restype = C.c_int
     L.aran_gpu_solver3d_tree_info.argtypes = [vp, i64p]
@@ -187,6 +209,34 @@ def plan_for_tolerance(tol: float, order: int = 0) -> tuple[int, str, float]:
     if est < 0:
         raise AranError(-1, load().aran_gpu_last_error().decode())
     return cfg.order, ("mixed" if cfg.precision == PRECISIONS["mixed"] else "fp64"), est
+
+
+def autotune(xyz, q, *, maxboxes=None, reps=3, db_path=None, **cfg_kw) -> dict:
+    """Times every leaf capacity of maxboxes (None: 16 .. 128) with every M2L
+    kernel serving the configuration on the sample (host arrays) and returns
+    the fastest; with db_path the choice is kept in that profile database
+    for solvers created with maxbox=0."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    cfg = make_config(**cfg_kw)
+    res = TuneResult()
+    mb = None if maxboxes is None else (C.c_int * len(maxboxes))(*[int(m) for m in maxboxes])
+    _check(load().aran_gpu_autotune3d(C.byref(cfg), len(q), _ptr(xyz), _ptr(q), MEM_HOST, mb,
+                                      0 if maxboxes is None else len(maxboxes), int(reps),
+                                      db_path.encode() if db_path else None, C.byref(res)))
+    return _tune_dict(res)
+
+
+def tune_lookup(db_path=None, **cfg_kw):
+    """The tuned choice for a configuration from the database (None when the
+    database has none)."""
+    cfg = make_config(**cfg_kw)
+    res = TuneResult()
+    rc = load().aran_gpu_tune_lookup(db_path.encode() if db_path else None, C.byref(cfg),
+                                     C.byref(res))
+    if rc < 0:
+        raise AranError(rc, load().aran_gpu_last_error().decode())
+    return _tune_dict(res) if rc == 1 else None
 
 
 def footprint_bytes(n: int, **cfg_kw) -> int:
@@ -289,6 +339,12 @@ class Solver3d:
         self._h = h
         if fp64_root_depth is not None:
             _check(L.aran_gpu_solver3d_set_fp64_root_depth(h, int(fp64_root_depth)))
+
+    def set_m2l_kernel(self, kernel="auto", nst=0, g=0):
+        """M2L kernel of the FP32 part: "auto", "lanes", "sibling" (with nst
+        table slots and g parents per CTA, 0 = the library's), "tc"."""
+        _check(load().aran_gpu_solver3d_set_m2l_kernel(self._h, M2L_KERNELS[kernel], int(nst),
+                                                       int(g)))
 
     def set_leaf_predicate(self, fn=None):
         """Nodes about to be split for which fn(NodeView) is true stay leaves

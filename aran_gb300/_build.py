@@ -16,7 +16,7 @@ OBJ = os.path.join(ROOT, "_build", "aran_gpu")
 LIB = os.path.join(HERE, "libaran_gpu.so")
 SOURCES = ["tables.cu", "tree.cu", "passes.cu", "p2p.cu", "m2l.cu", "m2l_lanes.cu", "m2l_tc.cu", "kkylin.cu",
            "noalloc.cu", "server.cu", "solver.cu", "compat.cu", "solver2d.cu", "compat2d.cu",
-           "semifar.cu", "series3d.cu", "profiledb.cpp"]
+           "semifar.cu", "series3d.cu", "tune.cu", "profiledb.cpp"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",

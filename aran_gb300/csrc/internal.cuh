@@ -209,6 +209,10 @@ struct AranGpuSolver3d {
   // solve): particle offsets (device, nsys + 1) and per system lb[3],
   // ub[3] and the key scales 2^21 / (ub - lb) (9 doubles, host and device)
   int nsys = 1;
+  // M2L kernel of the FP32 part (ARAN_M2L_*) and a forced sibling
+  // configuration (table slots, parents per CTA; 0 = the library's)
+  int m2l_kernel = ARAN_M2L_AUTO;
+  int m2l_nst = 0, m2l_g = 0;
   // dense M2L operators of the tensor-core kernel (m2l_tc.cu), made on
   // first use at order tc_p
   aran::DBuf<float> tc_tab;
@@ -244,8 +248,8 @@ void kkylin_pass(AranGpuSolver3d *s, int stage);
 void launch_m2l(AranGpuSolver3d *s, bool fp64, int first, int count, cudaStream_t st);
 bool launch_m2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, const int *parents, int count,
                       const cplx<float> *mult, cplx<float> *loc, cudaStream_t st);
-// m2l_tc.cu: the FP32 M2L on the tensor cores (orders 8 and 12, when
-// ARAN_M2L_KERNEL is "tc"); false leaves it to the other kernels
+// m2l_tc.cu: the FP32 M2L on the tensor cores (orders 8 and 12); false
+// leaves it to the other kernels
 bool launch_m2l_tc(AranGpuSolver3d *s, const int *parents, int count, const float *mult,
                    float *loc, cudaStream_t st);
 // p2p.cu
@@ -273,6 +277,13 @@ struct Forest2dHost {
 int solve2d_impl(AranGpuSolver2d *s, int nsys, const int64_t *offs, const double *box,
                  const double *xy, const double *q, double *acc, int mem, bool tree_only);
 int forest2d_to_host(AranGpuSolver2d *s, Forest2dHost &h, bool expansions);
+
+// m2l.cu: the M2L kernel a solve of s uses (the solver's setting, else
+// $ARAN_M2L_KERNEL, else ARAN_M2L_AUTO)
+int m2l_kernel_choice(const AranGpuSolver3d *s);
+// the sibling configurations (table slots, parents per CTA) that serve
+// order p: count, and the k-th
+int m2l_sibling_configs(int p, int *nst, int *g, int k);
 
 // poll limit of the M2L consumers' waits for a table copy: 2^20, or the
 // value of ARAN_DEBUG_WAIT_POLLS (a test sets it to 0 to make the wait give

@@ -19,6 +19,8 @@
 // the error word and the CTA stops issuing copies.  At orders whose tables
 // do not fit in shared memory (NST = 0) the warps read the offset tables
 // and vertical factors straight from global memory (L2-resident).
+#include <cstring>
+
 #include "internal.cuh"
 #include "async.cuh"
 
@@ -422,11 +424,13 @@ template <typename T>
 void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const int *parents, int count,
               const cplx<T> *mult, cplx<T> *loc, cudaStream_t st) {
   if (count <= 0) return;
+  const int kern = m2l_kernel_choice(s);
   if constexpr (sizeof(T) == 4) {
-    if (launch_m2l_tc(s, parents, count, reinterpret_cast<const float *>(mult),
+    if (kern == ARAN_M2L_TENSOR &&
+        launch_m2l_tc(s, parents, count, reinterpret_cast<const float *>(mult),
                       reinterpret_cast<float *>(loc), st))
       return;
-    if (launch_m2l_lanes(s, tb, parents, count, mult, loc, st)) return;
+    if (kern != ARAN_M2L_SIBLING && launch_m2l_lanes(s, tb, parents, count, mult, loc, st)) return;
   }
   upload_codes(s->device);
   const int p = s->cfg.order;
@@ -442,6 +446,23 @@ void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const int *parents, int count
   // R = rounds of 32 lanes over the tri(p+1) local coefficients; G parents
   // per CTA (each warp takes child w of every one of them)
   const int nl = tri(p + 1);
+  // a sibling configuration set on the solver (FP32 part), when it serves nl
+  if (sizeof(T) == 4 && s->m2l_nst > 0 && s->m2l_g > 0) {
+    const int nst = s->m2l_nst, g = s->m2l_g;
+    bool ok = false;
+#define ARAN_TRY(NST_, R_, G_)                                                               \
+  if (!ok && nst == NST_ && g == G_)                                                         \
+    ok = try_launch<T, NST_, R_, G_>(s, tb, D, parents, count, mult, loc, st, dev_smem);
+    if (nl <= 96) {
+      ARAN_TRY(1, 3, 1) ARAN_TRY(2, 3, 1) ARAN_TRY(3, 3, 1)
+      ARAN_TRY(1, 3, 2) ARAN_TRY(2, 3, 2) ARAN_TRY(3, 3, 2)
+    } else if (nl <= 160) {
+      ARAN_TRY(1, 5, 1) ARAN_TRY(2, 5, 1) ARAN_TRY(3, 5, 1)
+      ARAN_TRY(1, 5, 2) ARAN_TRY(2, 5, 2)
+    }
+#undef ARAN_TRY
+    if (ok) return;
+  }
   // (two table slots keep a p <= 12 FP32 CTA under a third of the shared
   // memory, so three CTAs share an SM)
   if (nl <= 96) {
@@ -464,6 +485,28 @@ void launch_t(AranGpuSolver3d *s, OpTables<T> &tb, const int *parents, int count
 }
 
 }  // namespace
+
+int m2l_kernel_choice(const AranGpuSolver3d *s) {
+  if (s->m2l_kernel != ARAN_M2L_AUTO) return s->m2l_kernel;
+  const char *pick = getenv("ARAN_M2L_KERNEL");
+  if (pick && strcmp(pick, "sibling") == 0) return ARAN_M2L_SIBLING;
+  if (pick && strcmp(pick, "lanes") == 0) return ARAN_M2L_LANES;
+  if (pick && strcmp(pick, "tc") == 0) return ARAN_M2L_TENSOR;
+  return ARAN_M2L_AUTO;
+}
+
+int m2l_sibling_configs(int p, int *nst, int *g, int k) {
+  static const int small[6][2] = {{1, 1}, {2, 1}, {3, 1}, {1, 2}, {2, 2}, {3, 2}};
+  static const int mid[5][2] = {{1, 1}, {2, 1}, {3, 1}, {1, 2}, {2, 2}};
+  const int nl = tri(p + 1);
+  const int (*tab)[2] = nl <= 96 ? small : (nl <= 160 ? mid : nullptr);
+  const int count = nl <= 96 ? 6 : (nl <= 160 ? 5 : 0);
+  if (tab && k >= 0 && k < count) {
+    *nst = tab[k][0];
+    *g = tab[k][1];
+  }
+  return count;
+}
 
 void launch_m2l(AranGpuSolver3d *s, bool fp64, int first, int count, cudaStream_t st) {
   const int *parents = s->tree.parents.ptr + first;

@@ -449,14 +449,12 @@ bool launch_p(AranGpuSolver3d *s, OpTables<float> &tb, const int *parents, int c
 
 }  // namespace
 
-// Runs the M2L pass with the lane-parallel kernel when the order has one
-// (and ARAN_M2L_KERNEL is not "sibling"); false leaves it to m2l.cu.
+// Runs the M2L pass with the lane-parallel kernel when the order has one;
+// false leaves it to m2l.cu.
 bool launch_m2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, const int *parents, int count,
                       const cplx<float> *mult, cplx<float> *loc, cudaStream_t st) {
   const int p = s->cfg.order;
   if (!m2l_lane_order(p) || tb.dir_lanes.ptr == nullptr || count <= 0) return false;
-  const char *pick = getenv("ARAN_M2L_KERNEL");
-  if (pick && strcmp(pick, "sibling") == 0) return false;
   switch (p) {
     case 4: return launch_p<4>(s, tb, parents, count, mult, loc, st);
     case 8: return launch_p<8>(s, tb, parents, count, mult, loc, st);

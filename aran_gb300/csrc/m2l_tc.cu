@@ -421,13 +421,11 @@ bool launch_tc(AranGpuSolver3d *s, const int *parents, int count, const float *m
 
 }  // namespace
 
-// The FP32 M2L on the tensor cores at orders 8 and 12 when
-// ARAN_M2L_KERNEL is "tc"; false leaves it to the other kernels.
+// The FP32 M2L on the tensor cores at orders 8 and 12; false leaves it to
+// the other kernels.
 bool launch_m2l_tc(AranGpuSolver3d *s, const int *parents, int count, const float *mult,
                    float *loc, cudaStream_t st) {
-  const char *pick = getenv("ARAN_M2L_KERNEL");
-  if (!pick || strcmp(pick, "tc") != 0 || count <= 0) return false;
-  if (s->cfg.flavour == ARAN_FLAVOUR_KKYLIN) return false;
+  if (count <= 0 || s->cfg.flavour == ARAN_FLAVOUR_KKYLIN) return false;
   switch (s->cfg.order) {
     case 8: return launch_tc<8>(s, parents, count, mult, loc, st);
     case 12: return launch_tc<12>(s, parents, count, mult, loc, st);

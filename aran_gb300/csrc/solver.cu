@@ -78,7 +78,7 @@ int check_config(const AranGpuConfig3d *c) {
   for (int a = 0; a < 3; ++a)
     if (!(c->ub[a] > c->lb[a]) || !std::isfinite(c->lb[a]) || !std::isfinite(c->ub[a]))
       return fail(ARAN_ERR_INVALID, "bounding box must satisfy lb < ub (finite)");
-  if (c->maxbox < 1) return fail(ARAN_ERR_INVALID, "maxbox must be >= 1");
+  if (c->maxbox < 0) return fail(ARAN_ERR_INVALID, "maxbox must be >= 1 (0: the tuned value)");
   if (c->order < 1 || c->order > kMaxOrder)
     return fail(ARAN_ERR_INVALID, "order must be in [1, " + std::to_string(kMaxOrder) + "]");
   // the normal flavour (aransphericalseriesd-translate.c:507-834) applies the
@@ -116,6 +116,18 @@ int aran_gpu_solver3d_create(const AranGpuConfig3d *cfg, AranGpuSolver3d **out) 
     return fail(ARAN_ERR_NO_DEVICE, std::string("no CUDA device available: ") + cudaGetErrorString(e));
   AranGpuSolver3d *s = new AranGpuSolver3d();
   s->cfg = *cfg;
+  if (cfg->maxbox == 0) {
+    // leaf capacity and M2L kernel from the autotuner's database
+    AranGpuTuneResult tr;
+    if (aran_gpu_tune_lookup(nullptr, cfg, &tr) == 1) {
+      s->cfg.maxbox = tr.maxbox;
+      s->m2l_kernel = tr.m2l_kernel;
+      s->m2l_nst = tr.m2l_nst;
+      s->m2l_g = tr.m2l_g;
+    } else {
+      s->cfg.maxbox = 64;
+    }
+  }
   try {
     ACHECK(cudaGetDevice(&s->device));
     ACHECK(cudaStreamCreateWithFlags(&s->s0, cudaStreamNonBlocking));
@@ -434,6 +446,17 @@ int aran_gpu_solver3d_set_leaf_predicate(AranGpuSolver3d *s, AranGpuLeafPredicat
   if (!s) return fail(ARAN_ERR_INVALID, "solver is NULL");
   s->leaf_pred = pred;
   s->leaf_pred_data = pred ? user_data : nullptr;
+  return ARAN_OK;
+}
+
+int aran_gpu_solver3d_set_m2l_kernel(AranGpuSolver3d *s, int kernel, int nst, int g) {
+  if (!s) return fail(ARAN_ERR_INVALID, "solver is NULL");
+  if (kernel < ARAN_M2L_AUTO || kernel > ARAN_M2L_TENSOR) return fail(ARAN_ERR_INVALID, "unknown M2L kernel");
+  if (nst < 0 || nst > 3 || g < 0 || g > 2 || ((nst == 0) != (g == 0)))
+    return fail(ARAN_ERR_INVALID, "sibling configuration: nst in 1..3 and g in 1..2, or both 0");
+  s->m2l_kernel = kernel;
+  s->m2l_nst = nst;
+  s->m2l_g = g;
   return ARAN_OK;
 }
 

@@ -99,6 +99,56 @@ int aran_gpu_solver3d_solve_forest (AranGpuSolver3d *s, int nsys, const int64_t 
                                     const double *boxes, const double *xyz, const double *q,
                                     double *pot, double *field, int mem);
 
+/* M2L kernel of the FP32 part of mixed solves (rotation flavours):
+ * ARAN_M2L_AUTO: the lane-parallel kernel at orders 4, 8 and 12, else the
+ * sibling kernel with the library's table slots and parents per CTA;
+ * ARAN_M2L_LANES / ARAN_M2L_SIBLING: that kernel (nst table slots in {1, 2,
+ * 3} and g parents per CTA in {1, 2}; 0 and 0 = the library's choice);
+ * ARAN_M2L_TENSOR: the tcgen05 kernel at orders 8 and 12 (TF32 products with
+ * a hi/lo split; the tensor core truncates its FP32 accumulation, which
+ * leaves about 2.5e-5 relative error).  Where the chosen kernel does not
+ * serve the order the next one in the order tensor, lanes, sibling does.
+ * Without a call, $ARAN_M2L_KERNEL ("lanes", "sibling", "tc") picks. */
+#define ARAN_M2L_AUTO 0
+#define ARAN_M2L_LANES 1
+#define ARAN_M2L_SIBLING 2
+#define ARAN_M2L_TENSOR 3
+int aran_gpu_solver3d_set_m2l_kernel (AranGpuSolver3d *s, int kernel, int nst, int g);
+
+/* ---- autotuner ---------------------------------------------------------
+ * Times solves of a sample (n particles, host or device pointers by mem)
+ * with cfg's box, order, flavour, precision and field for every leaf
+ * capacity of maxboxes (NULL: 16, 24, 32, 48, 64, 96, 128) and every M2L
+ * kernel that serves the order (lane-parallel, sibling configurations;
+ * mixed precision only, the tensor-core kernel excluded for its accuracy),
+ * reps timed solves each after one untimed, and keeps the fastest device
+ * time.  The choice goes to *out and, when db_path is not NULL, into the
+ * profile database file (profiledb.ini syntax, group [aran-gpu-tune], key
+ * p<order>-<precision>-<flavour>-<field|pot>, with the timed samples under
+ * samples-<key>; other groups and keys of the file are kept).  LibAran
+ * times operators for its cost model (aran/aranprofile.c:11-60,
+ * aran/aranprofiledb.c:158-200); this tunes the GPU solve itself. */
+typedef struct
+{
+  int maxbox;
+  int m2l_kernel;      /* ARAN_M2L_* */
+  int m2l_nst, m2l_g;  /* sibling configuration (0: the library's) */
+  double ms;           /* device time of one solve of the sample */
+  int candidates;      /* configurations timed */
+} AranGpuTuneResult;
+
+int aran_gpu_autotune3d (const AranGpuConfig3d *cfg, int64_t n, const double *xyz,
+                         const double *q, int mem, const int *maxboxes, int nmaxbox,
+                         int reps, const char *db_path, AranGpuTuneResult *out);
+/* The tuned choice for cfg's order, precision, flavour and field from the
+ * database (db_path, else $ARAN_PROFILE_DB, else profiledb.ini beside
+ * libaran_gpu.so): 1 and *out filled when found, 0 when not, negative on a
+ * malformed entry.  Host only.  A solver created with cfg->maxbox == 0
+ * takes its leaf capacity and M2L kernel from here (64 and the automatic
+ * kernel when there is no entry). */
+int aran_gpu_tune_lookup (const char *db_path, const AranGpuConfig3d *cfg,
+                          AranGpuTuneResult *out);
+
 /* Call counters of the last solve in the order of aran_solver3d_get_stats
  * (aran/aransolver3d.c:566-586): zero, p2p, p2m, m2m, m2l, l2l, l2p, p2l,
  * m2p, p2p_remote, m2l_remote. */

@@ -78,7 +78,8 @@ def test_no_device_fails_loudly():
 
 def test_invalid_configs_rejected_before_device_use():
     import aran_gb300
-    bad = [dict(order=0), dict(order=99), dict(maxbox=0), dict(max_depth=30),
+    # (3D maxbox 0 is valid: the tuned leaf capacity)
+    bad = [dict(order=0), dict(order=99), dict(maxbox=-1), dict(max_depth=30),
            dict(precision=7)]
     for kw in bad:
         with pytest.raises(aran_gb300.AranError) as ei:
@@ -112,3 +113,26 @@ def test_tolerance_plan():
     assert A.plan_for_tolerance(1e-8, order=20)[:2] == (20, "fp64")
     with pytest.raises(A.AranError):
         A.plan_for_tolerance(0.0)
+
+
+def test_tune_lookup(tmp_path):
+    """The autotuner's entries are read from the profile database (host only):
+    the key names order, precision, flavour and field; other groups of the
+    file do not matter; a malformed entry is an error, a missing one None."""
+    import aran_gb300 as A
+    db = tmp_path / "profiledb.ini"
+    db.write_text("[aran-profile]\naran_development3d_m2l_rotate=1e-6;2e-7;\n\n"
+                  "[aran-gpu-tune]\n# tuned on a sample\n"
+                  "p12-mixed-rotate-field=maxbox=48;m2l=1;nst=0;g=0;ms=24.5\n"
+                  "p10-mixed-rotate-field=maxbox=32;m2l=2;nst=3;g=2;ms=40.0\n"
+                  "p8-fp64-rotate-pot=maxbox=sixteen;m2l=0\n")
+    r = A.tune_lookup(str(db), order=12, precision="mixed")
+    assert r == {"maxbox": 48, "m2l_kernel": "lanes", "m2l_nst": 0, "m2l_g": 0, "ms": 24.5,
+                 "candidates": 0}
+    r = A.tune_lookup(str(db), order=10, precision="mixed")
+    assert (r["maxbox"], r["m2l_kernel"], r["m2l_nst"], r["m2l_g"]) == (32, "sibling", 3, 2)
+    assert A.tune_lookup(str(db), order=12, precision="fp64") is None
+    assert A.tune_lookup(str(db), order=12, precision="mixed", field=False) is None
+    with pytest.raises(A.AranError):
+        A.tune_lookup(str(db), order=8, precision="fp64", field=False)
+    assert A.tune_lookup(str(tmp_path / "absent.ini"), order=12) is None
