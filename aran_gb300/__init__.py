@@ -59,7 +59,8 @@ class Config3d(C.Structure):
 
 
 class Config2d(C.Structure):
-    _fields_ = [("maxbox", C.c_int), ("order", C.c_int), ("max_depth", C.c_int)]
+    _fields_ = [("maxbox", C.c_int), ("order", C.c_int), ("max_depth", C.c_int),
+                ("precision", C.c_int)]
 
 
 class NodeView(C.Structure):
@@ -467,10 +468,11 @@ class Solver2d:
     batch of independent systems per call.
 
     ``order`` is p of ``aran_development2d_new (0, p)``, ``maxbox`` the leaf
-    capacity of ``vsg_prtree2d_new_full``.  FP64 throughout."""
+    capacity of ``vsg_prtree2d_new_full``; ``precision`` "fp64" or "mixed"
+    (FP32 scaled expansions and near-field arithmetic, FP64 sums)."""
 
-    def __init__(self, *, maxbox=32, order=20, max_depth=21):
-        cfg = Config2d(int(maxbox), int(order), int(max_depth))
+    def __init__(self, *, maxbox=32, order=20, max_depth=21, precision="fp64"):
+        cfg = Config2d(int(maxbox), int(order), int(max_depth), PRECISIONS[precision])
         h = C.c_void_p()
         _check(load().aran_gpu_solver2d_create(C.byref(cfg), C.byref(h)))
         self._h = h

@@ -503,6 +503,321 @@ __global__ void k2_l2p(int64_t n, int p, const int *__restrict__ incl, const int
   out[2 * (int64_t)o + 1] = v.im;
 }
 
+// ------------------------------------------------- mixed precision passes
+// FP32 expansions scaled by the node size h (the larger side of the
+// system's box / 2^depth): multipole ma_k = a_{-k} / h^{k-1}, local
+// la_k = b_k h^k, so every operator works on O(1) numbers whatever the
+// depth; centres, node sizes and the near-field differences stay FP64 and
+// every particle's sum is FP64.  The operators are those of the FP64 kernels
+// above with z/h in place of z (rho = h_child / h_parent = 1/2):
+//   M2M  mb_i = sum_{j<i} C(i-1, j-1) rho^{j-1} ma_j u^{i-j} + rho^{i-1} ma_i,
+//        u = (z_child - z_parent) / h_parent;
+//   M2L  la_i = (1/h) (-w)^i sum_j C(i+j-1, j-1) ma_j w^j, w = h / (zt - zs);
+//   L2L  lc_i = rho^i sum_{j>=i} C(j, i) lb_j u^{j-i};
+//   L2P  sum_k la_k ((z - zc) / h)^k;  P2M  ma_k = sum q ((z - zc) / h)^{k-1}.
+typedef cplx<float> zf;
+
+__device__ __forceinline__ double node_size2(const double *__restrict__ sysbox, int sys, int depth) {
+  const double *b = sysbox + 6 * sys;
+  return fmax(b[2] - b[0], b[3] - b[1]) * ldexp(1.0, -depth);
+}
+
+__device__ __forceinline__ float shfl_sumf(float v) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ zf zfmul(zf a, zf b) {
+  return cmake(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+
+__global__ void k2f_p2m(int nleaves, int p, const int *__restrict__ leaf_node,
+                        const int *__restrict__ begin, const int *__restrict__ end,
+                        const int *__restrict__ sysn, const uint8_t *__restrict__ depth,
+                        const double *__restrict__ sysbox, const double *__restrict__ center,
+                        const double *__restrict__ sx, const double *__restrict__ sy,
+                        const double *__restrict__ sq, zf *__restrict__ mult) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nleaves) return;
+  int node = leaf_node[warp];
+  int b = begin[node], e = end[node];
+  const double cx = center[2 * node], cy = center[2 * node + 1];
+  const double ih = 1.0 / node_size2(sysbox, sysn[node], depth[node]);
+  zf acc[3];
+  for (int k = 0; k < 3; ++k) acc[k] = cmake(0.f, 0.f);
+  for (int base = b; base < e; base += 32) {
+    int i = base + lane;
+    zf d = cmake(0.f, 0.f), tmp = cmake(0.f, 0.f);
+    if (i < e) {
+      d = cmake((float)((sx[i] - cx) * ih), (float)((sy[i] - cy) * ih));
+      tmp = cmake((float)sq[i], 0.f);
+    }
+    for (int t = 1; t < p; ++t) {
+      float re = shfl_sumf(tmp.re), im = shfl_sumf(tmp.im);
+      if ((t & 31) == lane) {
+        zf v = cmake(re, im);
+        if (t < 32) acc[0] = cadd(acc[0], v);
+        else if (t < 64) acc[1] = cadd(acc[1], v);
+        else acc[2] = cadd(acc[2], v);
+      }
+      tmp = zfmul(tmp, d);
+    }
+  }
+  const int P1 = p + 1;
+  for (int k = 0; k < 3; ++k) {
+    int t = lane + 32 * k;
+    if (t <= p) mult[(int64_t)node * P1 + t] = acc[k];
+  }
+}
+
+__global__ void k2f_m2m(int cnt, int off, int p, const int *__restrict__ child,
+                        const int *__restrict__ begin, const int *__restrict__ end,
+                        const int *__restrict__ sysn, const uint8_t *__restrict__ depth,
+                        const double *__restrict__ sysbox, const double *__restrict__ center,
+                        const float *__restrict__ binom, int nb, zf *__restrict__ mult) {
+  __shared__ zf sm[4][kMaxOrder2d + 1];
+  int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int k = blockIdx.x * (blockDim.x >> 5) + wl;
+  int node = off + k;
+  bool active = k < cnt && child[node] >= 0;
+  const int P1 = p + 1;
+  zf acc[3];
+  for (int s = 0; s < 3; ++s) acc[s] = cmake(0.f, 0.f);
+  if (active) {
+    int c0 = child[node];
+    const double px = center[2 * node], py = center[2 * node + 1];
+    const double ih = 1.0 / node_size2(sysbox, sysn[node], depth[node]);
+    for (int c = c0; c < c0 + 4; ++c) {
+      if (end[c] == begin[c]) continue;
+      __syncwarp();
+      // rho^{t-1} ma_t, rho = 1/2
+      for (int t = lane; t <= p; t += 32) {
+        const zf v = mult[(int64_t)c * P1 + t];
+        const float r = t >= 1 ? ldexpf(1.f, 1 - t) : 1.f;
+        sm[wl][t] = cmake(v.re * r, v.im * r);
+      }
+      __syncwarp();
+      const zf u = cmake((float)((center[2 * c] - px) * ih), (float)((center[2 * c + 1] - py) * ih));
+      for (int s = 0; s < 3; ++s) {
+        int i = lane + 32 * s;
+        if (i > p) break;
+        if (i == 0) {
+          acc[s] = cadd(acc[s], sm[wl][0]);
+          continue;
+        }
+        zf sum = cmake(0.f, 0.f);
+        for (int j = 1; j < i; ++j) {
+          const float bc = binom[(i - 1) * nb + (j - 1)];
+          sum = zfmul(cadd(sum, cmake(sm[wl][j].re * bc, sm[wl][j].im * bc)), u);
+        }
+        acc[s] = cadd(acc[s], cadd(sum, sm[wl][i]));
+      }
+    }
+    for (int s = 0; s < 3; ++s) {
+      int i = lane + 32 * s;
+      if (i <= p) mult[(int64_t)node * P1 + i] = acc[s];
+    }
+  }
+}
+
+// M2L, warp per target node, lane i <-> local term i.  Per source, lane j
+// makes w^j (binary powers) and s_j = ma_j w^j; then
+// la_i += (1/h) (-1)^i w^i sum_j C(i+j-1, j-1) s_j, with the s_j of the
+// source read from shared memory (double-buffered, so one __syncwarp per
+// source) and the next source's coefficients loaded while this one runs.
+__global__ void __launch_bounds__(128) k2f_m2l(int nn, int p, const int *__restrict__ far_off,
+                                               const int *__restrict__ far_src,
+                                               const int *__restrict__ sysn,
+                                               const uint8_t *__restrict__ depth,
+                                               const double *__restrict__ sysbox,
+                                               const double *__restrict__ center,
+                                               const float *__restrict__ binom, int nb,
+                                               const zf *__restrict__ mult, zf *__restrict__ loc) {
+  extern __shared__ float smemf[];
+  const int P1 = p + 1;
+  const int SP = p | 1;
+  float *tab = smemf;                    // tab[i * SP + j] = C(i+j-1, j-1)
+  zf *sbuf = reinterpret_cast<zf *>(smemf + ((P1 * SP + 1) & ~1));
+  for (int x = threadIdx.x; x < P1 * SP; x += blockDim.x) {
+    int i = x / SP, j = x % SP;
+    tab[x] = (j >= 1 && j < p) ? binom[(i + j - 1) * nb + (j - 1)] : 0.f;
+  }
+  __syncthreads();
+  int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int t = blockIdx.x * (blockDim.x >> 5) + wl;
+  if (t >= nn) return;
+  int f0 = far_off[t], f1 = far_off[t + 1];
+  if (f0 == f1) return;
+  zf *sw = sbuf + wl * 2 * 32;           // two buffers of 32 per warp
+  const double tx = center[2 * t], ty = center[2 * t + 1];
+  const double h = node_size2(sysbox, sysn[t], depth[t]), ih = 1.0 / h;
+  const float *row = tab + (lane <= p ? lane : 0) * SP;
+  zf acc = cmake(0.f, 0.f);
+  const bool mine = lane >= 1 && lane < p;   // lanes holding a source term
+  int sn = far_src[f0];
+  zf ma = mine ? mult[(int64_t)sn * P1 + lane] : cmake(0.f, 0.f);
+  for (int f = f0; f < f1; ++f) {
+    // w = h / (zt - zs): the centre offset in node sizes (small integers,
+    // exact in FP32) from FP64, its inverse in FP32
+    const float ux = (float)((tx - center[2 * sn]) * ih), uy = (float)((ty - center[2 * sn + 1]) * ih);
+    const float iu2 = 1.f / (ux * ux + uy * uy);
+    const zf w = cmake(ux * iu2, -uy * iu2);
+    // prefetch the next source's term
+    zf nma = cmake(0.f, 0.f);
+    int nsn = sn;
+    if (f + 1 < f1) {
+      nsn = far_src[f + 1];
+      if (mine) nma = mult[(int64_t)nsn * P1 + lane];
+    }
+    // w^lane by binary powers
+    zf wp = cmake(1.f, 0.f), b = w;
+    for (int e = lane; e; e >>= 1) {
+      if (e & 1) wp = zfmul(wp, b);
+      b = zfmul(b, b);
+    }
+    zf *buf = sw + 32 * (f & 1);
+    buf[lane] = zfmul(ma, wp);
+    __syncwarp();
+    if (lane <= p) {
+      zf sum = cmake(0.f, 0.f);
+      for (int j = 1; j < p; ++j) {
+        const zf sj = buf[j];
+        sum.re = fmaf(row[j], sj.re, sum.re);
+        sum.im = fmaf(row[j], sj.im, sum.im);
+      }
+      acc = cadd(acc, zfmul(sum, wp));
+    }
+    sn = nsn;
+    ma = nma;
+  }
+  // (-1)^i of every term, applied once
+  const float ihf = (float)(1.0 / h);
+  if (lane <= p) {
+    const zf a = (lane & 1) ? cmake(-acc.re, -acc.im) : acc;
+    zf *o = loc + (int64_t)t * P1 + lane;
+    *o = cadd(*o, cmake(a.re * ihf, a.im * ihf));
+  }
+}
+
+__global__ void k2f_l2l(int cnt, int off, int p, const int *__restrict__ parent,
+                        const int *__restrict__ begin, const int *__restrict__ end,
+                        const int *__restrict__ sysn, const uint8_t *__restrict__ depth,
+                        const double *__restrict__ sysbox, const double *__restrict__ center,
+                        const float *__restrict__ binom, int nb, zf *__restrict__ loc) {
+  __shared__ zf sm[4][kMaxOrder2d + 1];
+  int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int k = blockIdx.x * (blockDim.x >> 5) + wl;
+  if (k >= cnt) return;
+  int node = off + k;
+  int par = parent[node];
+  if (par < 0 || end[node] == begin[node]) return;
+  const int P1 = p + 1;
+  for (int t = lane; t <= p; t += 32) sm[wl][t] = loc[(int64_t)par * P1 + t];
+  __syncwarp();
+  const double ihp = 1.0 / node_size2(sysbox, sysn[par], depth[par]);
+  const zf u = cmake((float)((center[2 * node] - center[2 * par]) * ihp),
+                     (float)((center[2 * node + 1] - center[2 * par + 1]) * ihp));
+  for (int s = 0; s < 3; ++s) {
+    int i = lane + 32 * s;
+    if (i > p) break;
+    zf sum = sm[wl][p];
+    for (int j = p - 1; j >= i; --j) {
+      const float bc = binom[j * nb + i];
+      sum = cadd(zfmul(sum, u), cmake(sm[wl][j].re * bc, sm[wl][j].im * bc));
+    }
+    const float r = ldexpf(1.f, -i);
+    zf *o = loc + (int64_t)node * P1 + i;
+    *o = cadd(*o, cmake(sum.re * r, sum.im * r));
+  }
+}
+
+// near field, warp per target leaf: each near range is staged 32 sources at
+// a time in shared memory as FP32 positions relative to the target leaf's
+// centre (the FP64 difference rounded once), and lanes sum their targets
+// against them in FP32; a pair closer than h/8 (h the target leaf's size),
+// where that rounding would show, is recomputed from the FP64 positions.
+// FP32 partial sums per range, FP64 sums per target.
+__global__ void __launch_bounds__(128) k2f_p2p(int nleaves, const int *__restrict__ leaf_be,
+                        const int *__restrict__ near_off, const int2 *__restrict__ near_rng,
+                        const int *__restrict__ leaf_node, const int *__restrict__ sysn,
+                        const uint8_t *__restrict__ depth, const double *__restrict__ sysbox,
+                        const double *__restrict__ center, const double *__restrict__ sx,
+                        const double *__restrict__ sy, const double *__restrict__ sq,
+                        zd *__restrict__ near_acc) {
+  __shared__ float4 stg[4][32];
+  const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = blockIdx.x * 4 + wl;
+  if (warp >= nleaves) return;
+  const int b = leaf_be[warp], e = leaf_be[warp + 1];
+  const int r0 = near_off[warp], r1 = near_off[warp + 1];
+  const int node = leaf_node[warp];
+  const double cx = center[2 * node], cy = center[2 * node + 1];
+  const double hh = node_size2(sysbox, sysn[node], depth[node]);
+  const float thr2 = (float)(hh * hh / 64.0);
+  float4 *buf = stg[wl];
+  for (int base = b; base < e; base += 32) {
+    const int i = base + lane;
+    const bool on = i < e;
+    const double xi = on ? sx[i] : cx, yi = on ? sy[i] : cy;
+    const float xr = (float)(xi - cx), yr = (float)(yi - cy);
+    double re = 0.0, im = 0.0;
+    for (int r = r0; r < r1; ++r) {
+      const int2 rg = near_rng[r];
+      const int j0 = leaf_be[rg.x], j1 = leaf_be[rg.y];
+      float fr = 0.f, fi = 0.f;
+      for (int c0 = j0; c0 < j1; c0 += 32) {
+        const int cnt = min(32, j1 - c0);
+        __syncwarp();
+        if (lane < cnt) {
+          const int j = c0 + lane;
+          buf[lane] = make_float4((float)(sx[j] - cx), (float)(sy[j] - cy), (float)sq[j],
+                                  __int_as_float(j));
+        }
+        __syncwarp();
+        for (int k = 0; k < cnt; ++k) {
+          const float4 sv = buf[k];
+          float dx = xr - sv.x, dy = yr - sv.y;
+          float r2 = dx * dx + dy * dy;
+          if (r2 < thr2) {
+            const int j = __float_as_int(sv.w);
+            if (j == i || !on) continue;
+            dx = (float)(xi - sx[j]);
+            dy = (float)(yi - sy[j]);
+            r2 = dx * dx + dy * dy;
+            if (!(r2 > 0.f)) continue;
+          }
+          const float wgt = sv.z * __frcp_rn(r2);
+          fr = fmaf(dx, wgt, fr);
+          fi = fmaf(-dy, wgt, fi);
+        }
+      }
+      re += fr;
+      im += fi;
+    }
+    if (on) near_acc[i] = cmake(re, im);
+  }
+}
+
+__global__ void k2f_l2p(int64_t n, int p, const int *__restrict__ incl, const int *__restrict__ leaf_node,
+                        const int *__restrict__ sysn, const uint8_t *__restrict__ depth,
+                        const double *__restrict__ sysbox, const double *__restrict__ center,
+                        const double *__restrict__ sx, const double *__restrict__ sy,
+                        const zf *__restrict__ loc, const zd *__restrict__ near_acc,
+                        const int *__restrict__ perm, double *__restrict__ out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int node = leaf_node[incl[i] - 1];
+  const zf *a = loc + (int64_t)node * (p + 1);
+  const double ih = 1.0 / node_size2(sysbox, sysn[node], depth[node]);
+  const zf z = cmake((float)((sx[i] - center[2 * node]) * ih), (float)((sy[i] - center[2 * node + 1]) * ih));
+  zf v = a[p];
+  for (int k = p - 1; k >= 0; --k) v = cadd(zfmul(v, z), a[k]);
+  const zd nr = near_acc[i];
+  int o = perm[i];
+  out[2 * (int64_t)o] = (double)v.re + nr.re;
+  out[2 * (int64_t)o + 1] = (double)v.im + nr.im;
+}
+
 // counters: [0] sum cnt_L * sum_r cnt(r), [1] sum cnt_L^2, [2] sum cnt_L (cnt_L + 1) / 2,
 // [3] non-empty nodes with a parent
 __global__ void k2_stats(int nleaves, int nn, const int *__restrict__ leaf_be,
@@ -562,6 +877,8 @@ struct AranGpuSolver2d {
   aran::DBuf<uint8_t> depth;
   aran::DBuf<double> center;
   aran::DBuf<aran::cplx<double>> mult, loc, near_acc;
+  aran::DBuf<aran::cplx<float>> mult32, loc32;   // mixed precision: scaled FP32 expansions
+  aran::DBuf<float> binom32;
   aran::DBuf<unsigned long long> stats_dev;
   std::vector<int> level_off;
   int nnodes = 0, nlevels = 0, nleaves = 0, nrng = 0, empty_roots = 0;
@@ -789,11 +1106,79 @@ void build_lists2(AranGpuSolver2d *s) {
   ACHECK(cudaEventRecord(s->ev[2 * Stage::LISTS + 1], st));
 }
 
+void run_passes2_mixed(AranGpuSolver2d *s, double *dacc) {
+  cudaStream_t st = s->s0, s1 = s->s1;
+  const int p = s->cfg.order, P1 = p + 1;
+  const int nn = s->nnodes, nl = s->nleaves;
+  const int64_t n = s->n;
+  typedef cplx<float> zf;
+  s->mult32.reserve((size_t)nn * P1);
+  s->loc32.reserve((size_t)nn * P1);
+  s->near_acc.reserve(n);
+  ACHECK(cudaEventRecord(s->ev_lists, st));
+  ACHECK(cudaStreamWaitEvent(s1, s->ev_lists, 0));
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::P2P], s1));
+  k2f_p2p<<<ceil_div(nl, 4), 128, 0, s1>>>(nl, s->leaf_be.ptr, s->near_off.ptr, s->near_rng.ptr,
+                                            s->leaf_node.ptr, s->nsys_.ptr, s->depth.ptr,
+                                            s->sysbox.ptr, s->center.ptr, s->sx.ptr, s->sy.ptr,
+                                            s->sq.ptr, s->near_acc.ptr);
+  s->launches++;
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::P2P + 1], s1));
+  ACHECK(cudaEventRecord(s->ev_p2p, s1));
+
+  ACHECK(cudaMemsetAsync(s->mult32.ptr, 0, (size_t)nn * P1 * sizeof(zf), st));
+  ACHECK(cudaMemsetAsync(s->loc32.ptr, 0, (size_t)nn * P1 * sizeof(zf), st));
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::P2M], st));
+  k2f_p2m<<<ceil_div((int64_t)nl * 32, 128), 128, 0, st>>>(
+      nl, p, s->leaf_node.ptr, s->begin.ptr, s->end.ptr, s->nsys_.ptr, s->depth.ptr, s->sysbox.ptr,
+      s->center.ptr, s->sx.ptr, s->sy.ptr, s->sq.ptr, s->mult32.ptr);
+  s->launches++;
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::P2M + 1], st));
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::M2M], st));
+  for (int d = s->nlevels - 2; d >= 0; --d) {
+    int off = s->level_off[d], cnt = s->level_off[d + 1] - off;
+    k2f_m2m<<<ceil_div(cnt, 4), 128, 0, st>>>(cnt, off, p, s->child.ptr, s->begin.ptr, s->end.ptr,
+                                              s->nsys_.ptr, s->depth.ptr, s->sysbox.ptr,
+                                              s->center.ptr, s->binom32.ptr, s->nb, s->mult32.ptr);
+    s->launches++;
+  }
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::M2M + 1], st));
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L], st));
+  {
+    size_t smem = (size_t)(((P1 * (p | 1)) + 1) & ~1) * sizeof(float) + 4 * 2 * 32 * sizeof(zf);
+    k2f_m2l<<<ceil_div(nn, 4), 128, smem, st>>>(nn, p, s->far_off.ptr, s->far_src.ptr, s->nsys_.ptr,
+                                                 s->depth.ptr, s->sysbox.ptr, s->center.ptr,
+                                                 s->binom32.ptr, s->nb, s->mult32.ptr, s->loc32.ptr);
+    s->launches++;
+  }
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::M2L + 1], st));
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::L2L], st));
+  for (int d = 2; d < s->nlevels; ++d) {
+    int off = s->level_off[d], cnt = s->level_off[d + 1] - off;
+    k2f_l2l<<<ceil_div(cnt, 4), 128, 0, st>>>(cnt, off, p, s->parent.ptr, s->begin.ptr, s->end.ptr,
+                                              s->nsys_.ptr, s->depth.ptr, s->sysbox.ptr,
+                                              s->center.ptr, s->binom32.ptr, s->nb, s->loc32.ptr);
+    s->launches++;
+  }
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::L2L + 1], st));
+  ACHECK(cudaStreamWaitEvent(st, s->ev_p2p, 0));
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::L2P], st));
+  k2f_l2p<<<ceil_div(n, 256), 256, 0, st>>>(n, p, s->incl.ptr, s->leaf_node.ptr, s->nsys_.ptr,
+                                            s->depth.ptr, s->sysbox.ptr, s->center.ptr, s->sx.ptr,
+                                            s->sy.ptr, s->loc32.ptr, s->near_acc.ptr, s->perm.ptr,
+                                            dacc);
+  s->launches++;
+  ACHECK(cudaEventRecord(s->ev[2 * Stage::L2P + 1], st));
+}
+
 void run_passes2(AranGpuSolver2d *s, double *dacc) {
   cudaStream_t st = s->s0, s1 = s->s1;
   const int p = s->cfg.order, P1 = p + 1;
   const int nn = s->nnodes, nl = s->nleaves;
   const int64_t n = s->n;
+  if (s->cfg.precision == ARAN_PRECISION_MIXED) {
+    run_passes2_mixed(s, dacc);
+  } else {
   s->mult.reserve((size_t)nn * P1);
   s->loc.reserve((size_t)nn * P1);
   s->near_acc.reserve(n);
@@ -847,6 +1232,7 @@ void run_passes2(AranGpuSolver2d *s, double *dacc) {
                                            s->perm.ptr, dacc);
   s->launches++;
   ACHECK(cudaEventRecord(s->ev[2 * Stage::L2P + 1], st));
+  }
   // counters
   s->stats_dev.reserve(4);
   ACHECK(cudaMemsetAsync(s->stats_dev.ptr, 0, 4 * sizeof(unsigned long long), st));
@@ -863,6 +1249,10 @@ int check2(const AranGpuConfig2d *c) {
     return fail(ARAN_ERR_INVALID, "order must be in [1, " + std::to_string(kMaxOrder2d) + "]");
   if (c->max_depth < 0 || c->max_depth > kKeyBits)
     return fail(ARAN_ERR_INVALID, "max_depth must be in [0, 21]");
+  if (c->precision != ARAN_PRECISION_FP64 && c->precision != ARAN_PRECISION_MIXED)
+    return fail(ARAN_ERR_INVALID, "unknown precision");
+  if (c->precision == ARAN_PRECISION_MIXED && c->order > 31)
+    return fail(ARAN_ERR_INVALID, "mixed precision 2D solves take orders up to 31");
   return ARAN_OK;
 }
 
@@ -902,6 +1292,10 @@ int aran_gpu_solver2d_create(const AranGpuConfig2d *cfg, AranGpuSolver2d **out) 
     s->binom.reserve(b.size());
     ACHECK(cudaMemcpyAsync(s->binom.ptr, b.data(), b.size() * sizeof(double), cudaMemcpyHostToDevice,
                            s->s0));
+    std::vector<float> bf(b.begin(), b.end());
+    s->binom32.reserve(bf.size());
+    ACHECK(cudaMemcpyAsync(s->binom32.ptr, bf.data(), bf.size() * sizeof(float),
+                           cudaMemcpyHostToDevice, s->s0));
     ACHECK(cudaStreamSynchronize(s->s0));
   } catch (const CudaError &ce) {
     int r = from_cuda(ce);
@@ -954,6 +1348,9 @@ void aran_gpu_solver2d_destroy(AranGpuSolver2d *s) {
   s->mult.release();
   s->loc.release();
   s->near_acc.release();
+  s->mult32.release();
+  s->loc32.release();
+  s->binom32.release();
   s->stats_dev.release();
   for (auto &ev : s->ev)
     if (ev) cudaEventDestroy(ev);
@@ -1113,8 +1510,27 @@ int forest2d_to_host(AranGpuSolver2d *s, Forest2dHost &h, bool expansions) {
       const size_t len = (size_t)nn * (h.p + 1) * 2;
       h.mult.resize(len);
       h.loc.resize(len);
-      ACHECK(cudaMemcpy(h.mult.data(), s->mult.ptr, len * sizeof(double), cudaMemcpyDeviceToHost));
-      ACHECK(cudaMemcpy(h.loc.data(), s->loc.ptr, len * sizeof(double), cudaMemcpyDeviceToHost));
+      if (s->cfg.precision == ARAN_PRECISION_MIXED) {
+        // back from the scaled FP32 storage: a_{-k} = ma_k h^{k-1}, b_k = la_k h^-k
+        std::vector<float> m32(len), l32(len);
+        ACHECK(cudaMemcpy(m32.data(), s->mult32.ptr, len * sizeof(float), cudaMemcpyDeviceToHost));
+        ACHECK(cudaMemcpy(l32.data(), s->loc32.ptr, len * sizeof(float), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nn; ++i) {
+          const double *b = s->h_sysbox.data() + 6 * (size_t)h.sys[i];
+          const double hs = std::max(b[2] - b[0], b[3] - b[1]) * std::ldexp(1.0, -(int)h.depth[i]);
+          for (int k = 0; k <= h.p; ++k) {
+            const size_t o = 2 * ((size_t)i * (h.p + 1) + k);
+            const double fm = k >= 1 ? std::pow(hs, k - 1) : 1.0, fl = std::pow(hs, -k);
+            h.mult[o] = m32[o] * fm;
+            h.mult[o + 1] = m32[o + 1] * fm;
+            h.loc[o] = l32[o] * fl;
+            h.loc[o + 1] = l32[o + 1] * fl;
+          }
+        }
+      } else {
+        ACHECK(cudaMemcpy(h.mult.data(), s->mult.ptr, len * sizeof(double), cudaMemcpyDeviceToHost));
+        ACHECK(cudaMemcpy(h.loc.data(), s->loc.ptr, len * sizeof(double), cudaMemcpyDeviceToHost));
+      }
     }
   } catch (const CudaError &ce) {
     return from_cuda(ce);

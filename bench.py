@@ -281,10 +281,13 @@ def _cpu_job2d(args):
 
 
 def run_batched_2d(nsys: int, steps: int, order: int = 20, maxbox: int = 32) -> dict:
-    """Config 4, 2D part: one forest solve of nsys systems per step."""
+    """Config 4, 2D part: one forest solve of nsys systems per step, in FP64
+    and in mixed precision (FP32 scaled expansions and near-field arithmetic
+    on FP64 differences, FP64 sums); the headline keys are the mixed run's."""
     import numpy as np
     import torch
     import aran_gb300 as A
+    import oracle
     from aran_gb300 import workloads as W
     xy, q, offs, boxes = W.batch2d(nsys)
     n = len(q)
@@ -292,45 +295,54 @@ def run_batched_2d(nsys: int, steps: int, order: int = 20, maxbox: int = 32) -> 
     dq = torch.from_numpy(q).cuda()
     dacc = torch.empty(2 * n, dtype=torch.float64, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    rng = np.random.default_rng(9)
+    check = [(int(offs[i]), int(offs[i + 1])) for i in rng.choice(nsys, 2, replace=False)]
+    refs = []
+    for a, b in check:
+        tgt = rng.choice(b - a, min(500, b - a), replace=False).astype(np.int32)
+        refs.append((a, b, tgt, oracle.direct2d(xy[a:b], q[a:b], tgt)))
+    runs = {}
+    for prec in ("fp64", "mixed"):
+        r = {}
+        with A.Solver2d(maxbox=maxbox, order=order, precision=prec) as s:
+            for _ in range(2):
+                s.solve_device(n, dxy.data_ptr(), dq.data_ptr(), dacc.data_ptr(), offs, boxes)
+            dev_ms, stages = 0.0, []
+            for _ in range(steps):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                s.solve_device(n, dxy.data_ptr(), dq.data_ptr(), dacc.data_ptr(), offs, boxes)
+                st = s.timings()
+                stages.append(st)
+                dev_ms += st["total"]
+            r["value"] = n * steps / (dev_ms * 1e-3)
+            r["unit"] = UNIT
+            r["ms_per_step"] = dev_ms / steps
+            r["stage_ms"] = {k: round(statistics.mean(d[k] for d in stages), 3) for k in stages[0]}
+            r["tree"] = s.tree_info()
+            r["gpu_launches_per_step"] = s.launches()
+            # end to end from pageable host arrays through the public call
+            e2e_ms = 0.0
+            for _ in range(steps):
+                acc = s.solve(xy, q, offs, boxes)
+                e2e_ms += s.timings()["total"]
+            r["e2e"] = {"value": n * steps / (e2e_ms * 1e-3), "unit": UNIT,
+                        "h2d_bytes_per_step": n * 24, "d2h_bytes_per_step": n * 16}
+        worst, rl2 = 0.0, 0.0
+        for a, b, tgt, ref in refs:
+            got = acc[a:b][tgt]
+            worst = max(worst, float((np.abs(got - ref) / np.maximum(np.abs(got), np.abs(ref))).max()))
+            rl2 = max(rl2, float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+        r["accuracy"] = {"max_rel_vs_direct": worst, "rel_l2_vs_direct": rl2,
+                         "systems": len(refs), "targets_each": 500}
+        runs[prec] = r
     out = {"systems": nsys, "particles": n, "order": order, "maxbox": maxbox,
            "description": "N log-uniform in [1e3, 1e5], uniform in [-1,1]^2, q~U[-1,1], "
-                          "sum_j q_j/(z_i - z_j) (tests/dummypot.c kernel), FP64"}
-    with A.Solver2d(maxbox=maxbox, order=order) as s:
-        for _ in range(2):
-            s.solve_device(n, dxy.data_ptr(), dq.data_ptr(), dacc.data_ptr(), offs, boxes)
-        dev_ms, stages = 0.0, []
-        for _ in range(steps):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            s.solve_device(n, dxy.data_ptr(), dq.data_ptr(), dacc.data_ptr(), offs, boxes)
-            st = s.timings()
-            stages.append(st)
-            dev_ms += st["total"]
-        out["value"] = n * steps / (dev_ms * 1e-3)
-        out["unit"] = UNIT
-        out["ms_per_step"] = dev_ms / steps
-        out["stage_ms"] = {k: round(statistics.mean(d[k] for d in stages), 3) for k in stages[0]}
-        out["tree"] = s.tree_info()
-        out["gpu_launches_per_step"] = s.launches()
-        # end to end from pageable host arrays through the public call
-        e2e_ms = 0.0
-        for _ in range(steps):
-            acc = s.solve(xy, q, offs, boxes)
-            e2e_ms += s.timings()["total"]
-        out["e2e"] = {"value": n * steps / (e2e_ms * 1e-3), "unit": UNIT,
-                      "h2d_bytes_per_step": n * 24, "d2h_bytes_per_step": n * 16}
-    # accuracy on two systems against the FP64 direct sum (500 targets each)
-    import oracle
-    rng = np.random.default_rng(9)
-    worst, rl2 = 0.0, 0.0
-    for i in rng.choice(nsys, 2, replace=False):
-        a, b = int(offs[i]), int(offs[i + 1])
-        tgt = rng.choice(b - a, min(500, b - a), replace=False).astype(np.int32)
-        ref = oracle.direct2d(xy[a:b], q[a:b], tgt)
-        got = acc[a:b][tgt]
-        worst = max(worst, float((np.abs(got - ref) / np.maximum(np.abs(got), np.abs(ref))).max()))
-        rl2 = max(rl2, float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
-    out["accuracy"] = {"max_rel_vs_direct": worst, "rel_l2_vs_direct": rl2}
+                          "sum_j q_j/(z_i - z_j) (tests/dummypot.c kernel)",
+           "precision": "mixed"}
+    out.update(runs["mixed"])
+    out["fp64"] = runs["fp64"]
+    out["speedup_vs_fp64_gpu"] = runs["fp64"]["ms_per_step"] / runs["mixed"]["ms_per_step"]
     # CPU: the oracle port on a sample of the systems, one process per core
     sample = [(xy[offs[i]:offs[i + 1]], q[offs[i]:offs[i + 1]], order, maxbox)
               for i in range(0, nsys, max(1, nsys // 32))][:32]

@@ -310,6 +310,9 @@ typedef struct
   int maxbox;          /* leaf capacity (vsg_prtree2d_new_full maxbox) */
   int order;           /* p of aran_development2d_new (0, p), 1..64 */
   int max_depth;       /* quadtree depth limit, 1..21 (0 = 21) */
+  int precision;       /* ARAN_PRECISION_FP64 (0), or ARAN_PRECISION_MIXED: FP32
+                          expansions scaled by the node size and FP32 near-field
+                          arithmetic on FP64 differences, FP64 centres and sums */
 } AranGpuConfig2d;
 
 typedef struct AranGpuSolver2d AranGpuSolver2d;

@@ -131,3 +131,53 @@ def test_bad_arguments(aran):
             with pytest.raises(aran.AranError) as ei:
                 s.solve(xy, q, offs, boxes)
             assert ei.value.code == -1
+
+
+def test_c4_batch_mixed(aran, oracle):
+    """Mixed precision 2D (FP32 expansions scaled by the node size, FP32
+    near-field arithmetic on FP64 differences, FP64 sums) on the C4 batch
+    shape: same forest and counters as FP64, results within 2e-6 (rel-L2) of
+    the FP64 solve and of the direct sum."""
+    rng = np.random.default_rng(4)
+    nsys = 96
+    sizes = np.exp(rng.uniform(np.log(1e3), np.log(3e4), nsys)).astype(int)
+    xy = rng.uniform(-1, 1, (sizes.sum(), 2))
+    q = rng.uniform(-1, 1, sizes.sum())
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    boxes = np.tile([-1.0, -1.0, 1.0, 1.0], (nsys, 1))
+    with aran.Solver2d(maxbox=32, order=20) as s:
+        a64 = s.solve(xy, q, offs, boxes)
+        st64 = s.get_stats()
+    with aran.Solver2d(maxbox=32, order=20, precision="mixed") as s:
+        a32 = s.solve(xy, q, offs, boxes)
+        st32 = s.get_stats()
+    assert st32 == st64
+    e = rel_l2(a32, a64)
+    print("mixed vs fp64 rel-L2", e)
+    assert e < 2e-6
+    worst = 0.0
+    for i in rng.choice(nsys, 4, replace=False):
+        a, b = offs[i], offs[i + 1]
+        tgt = rng.choice(b - a, min(500, b - a), replace=False).astype(np.int32)
+        ref = oracle.direct2d(xy[a:b], q[a:b], tgt)
+        got = a32[a:b][tgt]
+        assert rel_l2(got, ref) < 2e-6
+        worst = max(worst, (np.abs(got - ref) / np.maximum(np.abs(got), np.abs(ref))).max())
+    print("mixed per-particle worst", worst)
+    assert worst < 1e-4
+
+
+def test_mixed_forest_systems_and_boxes(aran):
+    """Mixed precision with systems of different box sizes and origins (the
+    node scale follows each system's box) and empty or one-point systems."""
+    sizes = [3000, 0, 1, 2, 700, 5000, 64, 0, 1500]
+    xy, q, offs, boxes = forest(11, sizes)
+    with aran.Solver2d(maxbox=16, order=20) as s:
+        a64 = s.solve(xy, q, offs, boxes)
+    with aran.Solver2d(maxbox=16, order=20, precision="mixed") as s:
+        a32 = s.solve(xy, q, offs, boxes)
+    for i in range(len(sizes)):
+        a, b = offs[i], offs[i + 1]
+        if b - a < 2:
+            continue
+        assert rel_l2(a32[a:b], a64[a:b]) < 2e-6, i
