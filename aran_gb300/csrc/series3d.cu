@@ -4,10 +4,13 @@
 //
 // Containers are host memory in the reference layout
 // (aran/aransphericalseriesd-private.h:38-70).  Every operator that computes
-// runs as one launch: the inputs are copied to the device, one thread
-// repeats the reference's algorithm in FP64 (the volume of one call is
-// small; the batched solver is where the throughput is), the result comes
-// back.  Restated from the reference:
+// runs as one launch of one warp: the inputs are copied to the device, the
+// reference's algorithm runs in FP64 with the lanes sharing the independent
+// outputs (rotations: one lane per output (l, m'); vertical translations:
+// one lane per output (l, m); phase factors: one lane per Wigner row) and
+// lane 0 running the recurrences (Wigner d, harmonics, the alpha table) and
+// the O(p^2) evaluations, the result comes back.  Restated from the
+// reference:
 //   rotate / rotate_inverse   Wigner D = e^{-i m alpha} d(beta) e^{-i m' gamma},
 //                             phases only for |angle| >= 1e-5
 //                             (aranwigner.c:83-313, -rotate.c:34-153);
@@ -78,6 +81,17 @@ __device__ __forceinline__ zd zconj(zd a) { return zc(a.re, -a.im); }
 __device__ __forceinline__ zd sph_sym(zd z, int m) {   // (-1)^m conj(z)
   z = zconj(z);
   return (m & 1) ? zc(-z.re, -z.im) : z;
+}
+
+// lane of the operator's warp, and the warp-wide step of lane-strided loops
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+constexpr int kLanes = 32;
+// (l, m) of the k-th coefficient in tri order
+__device__ __forceinline__ void tri_lm(int k, int &l, int &m) {
+  l = (int)((sqrt(8.0 * k + 1.0) - 1.0) * 0.5);
+  while (tri(l + 1) <= k) ++l;
+  while (tri(l) > k) --l;
+  m = k - tri(l);
 }
 
 __device__ __forceinline__ zd *sv_pos(Sv s, int l, int m) { return s.c + tri(l) + m; }
@@ -157,43 +171,50 @@ __device__ void harmonics(int n, double ct, double st, double cp, double sp, zd 
 
 // Wigner D for l <= L with the reference's phases
 __device__ void wigner_full(int L, double a, double b, double g, double *wd, zd *W, zd *e) {
-  gen_wigner_d(L, b, wd);
+  const int lane = lane_id();
+  if (lane == 0) gen_wigner_d(L, b, wd);
+  __syncwarp();
   const int n = wig_size(L);
-  for (int i = 0; i < n; ++i) W[i] = zc(wd[i], 0.);
-  if (fabs(a) >= 1e-5) {
-    zd ex = zc(cos(a), -sin(a));
-    e[0] = zc(1., 0.);
-    for (int k = 1; k <= L; ++k) e[k] = zmul_(e[k - 1], ex);
-    for (int l = 0; l <= L; ++l)
-      for (int mp = 0; mp <= l; ++mp) {
-        zd *row = W + wig_off(l) + mp * (2 * l + 1) + l;
+  for (int i = lane; i < n; i += kLanes) W[i] = zc(wd[i], 0.);
+  // rows (l, m') of the Wigner blocks, one lane each
+  const int nrows = tri(L + 1);
+  for (int pass = 0; pass < 2; ++pass) {
+    const double ang = pass == 0 ? a : g;
+    if (!(fabs(ang) >= 1e-5)) continue;
+    __syncwarp();
+    if (lane == 0) {
+      zd ex = zc(cos(ang), -sin(ang));
+      e[0] = zc(1., 0.);
+      for (int k = 1; k <= L; ++k) e[k] = zmul_(e[k - 1], ex);
+    }
+    __syncwarp();
+    for (int rrow = lane; rrow < nrows; rrow += kLanes) {
+      int l, mp;
+      tri_lm(rrow, l, mp);
+      zd *row = W + wig_off(l) + mp * (2 * l + 1) + l;
+      if (pass == 0) {
         for (int m = l; m >= 1; --m) row[-m] = zmul_(row[-m], zconj(e[m]));
         for (int m = 0; m <= l; ++m) row[m] = zmul_(row[m], e[m]);
-      }
-  }
-  if (fabs(g) >= 1e-5) {
-    zd ex = zc(cos(g), -sin(g));
-    e[0] = zc(1., 0.);
-    for (int k = 1; k <= L; ++k) e[k] = zmul_(e[k - 1], ex);
-    for (int l = 0; l <= L; ++l)
-      for (int mp = 0; mp <= l; ++mp) {
-        zd *row = W + wig_off(l) + mp * (2 * l + 1) + l;
+      } else {
         for (int m = -l; m <= l; ++m) row[m] = zmul_(row[m], e[mp]);
       }
+    }
   }
+  __syncwarp();
 }
 
 __device__ void buffer_rotate(const zd *W, int deg, const zd *src, zd *dst) {
-  for (int l = 0; l <= deg; ++l) {
+  for (int k = lane_id(); k < tri(deg + 1); k += kLanes) {
+    int l, mp;
+    tri_lm(k, l, mp);
     const int o = tri(l);
-    for (int mp = 0; mp <= l; ++mp) {
-      const zd *row = W + wig_off(l) + mp * (2 * l + 1) + l;
-      zd sum = zc(0., 0.);
-      for (int m = -l; m < 0; ++m) sum = zadd_(sum, zmul_(row[m], sph_sym(src[o - m], -m)));
-      for (int m = 0; m <= l; ++m) sum = zadd_(sum, zmul_(row[m], src[o + m]));
-      dst[o + mp] = zadd_(dst[o + mp], sum);
-    }
+    const zd *row = W + wig_off(l) + mp * (2 * l + 1) + l;
+    zd sum = zc(0., 0.);
+    for (int m = -l; m < 0; ++m) sum = zadd_(sum, zmul_(row[m], sph_sym(src[o - m], -m)));
+    for (int m = 0; m <= l; ++m) sum = zadd_(sum, zmul_(row[m], src[o + m]));
+    dst[o + mp] = zadd_(dst[o + mp], sum);
   }
+  __syncwarp();
 }
 
 __device__ void rotate_series(Sv src, double a, double b, double g, Sv dst, Arena ar, bool inverse) {
@@ -212,8 +233,10 @@ __device__ double alpha_lm(const double *al, int l, int m) { return al[tri(l, m)
 __device__ double bl_over_bn(int l, int n) { return beta_l(l) / beta_l(n); }
 
 __device__ void local_vertical(Sv src, Sv dst, double r, double cost, const double *al) {
-  for (int l = 0; l <= dst.pd; ++l)
-    for (int m = 0; m <= l; ++m) {
+  for (int k = lane_id(); k < tri(dst.pd + 1); k += kLanes) {
+    int l, m;
+    tri_lm(k, l, m);
+    {
       zd *d = sv_pos(dst, l, m);
       double rp = 1.;
       for (int n = l; n <= src.pd; ++n) {
@@ -224,11 +247,15 @@ __device__ void local_vertical(Sv src, Sv dst, double r, double cost, const doub
         *d = zadd_(*d, zscl(s, h * factor * bl_over_bn(l, n) * rp));
       }
     }
+  }
+  __syncwarp();
 }
 
 __device__ void multipole_vertical(Sv src, Sv dst, double r, double cost, const double *al) {
-  for (int l = 0; l < dst.nd; ++l)
-    for (int m = 0; m <= l; ++m) {
+  for (int k = lane_id(); k < tri(dst.nd); k += kLanes) {
+    int l, m;
+    tri_lm(k, l, m);
+    {
       zd *d = sv_neg(dst, l, m);
       for (int n = m; n <= min(l, src.nd - 1); ++n) {
         double rp = 1.;
@@ -239,12 +266,16 @@ __device__ void multipole_vertical(Sv src, Sv dst, double r, double cost, const 
         *d = zadd_(*d, zscl(s, h * factor * bl_over_bn(l, n) * rp));
       }
     }
+  }
+  __syncwarp();
 }
 
 __device__ void m2l_vertical(Sv src, Sv dst, double r, double cost, const double *al) {
   const double ir = 1. / r;
-  for (int l = 0; l <= dst.pd; ++l)
-    for (int m = 0; m <= l; ++m) {
+  for (int k = lane_id(); k < tri(dst.pd + 1); k += kLanes) {
+    int l, m;
+    tri_lm(k, l, m);
+    {
       zd sum = zc(0., 0.);
       for (int n = m; n < src.nd; ++n) {
         double rp = 1.;
@@ -258,6 +289,8 @@ __device__ void m2l_vertical(Sv src, Sv dst, double r, double cost, const double
       zd *d = sv_pos(dst, l, m);
       *d = zadd_(*d, sum);
     }
+  }
+  __syncwarp();
 }
 
 __device__ Sv zero_series(int pd, int nd, Arena &ar) {
@@ -266,7 +299,8 @@ __device__ Sv zero_series(int pd, int nd, Arena &ar) {
   s.nd = nd;
   const size_t n = ((size_t)(pd + 1) * (pd + 2) + (size_t)nd * (nd + 1)) / 2;
   s.c = ar.takez(n);
-  for (size_t i = 0; i < n; ++i) s.c[i] = zc(0., 0.);
+  for (size_t i = lane_id(); i < n; i += kLanes) s.c[i] = zc(0., 0.);
+  __syncwarp();
   return s;
 }
 
@@ -292,7 +326,8 @@ __device__ void via_rotation(Sv src, const double xs[3], Sv dst, const double xd
 __device__ void op_translate(const SeriesOp &o, Sv src, Sv dst, Arena ar) {
   const int La = 2 * max(max(src.pd, dst.pd), max(src.nd, dst.nd)) + 4;
   double *al = ar.take(tri(La + 1));
-  gen_alpha(La, al);
+  if (lane_id() == 0) gen_alpha(La, al);
+  __syncwarp();
   via_rotation(src, o.xs, dst, o.xd, ar, dst.pd, dst.nd, [&](Sv s, Sv d, double r, double c) {
     local_vertical(s, d, r, c, al);
     if (s.nd > 0) multipole_vertical(s, d, r, -c, al);
@@ -302,7 +337,8 @@ __device__ void op_translate(const SeriesOp &o, Sv src, Sv dst, Arena ar) {
 __device__ void op_to_local(const SeriesOp &o, Sv src, Sv dst, Arena ar) {
   const int La = 2 * max(max(src.pd, dst.pd), max(src.nd, dst.nd)) + 4;
   double *al = ar.take(tri(La + 1));
-  gen_alpha(La, al);
+  if (lane_id() == 0) gen_alpha(La, al);
+  __syncwarp();
   if (o.flavour != F_ROTATE) {
     // normal / kkylin: the source's local part is translated as well
     Sv sp = src;
@@ -428,16 +464,22 @@ __device__ void op_p2x(const SeriesOp &o, Sv dst, Arena ar, bool local) {
   }
 }
 
-__global__ void k_series_op(SeriesOp o) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+// one warp: the rotations and translations share their outputs over the
+// lanes; the O(p^2) operators run on lane 0
+__global__ void __launch_bounds__(32) k_series_op(SeriesOp o) {
+  if (blockIdx.x != 0) return;
   Arena ar{o.scratch};
   Sv src{o.sp, o.sn, const_cast<zd *>(o.src)};
   Sv dst{o.dp, o.dn, o.dst};
   switch (o.kind) {
-    case S_ROTATE: rotate_series(src, o.a, o.b, o.g, dst, ar, false); break;
-    case S_ROTATE_INV: rotate_series(src, o.a, o.b, o.g, dst, ar, true); break;
-    case S_TRANSLATE: op_translate(o, src, dst, ar); break;
-    case S_TO_LOCAL: op_to_local(o, src, dst, ar); break;
+    case S_ROTATE: rotate_series(src, o.a, o.b, o.g, dst, ar, false); return;
+    case S_ROTATE_INV: rotate_series(src, o.a, o.b, o.g, dst, ar, true); return;
+    case S_TRANSLATE: op_translate(o, src, dst, ar); return;
+    case S_TO_LOCAL: op_to_local(o, src, dst, ar); return;
+    default: break;
+  }
+  if (lane_id() != 0) return;
+  switch (o.kind) {
     case S_P2M: op_p2x(o, dst, ar, false); break;
     case S_P2L: op_p2x(o, dst, ar, true); break;
     case S_EVAL:

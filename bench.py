@@ -53,6 +53,9 @@ WORKLOADS = {
                   "N=4,000,000 Plummer (a=0.05, r<=1), q~U[0,1], p=12, leaf 64, field"),
     "uniform1m": ("uniform", 1_000_000, 12, 64, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0),
                   "N=1,000,000 uniform in [0,1]^3, q~U[-1,1], p=12, leaf 64, field"),
+    # small case for full-set kernel captures (a few hundred MB on the device)
+    "plummer400k": ("plummer", 400_000, 12, 64, (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0),
+                    "N=400,000 Plummer (a=0.05, r<=1), q~U[0,1], p=12, leaf 64, field"),
 }
 
 

@@ -117,7 +117,9 @@ def test_served_results_meet_their_tolerance(aran, oracle):
         else:
             x, q = W.uniform(n, 400 + i)
             lb, ub = (0, 0, 0), (1, 1, 1)
-        reqs.append((x, q, TOLERANCES[i % 3], dict(lbound=lb, ubound=ub, maxbox=32, field=True)))
+        # order 0: the server picks order and precision from the tolerance
+        reqs.append((x, q, TOLERANCES[i % 3],
+                     dict(lbound=lb, ubound=ub, maxbox=32, order=0, field=True)))
     with aran.Server(nslots=4, hbm_budget_bytes=100e9) as sv:
         tickets = [sv.submit(x, q, tolerance=tol, **kw) for x, q, tol, kw in reqs]
         served = [sv.wait(t) for t in tickets]
