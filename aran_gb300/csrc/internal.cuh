@@ -290,11 +290,14 @@ int m2l_sibling_configs(int p, int *nst, int *g, int k);
 // up; copies already issued are still waited for with the full limit)
 int consumer_wait_polls();
 
+// raises a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes` and never lowers it: solvers of different orders on other
+// threads launch the same kernel with their own sizes at the same time
+void smem_raise(const void *kernel, size_t bytes);
 // lets a kernel use more than the default 48 KB of dynamic shared memory
 template <typename K>
 void smem_opt_in(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024)
-    ACHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  if (bytes > 48 * 1024) smem_raise(reinterpret_cast<const void *>(kernel), bytes);
 }
 
 }  // namespace aran

@@ -548,7 +548,7 @@ static void kk_passes_t(AranGpuSolver3d *s, KkTables<T> &kk, OpTables<T> &tb, cp
   const size_t sm = (size_t)kKkWarps * kk_warp_cplx(p) * sizeof(cplx<T>);
   if (stage == 0) {  // M2M, deepest level first
     if (sm > 48 * 1024)
-      ACHECK(cudaFuncSetAttribute(k_m2m_kk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      smem_opt_in(k_m2m_kk<T>, sm);
     for (int d = t.nlevels - 2; d >= 0; --d) {
       if (t.level_internal[d] == 0) continue;
       int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
@@ -562,7 +562,7 @@ static void kk_passes_t(AranGpuSolver3d *s, KkTables<T> &kk, OpTables<T> &tb, cp
   } else if (stage == 1) {  // M2L
     if (t.nlevels > 2) {
       if (sm > 48 * 1024)
-        ACHECK(cudaFuncSetAttribute(k_m2l_kk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        smem_opt_in(k_m2l_kk<T>, sm);
       int off = t.level_off[2], cnt = t.nnodes - off;
       k_m2l_kk<T><<<ceil_div(cnt, kKkWarps), TB, sm, st>>>(cnt, off, t.far_off.ptr, t.far_src.ptr,
                                                            t.far_dir.ptr, t.depth.ptr, p,
@@ -574,7 +574,7 @@ static void kk_passes_t(AranGpuSolver3d *s, KkTables<T> &kk, OpTables<T> &tb, cp
     }
   } else {  // L2L from depth 3
     if (sm > 48 * 1024)
-      ACHECK(cudaFuncSetAttribute(k_l2l_kk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      smem_opt_in(k_l2l_kk<T>, sm);
     for (int d = 3; d < t.nlevels; ++d) {
       int off = t.level_off[d], cnt = t.level_off[d + 1] - off;
       k_l2l_kk<T><<<ceil_div(cnt, kKkWarps), TB, sm, st>>>(cnt, off, t.parent.ptr, t.child.ptr,

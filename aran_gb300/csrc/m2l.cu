@@ -409,8 +409,7 @@ bool try_launch(AranGpuSolver3d *s, OpTables<T> &tb, const M2LOffsets &D, const 
   const int p = s->cfg.order;
   size_t sm = m2l_smem<T, NST, G>(p, D.stride);
   if ((int)sm > dev_smem) return false;
-  ACHECK(cudaFuncSetAttribute(k_m2l_sibling<T, NST, R, G>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  smem_opt_in(k_m2l_sibling<T, NST, R, G>, sm);
   k_m2l_sibling<T, NST, R, G><<<ceil_div(count, G), 32 * (kSibWarps + 1), sm, st>>>(
       count, parents, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
       t.ijk.ptr, t.depth.ptr, p, tb.dir_m2l.ptr, D, tb.lm.ptr, s->scale_e, mult, loc,

@@ -436,8 +436,7 @@ bool launch_p(AranGpuSolver3d *s, OpTables<float> &tb, const int *parents, int c
   int dev_smem = 0;
   ACHECK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
   if ((int)sm > dev_smem) return false;
-  ACHECK(cudaFuncSetAttribute(k_m2l_lanes<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)sm));
+  smem_opt_in(k_m2l_lanes<P>, sm);
   k_m2l_lanes<P><<<ceil_div(count, kLanePar), 32 * kLaneWarps, sm, st>>>(
       count, parents, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr,
       t.ijk.ptr, t.depth.ptr, tb.dir_lanes.ptr, s->scale_e, mult, loc, s->err_dev.ptr,

@@ -408,7 +408,7 @@ bool launch_tc(AranGpuSolver3d *s, const int *parents, int count, const float *m
   int dev_smem = 0;
   ACHECK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
   if ((int)(sm + 2048) > dev_smem) return false;
-  ACHECK(cudaFuncSetAttribute(k_m2l_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  smem_opt_in(k_m2l_tc<P>, sm);
   const int groups = ceil_div(count, kTcRows);
   k_m2l_tc<P><<<8 * groups, kTcThreads, sm, st>>>(
       count, parents, t.child.ptr, t.begin.ptr, t.end.ptr, t.col.ptr, t.ncol.ptr, t.ijk.ptr,

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 
 #include "internal.cuh"
@@ -24,6 +25,18 @@ int consumer_wait_polls() {
 }
 
 void scatter_outputs(AranGpuSolver3d *s, double *pot, double *fld);
+
+void smem_raise(const void *kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> limit;
+  int dev = 0;
+  ACHECK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &cur = limit[{dev, kernel}];
+  if (cur >= bytes) return;
+  ACHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
+}
 
 // uploads the systems of a solve (offs/boxes NULL: one system in the
 // solver's box); skipped when they equal the last solve's

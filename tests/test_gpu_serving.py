@@ -130,3 +130,26 @@ def test_served_results_meet_their_tolerance(aran, oracle):
         tg = np.random.default_rng(len(q)).choice(len(q), size=2000, replace=False)
         rp, _ = oracle.direct(x, q, targets=tg)
         assert rel_l2(pot[tg], rp) <= tol, (tol, len(q), order, prec)
+
+
+def test_concurrent_orders_share_kernels(aran):
+    """Requests of different orders run at once on the request loop's slots
+    and launch the same kernels with different shared-memory sizes (FP64 at
+    order 26 needs more than 128 KB in the M2M); each result equals the same
+    solve alone."""
+    reqs = []
+    for i, p in enumerate((26, 8, 20, 12, 24, 6)):
+        x, q = W.uniform(20000 + 1000 * i, 600 + i)
+        reqs.append((x, q, p))
+    alone = []
+    for x, q, p in reqs:
+        with aran.Solver3d(maxbox=32, order=p, field=True, precision="fp64") as s:
+            alone.append(s.solve(x, q))
+    with aran.Server(nslots=4, hbm_budget_bytes=100e9) as sv:
+        tickets = [sv.submit(x, q, maxbox=32, order=p, field=True, precision="fp64")
+                   for x, q, p in reqs]
+        outs = [sv.wait(t) for t in tickets]
+    for (pa, fa), (pm, fm, info) in zip(alone, outs):
+        assert info["status"] == 0
+        assert rel_l2(pm, pa) < TOL
+        assert rel_l2(fm, fa) < TOL
