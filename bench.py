@@ -506,6 +506,50 @@ def run_flavours(steps: int, direct_targets: int) -> dict:
     return out
 
 
+def run_c1(reps: int = 20) -> dict:
+    """Config 1: N=10,000 uniform in [0,1]^3, q~U[-1,1], p=8, leaf 20, rotate,
+    potential only (tests/newtonpot3.c's kernel).  GPU mixed and FP64 solves
+    (device time and end to end from host arrays), the oracle's
+    single-threaded solve on the host, errors against the FP64 direct sum on
+    every particle."""
+    import numpy as np
+
+    import aran_gb300 as A
+    import oracle
+    from aran_gb300 import workloads as W
+
+    x, q = W.uniform(10_000, 1)
+    n = len(q)
+    rp, _ = oracle.direct(x, q)
+
+    def rl2(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    out = {"workload": "c1", "description": "N=10,000 uniform in [0,1]^3, q~U[-1,1], p=8, "
+                                            "leaf 20, rotate, potential"}
+    for prec in ("mixed", "fp64"):
+        with A.Solver3d(maxbox=20, order=8, field=False, precision=prec) as s:
+            for _ in range(3):
+                pot, _ = s.solve(x, q)
+            dev, wall = [], []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                pot, _ = s.solve(x, q)
+                wall.append(time.perf_counter() - t0)
+                dev.append(s.timings()["total"])
+        out[prec] = {"value": n / (statistics.median(dev) * 1e-3), "unit": UNIT,
+                     "device_ms": statistics.median(dev),
+                     "e2e_ms": 1e3 * statistics.median(wall),
+                     "pot_vs_direct": rl2(pot, rp)}
+    t0 = time.perf_counter()
+    opot, _ = oracle.solve(x, q, order=8, maxbox=20, field=False, nthreads=1)
+    el = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": n / el, "unit": UNIT, "cores": 1, "kind": "port",
+                           "seconds": el, "pot_vs_direct": rl2(opot, rp),
+                           "sample": "the whole workload, one solve, one thread"}
+    return out
+
+
 def cpu_model() -> str:
     try:
         out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
@@ -799,6 +843,7 @@ def run_gpu(args):
                 "d2h_bytes_per_step": n * 8 + n * 3 * 8},
         "gpu_launches": launches,
     }
+    line["c1"] = run_c1()
     if args.flavours:
         line["flavours"] = run_flavours(max(1, min(args.steps, 5)), args.direct_targets or 10000)
     if args.serving_requests > 0:
