@@ -121,6 +121,61 @@ struct Candidate {
   int maxbox, kernel, nst, g;
 };
 
+// merges "x:value;" into the samples string of a profile-database key
+std::string merge_sample(const std::string &old, double x, double value) {
+  std::vector<std::pair<double, std::string>> items;
+  std::istringstream in(old);
+  std::string item;
+  while (std::getline(in, item, ';')) {
+    item = trim(item);
+    const size_t c = item.find(':');
+    if (c == std::string::npos) continue;
+    const double k = std::strtod(item.substr(0, c).c_str(), nullptr);
+    if (k != x) items.push_back({k, item});
+  }
+  char buf[64];
+  std::snprintf(buf, sizeof(buf), "%g:%.6e", x, value);
+  items.push_back({x, buf});
+  std::sort(items.begin(), items.end(),
+            [](const std::pair<double, std::string> &a, const std::pair<double, std::string> &b) {
+              return a.first < b.first;
+            });
+  std::string out;
+  for (const auto &it : items) out += it.second + ";";
+  return out;
+}
+
+// amortised cost of one operator call on the GPU for the chosen
+// configuration (a stage's CUDA-event time over the operations it ran),
+// stored as samples at x = order under the reference's operator names in
+// the operator-cost group, which aran_solver3d_db_profile_operators reads
+// (aran/aransolver3d.c:687-740)
+void write_operator_costs(const std::string &path, const AranGpuConfig3d *cfg,
+                          const double ms[16], const int64_t st[11]) {
+  const char *suffix = cfg->flavour == ARAN_FLAVOUR_KKYLIN ? "_kkylin"
+                       : (cfg->flavour == ARAN_FLAVOUR_NORMAL ? "" : "_rotate");
+  const char *group = std::getenv("ARAN_PROFILE_GROUP");
+  const std::string grp = group ? group : "aran-profile";
+  struct Op {
+    std::string name;
+    double ms;
+    int64_t count;
+  };
+  const Op ops[] = {{"aran_development3d_p2m", ms[4], st[2]},
+                    {std::string("aran_development3d_m2m") + suffix, ms[5], st[3]},
+                    {std::string("aran_development3d_m2l") + suffix, ms[6], st[4]},
+                    {std::string("aran_development3d_l2l") + suffix, ms[7], st[5]},
+                    {"aran_development3d_l2p", ms[8], st[6]}};
+  std::vector<std::pair<std::string, std::string>> kv;
+  for (const Op &o : ops) {
+    if (o.count <= 0 || !(o.ms > 0)) continue;
+    std::string old;
+    ini_get(path, grp, "samples-" + o.name, old);
+    kv.push_back({"samples-" + o.name, merge_sample(old, cfg->order, o.ms * 1e-3 / (double)o.count)});
+  }
+  if (!kv.empty()) ini_set(path, grp, kv);
+}
+
 }  // namespace
 }  // namespace aran
 
@@ -222,6 +277,25 @@ int aran_gpu_autotune3d(const AranGpuConfig3d *cfg, int64_t n, const double *xyz
   best.candidates = (int)cands.size();
   *out = best;
   if (path) {
+    // one more solve of the chosen configuration for the operator costs
+    AranGpuConfig3d cc = *cfg;
+    cc.maxbox = best.maxbox;
+    AranGpuSolver3d *s = nullptr;
+    int rc = aran_gpu_solver3d_create(&cc, &s);
+    if (rc) return rc;
+    double ms[16];
+    int64_t st[11];
+    rc = aran_gpu_solver3d_set_m2l_kernel(s, best.m2l_kernel, best.m2l_nst, best.m2l_g);
+    if (!rc) rc = aran_gpu_solver3d_solve(s, n, xyz, q, nullptr, nullptr, mem);
+    if (!rc) rc = aran_gpu_solver3d_timings(s, ms);
+    if (!rc) rc = aran_gpu_solver3d_get_stats(s, st);
+    aran_gpu_solver3d_destroy(s);
+    if (rc) return rc;
+    try {
+      write_operator_costs(path, cfg, ms, st);
+    } catch (const std::exception &e) {
+      return fail(ARAN_ERR_INVALID, e.what());
+    }
     char v[160];
     std::snprintf(v, sizeof(v), "maxbox=%d;m2l=%d;nst=%d;g=%d;ms=%.4f", best.maxbox,
                   best.m2l_kernel, best.m2l_nst, best.m2l_g, best.ms);

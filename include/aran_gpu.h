@@ -116,6 +116,12 @@ int aran_gpu_solver3d_solve_forest (AranGpuSolver3d *s, int nsys, const int64_t 
 int aran_gpu_solver3d_set_m2l_kernel (AranGpuSolver3d *s, int kernel, int nst, int g);
 
 /* ---- autotuner ---------------------------------------------------------
+ * With db_path it also stores, in the operator-cost group ($ARAN_PROFILE_GROUP
+ * or "aran-profile"), samples at x = order of the amortised GPU cost of one
+ * call of every development operator under the reference's names
+ * (aran_development3d_p2m, _m2m_rotate, _m2l_rotate, _l2l_rotate, _l2p;
+ * the flavour's suffix), from a solve of the chosen configuration: what
+ * aran_solver3d_db_profile_operators and aran_profile_db_* read.
  * Times solves of a sample (n particles, host or device pointers by mem)
  * with cfg's box, order, flavour, precision and field for every leaf
  * capacity of maxboxes (NULL: 16, 24, 32, 48, 64, 96, 128) and every M2L

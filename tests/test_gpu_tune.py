@@ -2,6 +2,8 @@
 sample, keeps the fastest in the profile database without disturbing the
 file's other groups, and a solver created with maxbox=0 then runs the tuned
 configuration (same results as a solver given that configuration)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -21,6 +23,19 @@ def test_autotune_roundtrip(aran, tmp_path, monkeypatch):
     assert res["maxbox"] in (16, 32, 64) and res["ms"] > 0
     text = db.read_text()
     assert "[aran-profile]" in text and "aran_development3d_p2m=1e-7;" in text
+    # operator costs under the reference's names, read back by the profile DB
+    L = aran.load()
+    L.aran_profile_db_read_file.argtypes = [C.c_char_p, C.c_char_p]
+    L.aran_profile_db_name_eval.argtypes = [C.c_char_p, C.c_double]
+    L.aran_profile_db_name_eval.restype = C.c_double
+    assert L.aran_profile_db_read_file(str(db).encode(), None)
+    for name in ("aran_development3d_m2l_rotate", "aran_development3d_m2m_rotate",
+                 "aran_development3d_l2l_rotate", "aran_development3d_p2m",
+                 "aran_development3d_l2p"):
+        cost = L.aran_profile_db_name_eval(name.encode(), 10.0)
+        assert 0 < cost < 1e-3, (name, cost)
+    # the polynomial stays for other orders; the sample wins at order 10
+    assert L.aran_profile_db_name_eval(b"aran_development3d_p2m", 3.0) == pytest.approx(1e-7)
     assert "p10-mixed-rotate-field=" in text and "samples-p10-mixed-rotate-field=" in text
     samples = text.split("samples-p10-mixed-rotate-field=")[1].splitlines()[0].split(";")
     assert len(samples) == 21
