@@ -152,10 +152,11 @@ struct OpTables {
 template <typename T>
 struct KkTables {
   int p = -1;
-  DBuf<T> alpha, beta, dirs[3];
+  DBuf<T> alpha, ialpha, beta, dirs[3];   // ialpha = 1 / alpha
   int stride[3] = {0, 0, 0};
   void release() {
     alpha.release();
+    ialpha.release();
     beta.release();
     for (auto &d : dirs) d.release();
     p = -1;

@@ -135,45 +135,59 @@ __device__ __forceinline__ T ipow(T x, int e) {
 
 // M2L: aran/aransphericalseriesd-kkylin.c:364-517, with the vertical case of
 // aran/aransphericalseriesd-translate.c:609-676 when |sin theta| < 1e-5.
-// out accumulates the (unscaled-by-1/h) local.
+// out accumulates the (unscaled-by-1/h) local.  One half-warp per source
+// (hl = lane within the half): both halves walk
+// the degrees l together (the __syncwarp calls are warp-wide), each with its
+// own source, table, partial sums and output (lane hl owns the source
+// degrees hl and hl + 16); a half whose direction is vertical takes the
+// direct case and idles through the recurrence.  The
+// ratios alpha(n)/alpha(l+n) use the reciprocal table and the radial powers
+// a running product instead of a division and a power per term.
 template <typename T>
-__device__ void kk_m2l_warp(int p, const cplx<T> *src, const T *tab, const T *alpha,
-                            const T *beta, const T *vt, cplx<T> *P, cplx<T> *Q, cplx<T> *out,
-                            int lane) {
+__device__ void kk_m2l_half(int p, bool active, const cplx<T> *src, const T *tab, const T *alpha,
+                            const T *ialpha, const T *beta, const T *vt, cplx<T> *P, cplx<T> *Q,
+                            cplx<T> *out, int hl) {
   const T r = tab[0], cost = tab[1], sint = tab[2], cosp = tab[3], sinp = tab[4];
   const T *H = tab + 8;
   const T inv_r = (T)1 / r;
   const int nl = tri(p + 1);
-  if (fabs((double)sint) < 1.e-5) {
-    for (int c = lane; c < nl; c += 32) {
+  const bool vert = active && fabs((double)sint) < 1.e-5;
+  if (vert) {
+    for (int c = hl; c < nl; c += 16) {
       int l = 0;
       while (tri(l + 1) <= c) ++l;
       int m = c - tri(l);
       cplx<T> sum = cmake<T>(0, 0);
-      for (int n = m; n < p; ++n) {
-        int k = l + n + 1;
-        T rp = ipow(inv_r, k);
-        if (k % 2 == 0) rp *= cost;
-        T f = vt[c * p + n] * rp;
+      T rp = ipow(inv_r, l + m + 1);
+      for (int n = m; n < p; ++n, rp *= inv_r) {
+        const int k = l + n + 1;
+        const T f = vt[c * p + n] * ((k % 2 == 0) ? rp * cost : rp);
         sum.re += f * src[tri(n, m)].re;
         sum.im += f * src[tri(n, m)].im;
       }
       out[c].re += sum.re;
       out[c].im += sum.im;
     }
-    __syncwarp();
-    return;
   }
+  const bool rec = active && !vert;
   const int W = p;
   const cplx<T> expp = cmake<T>(cosp, sinp);
-  const cplx<T> two_cott_expp = cmake<T>((T)2 * cost / sint * cosp, (T)2 * cost / sint * sinp);
+  const T cott2 = rec ? (T)2 * cost / sint : (T)0;
+  const cplx<T> two_cott_expp = cmake<T>(cott2 * cosp, cott2 * sinp);
   const cplx<T> exp2p = cmul(expp, expp);
+  const T isint = rec ? (T)1 / sint : (T)0;
   cplx<T> *partial = P, *partial_m_1 = Q;
   T sign = (T)1;
+  // inv_r^(l+n+1) of this lane's sources n = hl, hl + 16 (orders up to
+  // 32), advanced by inv_r per degree
+  T rpow[2] = {ipow(inv_r, hl + 1), ipow(inv_r, hl + 17)};
   for (int l = 0; l <= p; ++l) {
-    for (int n = lane; n < p; n += 32) {
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int n = hl + 16 * k;
+      if (!rec || n >= p) continue;
       const int ln = l + n;
-      const T fact = ipow(inv_r, ln + 1) * beta[ln] / beta[n];
+      const T fact = rpow[k] * beta[ln] / beta[n];
       cplx<T> s0 = cmake<T>(0, 0);
       for (int o = -n; o <= n; ++o) {
         int ao = o < 0 ? -o : o;
@@ -183,7 +197,7 @@ __device__ void kk_m2l_warp(int p, const cplx<T> *src, const T *tab, const T *al
           h = sph_sym(h, ao);
           sv = sph_sym(sv, ao);
         }
-        cfma(s0, h, sv, alpha[tri(n, ao)] / alpha[tri(ln, ao)]);
+        cfma(s0, h, sv, alpha[tri(n, ao)] * ialpha[tri(ln, ao)]);
       }
       partial[n] = cmake<T>(s0.re * fact, s0.im * fact);
       if (l > 0) {
@@ -195,11 +209,11 @@ __device__ void kk_m2l_warp(int p, const cplx<T> *src, const T *tab, const T *al
           cplx<T> sv = src[tri(n, ao)];
           if (op1 < 0) h = sph_sym(h, aop1);
           if (o < 0) sv = sph_sym(sv, ao);
-          cfma(s1, h, sv, alpha[tri(n, ao)] / alpha[tri(ln, aop1)]);
+          cfma(s1, h, sv, alpha[tri(n, ao)] * ialpha[tri(ln, aop1)]);
         }
         partial[W + n] = cmake<T>(s1.re * fact, s1.im * fact);
       }
-      const T tlf = (T)2 * (T)ln * inv_r / sint;
+      const T tlf = (T)2 * (T)ln * inv_r * isint;
       const cplx<T> tl = cmake<T>(tlf * cosp, tlf * sinp);
       for (int m = 2; m <= l; ++m) {
         cplx<T> a = cmul(two_cott_expp, partial[(m - 1) * W + n]);
@@ -208,17 +222,21 @@ __device__ void kk_m2l_warp(int p, const cplx<T> *src, const T *tab, const T *al
         partial[m * W + n] = cmake<T>(a.re + b.re - c.re, a.im + b.im - c.im);
       }
     }
+    rpow[0] *= inv_r;
+    rpow[1] *= inv_r;
     __syncwarp();
-    const T fb = beta[l] * sign;
-    for (int m = lane; m <= l; m += 32) {
-      cplx<T> sum = cmake<T>(0, 0);
-      for (int n = 0; n < p; ++n) {
-        sum.re += partial[m * W + n].re;
-        sum.im += partial[m * W + n].im;
+    if (rec) {
+      const T fb = beta[l] * sign;
+      for (int m = hl; m <= l; m += 16) {
+        cplx<T> sum = cmake<T>(0, 0);
+        for (int n = 0; n < p; ++n) {
+          sum.re += partial[m * W + n].re;
+          sum.im += partial[m * W + n].im;
+        }
+        const T f = alpha[tri(l, m)] * fb;
+        out[tri(l, m)].re += sum.re * f;
+        out[tri(l, m)].im += -sum.im * f;
       }
-      const T f = alpha[tri(l, m)] * fb;
-      out[tri(l, m)].re += sum.re * f;
-      out[tri(l, m)].im += -sum.im * f;
     }
     __syncwarp();
     cplx<T> *fl = partial;
@@ -403,7 +421,8 @@ __device__ void kk_l2l_warp(int p, const cplx<T> *src, const T *tab, const T *al
   }
 }
 
-// shared memory per warp: src (nl) + out (nl) + P, Q ((p+1)^2 each)
+// shared memory per warp: src (nl) + out (nl) + P, Q ((p+1)^2 each); the
+// M2L uses twice that (one set per half-warp)
 __host__ __device__ inline int kk_warp_cplx(int p) { return 2 * tri(p + 1) + 2 * (p + 1) * (p + 1); }
 
 constexpr int kKkWarps = 4;
@@ -412,31 +431,42 @@ template <typename T>
 __global__ void k_m2l_kk(int cnt, int off, const int *__restrict__ far_off,
                          const int *__restrict__ far_src, const uint16_t *__restrict__ far_dir,
                          const uint8_t *__restrict__ depth, int p, const T *__restrict__ dirs,
-                         int stride, const T *__restrict__ alpha, const T *__restrict__ beta,
-                         const T *__restrict__ vt, double scale_e, const cplx<T> *__restrict__ mult,
-                         cplx<T> *__restrict__ loc) {
+                         int stride, const T *__restrict__ alpha, const T *__restrict__ ialpha,
+                         const T *__restrict__ beta, const T *__restrict__ vt, double scale_e,
+                         const cplx<T> *__restrict__ mult, cplx<T> *__restrict__ loc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int t = off + blockIdx.x * kKkWarps + w;
+  const int half = lane >> 4, hl = lane & 15;
+  const int t = off + blockIdx.x * (int)(blockDim.x >> 5) + w;
   if (t >= off + cnt) return;
   const int j0 = far_off[t], j1 = far_off[t + 1];
   if (j0 == j1) return;
   const int nm = tri(p), nl = tri(p + 1);
-  cplx<T> *src = reinterpret_cast<cplx<T> *>(smem_raw) + (size_t)w * kk_warp_cplx(p);
+  cplx<T> *src = reinterpret_cast<cplx<T> *>(smem_raw) + (size_t)(2 * w + half) * kk_warp_cplx(p);
   cplx<T> *out = src + nl;
   cplx<T> *P = out + nl;
   cplx<T> *Q = P + (p + 1) * (p + 1);
-  for (int c = lane; c < nl; c += 32) out[c] = cmake<T>(0, 0);
-  for (int j = j0; j < j1; ++j) {
-    const int s = far_src[j];
+  for (int c = hl; c < nl; c += 16) out[c] = cmake<T>(0, 0);
+  for (int j = j0; j < j1; j += 2) {
+    const int jj = j + half;
+    const bool active = jj < j1;
     __syncwarp();
-    for (int c = lane; c < nm; c += 32) src[c] = mult[(size_t)s * nm + c];
+    if (active) {
+      const int s = far_src[jj];
+      for (int c = hl; c < nm; c += 16) src[c] = mult[(size_t)s * nm + c];
+    }
     __syncwarp();
-    kk_m2l_warp<T>(p, src, dirs + (size_t)far_dir[j] * stride, alpha, beta, vt, P, Q, out, lane);
+    kk_m2l_half<T>(p, active, src, dirs + (size_t)far_dir[active ? jj : j] * stride, alpha, ialpha,
+                   beta, vt, P, Q, out, hl);
   }
   __syncwarp();
+  // the two halves' locals summed
+  const cplx<T> *out1 = reinterpret_cast<const cplx<T> *>(smem_raw) +
+                        (size_t)(2 * w + 1) * kk_warp_cplx(p) + nl;
+  const cplx<T> *out0 = reinterpret_cast<const cplx<T> *>(smem_raw) + (size_t)(2 * w) * kk_warp_cplx(p) + nl;
   const T ih = (T)(ldexp(1.0, depth[t]) / scale_e);
-  for (int c = lane; c < nl; c += 32) loc[(size_t)t * nl + c] = cmake<T>(out[c].re * ih, out[c].im * ih);
+  for (int c = lane; c < nl; c += 32)
+    loc[(size_t)t * nl + c] = cmake<T>((out0[c].re + out1[c].re) * ih, (out0[c].im + out1[c].im) * ih);
 }
 
 template <typename T>
@@ -500,10 +530,13 @@ __global__ void k_l2l_kk(int cnt, int off, const int *__restrict__ parent,
 }
 
 template <typename T>
-__global__ void k_kk_scalars(int L, T *alpha, T *beta, double *scratch) {
+__global__ void k_kk_scalars(int L, T *alpha, T *ialpha, T *beta, double *scratch) {
   if (blockIdx.x || threadIdx.x) return;
   gen_alpha(L, scratch);
-  for (int i = 0; i < tri(L + 1); ++i) alpha[i] = (T)scratch[i];
+  for (int i = 0; i < tri(L + 1); ++i) {
+    alpha[i] = (T)scratch[i];
+    ialpha[i] = (T)(1.0 / scratch[i]);
+  }
   for (int l = 0; l <= L; ++l) beta[l] = (T)beta_l(l);
 }
 
@@ -514,12 +547,13 @@ void build_kk_t(AranGpuSolver3d *s, KkTables<T> &kk, cudaStream_t st) {
   kk.p = p;
   int La = 2 * p + 2;
   kk.alpha.reserve(tri(La + 1));
+  kk.ialpha.reserve(tri(La + 1));
   kk.beta.reserve(La + 1);
   DBuf<double> scratch;
   int Lh = 2 * p;
   int sstride = 3 * tri(Lh + 1) + 2 * tri(Lh + 1) + 16;
   scratch.reserve((size_t)343 * sstride + tri(La + 1));
-  k_kk_scalars<T><<<1, 1, 0, st>>>(La, kk.alpha.ptr, kk.beta.ptr, scratch.ptr);
+  k_kk_scalars<T><<<1, 1, 0, st>>>(La, kk.alpha.ptr, kk.ialpha.ptr, kk.beta.ptr, scratch.ptr);
   ACHECK(cudaGetLastError());
   double ext = s->scale_e;
   double ex = (s->cfg.ub[0] - s->cfg.lb[0]) / ext, ey = (s->cfg.ub[1] - s->cfg.lb[1]) / ext,
@@ -561,14 +595,22 @@ static void kk_passes_t(AranGpuSolver3d *s, KkTables<T> &kk, OpTables<T> &tb, cp
     }
   } else if (stage == 1) {  // M2L
     if (t.nlevels > 2) {
-      if (sm > 48 * 1024)
-        smem_opt_in(k_m2l_kk<T>, sm);
+      // two half-warp sets of buffers per warp; fewer warps per CTA where
+      // four would not fit in shared memory (FP64 at high orders)
+      const size_t per_warp = 2 * (size_t)kk_warp_cplx(p) * sizeof(cplx<T>);
+      int dev_smem = 0;
+      ACHECK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
+      int wpb = kKkWarps;
+      while (wpb > 1 && (size_t)wpb * per_warp > (size_t)dev_smem) --wpb;
+      const size_t sm2 = (size_t)wpb * per_warp;
+      smem_opt_in(k_m2l_kk<T>, sm2);
       int off = t.level_off[2], cnt = t.nnodes - off;
-      k_m2l_kk<T><<<ceil_div(cnt, kKkWarps), TB, sm, st>>>(cnt, off, t.far_off.ptr, t.far_src.ptr,
-                                                           t.far_dir.ptr, t.depth.ptr, p,
-                                                           kk.dirs[0].ptr, kk.stride[0],
-                                                           kk.alpha.ptr, kk.beta.ptr, tb.vt.ptr,
-                                                           s->scale_e, mult, loc);
+      k_m2l_kk<T><<<ceil_div(cnt, wpb), 32 * wpb, sm2, st>>>(cnt, off, t.far_off.ptr, t.far_src.ptr,
+                                                            t.far_dir.ptr, t.depth.ptr, p,
+                                                            kk.dirs[0].ptr, kk.stride[0],
+                                                            kk.alpha.ptr, kk.ialpha.ptr,
+                                                            kk.beta.ptr, tb.vt.ptr, s->scale_e,
+                                                            mult, loc);
       ACHECK(cudaGetLastError());
       s->launches++;
     }

@@ -104,6 +104,10 @@ int check_config(const AranGpuConfig3d *c) {
     return fail(ARAN_ERR_INVALID, "unknown precision");
   if (c->max_depth < 0 || c->max_depth > kKeyBits)
     return fail(ARAN_ERR_INVALID, "max_depth must be in [0, 21]");
+  // the kkylin M2L scales by alpha(n, m) / alpha(l + n, m) with l + n up to
+  // 2p; 1 / (2p)! leaves the FP32 range above order 16
+  if (c->flavour == ARAN_FLAVOUR_KKYLIN && c->precision == ARAN_PRECISION_MIXED && c->order > 16)
+    return fail(ARAN_ERR_INVALID, "mixed-precision kkylin takes orders up to 16");
   return ARAN_OK;
 }
 
