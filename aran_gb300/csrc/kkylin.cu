@@ -427,25 +427,43 @@ __host__ __device__ inline int kk_warp_cplx(int p) { return 2 * tri(p + 1) + 2 *
 
 constexpr int kKkWarps = 4;
 
+// per half-warp of the M2L: src, out, P, Q and the direction's table
+// (stride T values), in complex units
+__host__ __device__ inline int kk_m2l_half_cplx(int p, int stride) {
+  return kk_warp_cplx(p) + (stride + 1) / 2;
+}
+
 template <typename T>
 __global__ void k_m2l_kk(int cnt, int off, const int *__restrict__ far_off,
                          const int *__restrict__ far_src, const uint16_t *__restrict__ far_dir,
                          const uint8_t *__restrict__ depth, int p, const T *__restrict__ dirs,
-                         int stride, const T *__restrict__ alpha, const T *__restrict__ ialpha,
-                         const T *__restrict__ beta, const T *__restrict__ vt, double scale_e,
-                         const cplx<T> *__restrict__ mult, cplx<T> *__restrict__ loc) {
+                         int stride, const T *__restrict__ alpha_g, const T *__restrict__ ialpha_g,
+                         int nalpha, const T *__restrict__ beta, const T *__restrict__ vt,
+                         double scale_e, const cplx<T> *__restrict__ mult,
+                         cplx<T> *__restrict__ loc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int half = lane >> 4, hl = lane & 15;
+  // alpha and 1/alpha for the block, then per warp two half sets
+  T *alpha = reinterpret_cast<T *>(smem_raw);
+  T *ialpha = alpha + nalpha;
+  for (int i = threadIdx.x; i < nalpha; i += blockDim.x) {
+    alpha[i] = alpha_g[i];
+    ialpha[i] = ialpha_g[i];
+  }
+  __syncthreads();
   const int t = off + blockIdx.x * (int)(blockDim.x >> 5) + w;
   if (t >= off + cnt) return;
   const int j0 = far_off[t], j1 = far_off[t + 1];
   if (j0 == j1) return;
   const int nm = tri(p), nl = tri(p + 1);
-  cplx<T> *src = reinterpret_cast<cplx<T> *>(smem_raw) + (size_t)(2 * w + half) * kk_warp_cplx(p);
+  const int hsz = kk_m2l_half_cplx(p, stride);
+  cplx<T> *base = reinterpret_cast<cplx<T> *>(smem_raw + ((2 * nalpha * sizeof(T) + 15) & ~(size_t)15));
+  cplx<T> *src = base + (size_t)(2 * w + half) * hsz;
   cplx<T> *out = src + nl;
   cplx<T> *P = out + nl;
   cplx<T> *Q = P + (p + 1) * (p + 1);
+  T *tab = reinterpret_cast<T *>(Q + (p + 1) * (p + 1));
   for (int c = hl; c < nl; c += 16) out[c] = cmake<T>(0, 0);
   for (int j = j0; j < j1; j += 2) {
     const int jj = j + half;
@@ -454,16 +472,16 @@ __global__ void k_m2l_kk(int cnt, int off, const int *__restrict__ far_off,
     if (active) {
       const int s = far_src[jj];
       for (int c = hl; c < nm; c += 16) src[c] = mult[(size_t)s * nm + c];
+      const T *tg = dirs + (size_t)far_dir[jj] * stride;
+      for (int c = hl; c < stride; c += 16) tab[c] = tg[c];
     }
     __syncwarp();
-    kk_m2l_half<T>(p, active, src, dirs + (size_t)far_dir[active ? jj : j] * stride, alpha, ialpha,
-                   beta, vt, P, Q, out, hl);
+    kk_m2l_half<T>(p, active, src, tab, alpha, ialpha, beta, vt, P, Q, out, hl);
   }
   __syncwarp();
   // the two halves' locals summed
-  const cplx<T> *out1 = reinterpret_cast<const cplx<T> *>(smem_raw) +
-                        (size_t)(2 * w + 1) * kk_warp_cplx(p) + nl;
-  const cplx<T> *out0 = reinterpret_cast<const cplx<T> *>(smem_raw) + (size_t)(2 * w) * kk_warp_cplx(p) + nl;
+  const cplx<T> *out0 = base + (size_t)(2 * w) * hsz + nl;
+  const cplx<T> *out1 = base + (size_t)(2 * w + 1) * hsz + nl;
   const T ih = (T)(ldexp(1.0, depth[t]) / scale_e);
   for (int c = lane; c < nl; c += 32)
     loc[(size_t)t * nl + c] = cmake<T>((out0[c].re + out1[c].re) * ih, (out0[c].im + out1[c].im) * ih);
@@ -597,18 +615,20 @@ static void kk_passes_t(AranGpuSolver3d *s, KkTables<T> &kk, OpTables<T> &tb, cp
     if (t.nlevels > 2) {
       // two half-warp sets of buffers per warp; fewer warps per CTA where
       // four would not fit in shared memory (FP64 at high orders)
-      const size_t per_warp = 2 * (size_t)kk_warp_cplx(p) * sizeof(cplx<T>);
+      const int nalpha = tri(2 * p + 3);
+      const size_t head = (2 * (size_t)nalpha * sizeof(T) + 15) & ~(size_t)15;
+      const size_t per_warp = 2 * (size_t)kk_m2l_half_cplx(p, kk.stride[0]) * sizeof(cplx<T>);
       int dev_smem = 0;
       ACHECK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
       int wpb = kKkWarps;
-      while (wpb > 1 && (size_t)wpb * per_warp > (size_t)dev_smem) --wpb;
-      const size_t sm2 = (size_t)wpb * per_warp;
+      while (wpb > 1 && head + (size_t)wpb * per_warp > (size_t)dev_smem) --wpb;
+      const size_t sm2 = head + (size_t)wpb * per_warp;
       smem_opt_in(k_m2l_kk<T>, sm2);
       int off = t.level_off[2], cnt = t.nnodes - off;
       k_m2l_kk<T><<<ceil_div(cnt, wpb), 32 * wpb, sm2, st>>>(cnt, off, t.far_off.ptr, t.far_src.ptr,
                                                             t.far_dir.ptr, t.depth.ptr, p,
                                                             kk.dirs[0].ptr, kk.stride[0],
-                                                            kk.alpha.ptr, kk.ialpha.ptr,
+                                                            kk.alpha.ptr, kk.ialpha.ptr, nalpha,
                                                             kk.beta.ptr, tb.vt.ptr, s->scale_e,
                                                             mult, loc);
       ACHECK(cudaGetLastError());
