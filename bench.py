@@ -70,6 +70,62 @@ def m2l_flops_rotate(p: int) -> int:
     return 4 * (a(p - 1) + p * (p + 1) * (p + 2) // 3 + a(p))
 
 
+def m2m_flops_rotate(p: int) -> int:
+    """Algorithmic flops of one rotate M2M: 8 A(p-1) + 4 sum_{l<p} (l+1)(l+2)/2
+    (two real-d rotations of the tri(p) multipole and the vertical shift)."""
+    a = lambda L: (L + 1) * (L + 2) * (4 * L + 3) // 6
+    return 8 * a(p - 1) + 4 * sum((l + 1) * (l + 2) // 2 for l in range(p))
+
+
+def l2l_flops_rotate(p: int) -> int:
+    """Algorithmic flops of one rotate L2L: 8 A(p) + 4 sum_{l<=p} sum_{m<=l}
+    (p - l + 1) (two rotations of the tri(p+1) local and the vertical shift)."""
+    a = lambda L: (L + 1) * (L + 2) * (4 * L + 3) // 6
+    return 8 * a(p) + 4 * sum((p - l + 1) * (l + 1) for l in range(p + 1))
+
+
+def p2m_flops(p: int) -> int:
+    """Algorithmic flops of P2M per particle: 16 tri(p)."""
+    return 16 * p * (p + 1) // 2
+
+
+def l2p_flops(p: int) -> int:
+    """Algorithmic flops of L2P with the gradient per particle: 32 tri(p+1)."""
+    return 32 * (p + 1) * (p + 2) // 2
+
+
+def stage_rooflines(stage_ms: dict, stats: dict, info: dict, n: int, p: int, fp32_tflops: float,
+                    hbm_gbs: float) -> dict:
+    """Ideal time of every stage against its bound (FP32 CUDA-core peak for
+    the expansion and near-field stages, HBM for sort/tree/lists) from the
+    algorithmic work: P2P 20 flops per directed pair (2 x the pair counter),
+    M2L F(p) per translation, M2M/L2L by their rotate definitions per
+    translation, P2M 16 tri(p) and L2P 32 tri(p+1) per particle, tree 80 B per
+    particle (32 B read, 32 B sorted copy, 16 B key and permutation); the
+    fraction is ideal / measured, and the sum of ideal times over the step's
+    measured time is the step's roofline fraction."""
+    peak = fp32_tflops * 1e12
+    work = {
+        "p2p": (20.0 * 2 * stats["p2p"], "flop"),
+        "m2l": (float(info["far"]) * m2l_flops_rotate(p), "flop"),
+        "m2m": (float(stats["m2m"]) * m2m_flops_rotate(p), "flop"),
+        "l2l": (float(stats["l2l"]) * l2l_flops_rotate(p), "flop"),
+        "p2m": (float(n) * p2m_flops(p), "flop"),
+        "l2p": (float(n) * l2p_flops(p), "flop"),
+        "sort+tree+lists": (80.0 * n, "byte"),
+    }
+    out, ideal_total = {}, 0.0
+    for k, (w, unit) in work.items():
+        meas = (sum(stage_ms[x] for x in ("sort", "tree", "lists")) if k == "sort+tree+lists"
+                else stage_ms[k])
+        ideal = 1e3 * (w / peak if unit == "flop" else w / (hbm_gbs * 1e9))
+        ideal_total += ideal
+        out[k] = {"work": w, "unit": unit, "ideal_ms": round(ideal, 4),
+                  "measured_ms": round(meas, 4), "frac": round(ideal / meas, 4) if meas else None}
+    out["sum_ideal_over_step"] = round(ideal_total / stage_ms["total"], 4)
+    return out
+
+
 def m2l_flops(p: int) -> int:
     """Algorithmic flops of one rotate-flavour M2L as the GPU applies it:
     2 flops per multiply-add of
@@ -810,6 +866,8 @@ def run_gpu(args):
                               "hbm_peak_gbs": peaks.get("hbm_gbs")},
         "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on "
                            "this workload" if traffic is not None else "not captured"),
+        "stages": stage_rooflines(stage_ms, stats, info, n, p, fp32_peak,
+                                  peaks.get("hbm_gbs") or 6800.0),
         "bf16_tensor_peak_tflops": peaks.get("bf16_tflops"),
         "tensor_frac": (round(achieved / peaks["bf16_tflops"], 4)
                         if peaks.get("bf16_tflops") else None),

@@ -45,3 +45,36 @@ def test_rotate_operator_flops():
         assert bench.m2l_flops_rotate(p) == 4 * (a(p - 1) + b(p) + a(p)), p
     assert (bench.m2l_flops_rotate(8), bench.m2l_flops_rotate(12),
             bench.m2l_flops_rotate(16)) == (4548, 13988, 31620)
+
+
+def test_m2m_l2l_p2m_l2p_flops():
+    """The per-translation and per-particle counts of the other stages,
+    enumerated: M2M = two real-d rotations of degrees < p (2 x 4 A(p-1)) plus
+    the vertical shift of multipole (l, m) from degrees n <= l (4 per term);
+    L2L the same with degrees <= p and the local shift from degrees n >= l;
+    P2M 16 flops and L2P with gradient 32 flops per coefficient."""
+    def a(L):
+        return sum((l + 1) * (2 * l + 1) for l in range(L + 1))
+
+    for p in (4, 8, 12, 16):
+        shift_m = sum(1 for l in range(p) for m in range(l + 1))            # tri(p) outputs
+        vert_m = sum(l + 1 for l in range(p))                               # (l+1)(l+2)/2 summed
+        assert bench.m2m_flops_rotate(p) == 8 * a(p - 1) + 4 * sum(
+            (l + 1) * (l + 2) // 2 for l in range(p)), p
+        assert shift_m == p * (p + 1) // 2 and vert_m == p * (p + 1) // 2
+        vert_l = sum(p - l + 1 for l in range(p + 1) for m in range(l + 1))
+        assert bench.l2l_flops_rotate(p) == 8 * a(p) + 4 * vert_l, p
+        assert bench.p2m_flops(p) == 16 * (p * (p + 1) // 2)
+        assert bench.l2p_flops(p) == 32 * ((p + 1) * (p + 2) // 2)
+
+
+def test_stage_rooflines_arithmetic():
+    stage_ms = {"total": 10.0, "sort": 0.5, "tree": 0.5, "lists": 0.5, "p2p": 2.0, "m2l": 5.0,
+                "m2m": 0.5, "l2l": 0.5, "p2m": 0.25, "l2p": 0.25}
+    stats = {"p2p": 1_000_000, "m2m": 1000, "l2l": 1000}
+    r = bench.stage_rooflines(stage_ms, stats, {"far": 100_000}, 100_000, 12, 80.0, 8000.0)
+    assert r["m2l"]["ideal_ms"] == round(1e3 * 100_000 * 13988 / 80e12, 4)
+    assert r["p2p"]["work"] == 40e6
+    assert r["sort+tree+lists"]["measured_ms"] == 1.5
+    total = sum(v["ideal_ms"] for k, v in r.items() if isinstance(v, dict))
+    assert abs(r["sum_ideal_over_step"] - total / 10.0) < 1e-3
