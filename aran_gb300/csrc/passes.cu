@@ -385,14 +385,17 @@ __global__ void k_l2l_rotate(int cnt, int off, const int *__restrict__ parent,
 // d/dx - i d/dy of a degree-p local are degree-(p-1) locals built once per
 // leaf, so a particle only evaluates S_l^m(xhat) once.
 // ---------------------------------------------------------------------------
-template <typename T, bool FIELD>
+// PC > 0: the order as a compile-time constant (loops unrolled, indices
+// folded); PC = 0: the order p at run time
+template <typename T, bool FIELD, int PC = 0>
 __global__ void k_l2p(int nleaves, const int *__restrict__ leaf_node, const int *__restrict__ begin,
                       const int *__restrict__ end, const uint8_t *__restrict__ depth,
-                      const real4<T> *__restrict__ rel, int p, const T *__restrict__ rec_g,
+                      const real4<T> *__restrict__ rel, int p_rt, const T *__restrict__ rec_g,
                       const T *__restrict__ gz_g, const T *__restrict__ gm_g, double scale_e,
                       const cplx<T> *__restrict__ loc, double *__restrict__ acc_pot,
                       double *__restrict__ acc_fld) {
   extern __shared__ unsigned char smem_raw[];
+  const int p = PC > 0 ? PC : p_rt;
   const int nl = tri(p + 1), nm = tri(p);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   T *rec = reinterpret_cast<T *>(smem_raw);
@@ -445,6 +448,7 @@ __global__ void k_l2p(int nleaves, const int *__restrict__ leaf_node, const int 
     T r2 = x * x + y * y + z * z;
     T phi = 0, dz = 0, gre = 0, gim = 0;
     cplx<T> diag = cmake<T>(rec[0], 0);
+#pragma unroll 1
     for (int m = 0; m <= p; ++m) {
       if (m > 0) {
         T a = rec[2 * tri(m, m)];
@@ -453,6 +457,7 @@ __global__ void k_l2p(int nleaves, const int *__restrict__ leaf_node, const int 
       cplx<T> s1 = diag, s2 = cmake<T>(0, 0);
       const T wm = m == 0 ? (T)1 : (T)2;
       const T sg = (m & 1) ? (T)-1 : (T)1;
+#pragma unroll 4
       for (int l = m; l <= p; ++l) {
         cplx<T> S;
         if (l == m) S = diag;
@@ -723,7 +728,14 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
     smem_opt_in(k_l2p<T, true>, sm);
     smem_opt_in(k_l2p<T, false>, sm);
     const int nb = ceil_div(t.nleaves, LPB);
-    if (field)
+    if (sizeof(T) == 4 && field && (p == 8 || p == 12)) {
+      // the bench orders with the order folded in at compile time
+      auto kern = p == 8 ? k_l2p<T, true, 8> : k_l2p<T, true, 12>;
+      smem_opt_in(kern, sm);
+      kern<<<nb, 32 * LPB, sm, st>>>(t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
+                                     t.depth.ptr, rel, p, tb.rec.ptr, tb.gz.ptr, tb.gm.ptr,
+                                     s->scale_e, loc, s->acc_pot.ptr, s->acc_fld.ptr);
+    } else if (field)
       k_l2p<T, true><<<nb, 32 * LPB, sm, st>>>(t.nleaves, t.leaf_node.ptr, t.begin.ptr, t.end.ptr,
                                                  t.depth.ptr, rel, p, tb.rec.ptr, tb.gz.ptr,
                                                  tb.gm.ptr, s->scale_e, loc, s->acc_pot.ptr,
