@@ -105,8 +105,9 @@ int aran_gpu_solver3d_solve_forest (AranGpuSolver3d *s, int nsys, const int64_t 
  * ARAN_M2L_LANES / ARAN_M2L_SIBLING: that kernel (nst table slots in {1, 2,
  * 3} and g parents per CTA in {1, 2}; 0 and 0 = the library's choice);
  * ARAN_M2L_TENSOR: the tcgen05 kernel at orders 8 and 12 (TF32 products with
- * a hi/lo split; the tensor core truncates its FP32 accumulation, which
- * leaves about 2.5e-5 relative error).  Where the chosen kernel does not
+ * a hi/lo split, the accumulator drained into FP32 registers per offset;
+ * about twice the FP32 kernels' rounding error, 5e-7 against 3e-7 relative
+ * at order 12).  Where the chosen kernel does not
  * serve the order the next one in the order tensor, lanes, sibling does.
  * Without a call, $ARAN_M2L_KERNEL ("lanes", "sibling", "tc") picks. */
 #define ARAN_M2L_AUTO 0
@@ -126,7 +127,8 @@ int aran_gpu_solver3d_set_m2l_kernel (AranGpuSolver3d *s, int kernel, int nst, i
  * with cfg's box, order, flavour, precision and field for every leaf
  * capacity of maxboxes (NULL: 16, 24, 32, 48, 64, 96, 128) and every M2L
  * kernel that serves the order (lane-parallel, sibling configurations;
- * mixed precision only, the tensor-core kernel excluded for its accuracy),
+ * mixed precision only; the tensor-core kernel is no candidate, as it
+ * trades accuracy for time),
  * reps timed solves each after one untimed, and keeps the fastest device
  * time.  The choice goes to *out and, when db_path is not NULL, into the
  * profile database file (profiledb.ini syntax, group [aran-gpu-tune], key

@@ -129,10 +129,11 @@ TC_CASES = [c for c in M2L_KERNEL_CASES if c[4] in (8, 12)]
 @pytest.mark.parametrize("case", TC_CASES, ids=[c[0] for c in TC_CASES])
 def test_tensor_core_m2l(aran, oracle, case, monkeypatch):
     """The tcgen05 M2L (ARAN_M2L_KERNEL=tc, orders 8 and 12) applies the same
-    operator as dense TF32 products with a hi/lo split.  Its results stay
-    within 5e-5 of the lane-parallel kernel's; the gap is the truncation of
-    the tensor core's FP32 accumulation over the ~10^4 MMAs chained into one
-    accumulator (halving the chain halves it), not the operator."""
+    operator as dense TF32 products with a hi/lo split, its accumulator
+    drained into FP32 registers after every offset.  Its results stay within
+    2e-6 of the lane-parallel kernel's (measured 6-7e-7: the dropped lo*lo
+    product and the tensor core's accumulation within one offset) and within
+    the mixed tolerance of the oracle's FP64 solve."""
     name, gen, n, maxbox, p, lb, ub = case
     x, q = gen(n)
     out = {}
@@ -142,11 +143,11 @@ def test_tensor_core_m2l(aran, oracle, case, monkeypatch):
             out[kernel] = s.solve(x, q)
             out[kernel + "_stats"] = s.get_stats()
     monkeypatch.delenv("ARAN_M2L_KERNEL")
-    assert rel_l2(out["tc"][0], out["lanes"][0]) < 5e-5
-    assert rel_l2(out["tc"][1], out["lanes"][1]) < 5e-5
+    assert rel_l2(out["tc"][0], out["lanes"][0]) < 2e-6
+    assert rel_l2(out["tc"][1], out["lanes"][1]) < 2e-6
     assert out["tc_stats"] == out["lanes_stats"]
     opot, _ = oracle.solve(x, q, order=p, maxbox=maxbox, field=False, lb=lb, ub=ub)
-    assert rel_l2(out["tc"][0], opot) < 1e-4
+    assert rel_l2(out["tc"][0], opot) < MIXED_TOL
 
 
 @pytest.mark.parametrize("p", [1, 2, 4, 6, 16, 20])
