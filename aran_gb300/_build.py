@@ -14,7 +14,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(ROOT, "_build", "aran_gpu")
 LIB = os.path.join(HERE, "libaran_gpu.so")
-SOURCES = ["tables.cu", "tree.cu", "passes.cu", "p2p.cu", "m2l.cu", "m2l_lanes.cu", "m2l_tc.cu", "kkylin.cu",
+SOURCES = ["tables.cu", "tree.cu", "passes.cu", "p2p.cu", "m2l.cu", "m2l_lanes.cu", "m2l_tc.cu", "m2m_lanes.cu", "kkylin.cu",
            "noalloc.cu", "server.cu", "solver.cu", "compat.cu", "solver2d.cu", "compat2d.cu",
            "semifar.cu", "series3d.cu", "tune.cu", "profiledb.cpp"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")

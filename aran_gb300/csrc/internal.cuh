@@ -143,6 +143,7 @@ struct OpTables {
   DBuf<T> gz, gm;   // gradient coefficients
   DBuf<T> dir_m2l, dir_m2m, dir_l2l;
   DBuf<T> dir_lanes; // lane-parallel M2L stream tables (FP32, m2l_lane_order)
+  DBuf<float> oct_lanes[2];   // lane-parallel M2M / L2L octant-0 stream tables (FP32)
   DBuf<uint8_t> lm; // (l,m) of coefficient index, 2*tri(p+1)
 };
 
@@ -239,6 +240,9 @@ void build_far_lists(AranGpuSolver3d *s);
 // tables.cu
 void build_tables(AranGpuSolver3d *s);
 void build_tables_fp64(AranGpuSolver3d *s);   // FP64 tables beside a mixed solver's FP32 ones
+// offset of part `what` (0 ef, 1 of, 2 ei, 3 oi, 4 ph, 5 rp, 6 stride, 7 vv) in
+// a direction table of kind 0 (M2L), 1 (M2M) or 2 (L2L) at order p
+int dir_offset(int p, int kind, int what);
 // passes.cu
 void run_passes(AranGpuSolver3d *s);
 // kkylin.cu: stage 0 = M2M, 1 = M2L, 2 = L2L
@@ -249,6 +253,14 @@ void kkylin_pass(AranGpuSolver3d *s, int stage);
 void launch_m2l(AranGpuSolver3d *s, bool fp64, int first, int count, cudaStream_t st);
 bool launch_m2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, const int *parents, int count,
                       const cplx<float> *mult, cplx<float> *loc, cudaStream_t st);
+// m2m_lanes.cu: lane-parallel FP32 M2M (parents of depths dhi down to dlo)
+// and L2L (children of depths dlo up to dhi, from depth 3) at the orders
+// m2l_lane_order accepts; false leaves the pass to passes.cu's kernels
+void build_oct_lane_tables(OpTables<float> &tb, cudaStream_t st);
+bool launch_m2m_lanes(AranGpuSolver3d *s, OpTables<float> &tb, cplx<float> *mult, int dhi,
+                      int dlo, cudaStream_t st);
+bool launch_l2l_lanes(AranGpuSolver3d *s, OpTables<float> &tb, cplx<float> *loc, int dlo,
+                      int dhi, cudaStream_t st);
 // m2l_tc.cu: the FP32 M2L on the tensor cores (orders 8 and 12); false
 // leaves it to the other kernels
 bool launch_m2l_tc(AranGpuSolver3d *s, const int *parents, int count, const float *mult,

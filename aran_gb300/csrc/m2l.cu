@@ -26,7 +26,6 @@
 
 namespace aran {
 
-int dir_offset(int p, int kind, int what);
 
 namespace {
 

@@ -17,7 +17,6 @@
 
 namespace aran {
 
-int dir_offset(int p, int kind, int what);
 
 namespace {
 
@@ -557,6 +556,8 @@ void m2m_levels(AranGpuSolver3d *s, OpTables<T> &tb, cplx<T> *mult, int dhi, int
   DevTree &t = s->tree;
   const int p = s->cfg.order;
   const int nm = tri(p), nl = tri(p + 1);
+  if constexpr (sizeof(T) == 4)
+    if (launch_m2m_lanes(s, tb, mult, dhi, dlo, st)) return;
   DirOffsets D = offsets<T>(p, 1);
   size_t sm = ((2 * nl + 15) & ~15) + (size_t)8 * 3 * nm * sizeof(cplx<T>) + 64;
   smem_opt_in(k_m2m_rotate<T>, sm);
@@ -578,6 +579,8 @@ void l2l_levels(AranGpuSolver3d *s, OpTables<T> &tb, cplx<T> *loc, int dlo, int 
   DevTree &t = s->tree;
   const int p = s->cfg.order;
   const int nl = tri(p + 1);
+  if constexpr (sizeof(T) == 4)
+    if (launch_l2l_lanes(s, tb, loc, dlo, dhi, st)) return;
   DirOffsets D = offsets<T>(p, 2);
   const int WPB = 4;
   size_t sm = ((2 * nl + 15) & ~15) + (size_t)WPB * 2 * nl * sizeof(cplx<T>) + 64;

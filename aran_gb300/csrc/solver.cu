@@ -187,12 +187,14 @@ void aran_gpu_solver3d_destroy(AranGpuSolver3d *s) {
     tb->rec.release(); tb->p2mf.release(); tb->vt.release(); tb->vm.release(); tb->vl.release();
     tb->gz.release(); tb->gm.release(); tb->dir_m2l.release(); tb->dir_m2m.release();
     tb->dir_l2l.release(); tb->dir_lanes.release(); tb->lm.release();
+    tb->oct_lanes[0].release(); tb->oct_lanes[1].release();
   }
   {
     auto *tb = &s->t32;
     tb->rec.release(); tb->p2mf.release(); tb->vt.release(); tb->vm.release(); tb->vl.release();
     tb->gz.release(); tb->gm.release(); tb->dir_m2l.release(); tb->dir_m2m.release();
     tb->dir_l2l.release(); tb->dir_lanes.release(); tb->lm.release();
+    tb->oct_lanes[0].release(); tb->oct_lanes[1].release();
   }
   s->keys_in.release(); s->keys_out.release(); s->idx_in.release(); s->perm.release();
   s->cub_tmp.release(); s->sx.release(); s->sy.release(); s->sz.release(); s->sq.release();

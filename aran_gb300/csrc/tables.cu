@@ -311,6 +311,10 @@ void build_tables_t(AranGpuSolver3d *s, OpTables<T> &tb, cudaStream_t st) {
     }
     ACHECK(cudaStreamSynchronize(st));
   }
+  if constexpr (sizeof(T) == 4) {
+    build_oct_lane_tables(tb, st);
+    ACHECK(cudaStreamSynchronize(st));
+  }
   scratch.release();
 }
 
