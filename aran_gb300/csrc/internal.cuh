@@ -110,6 +110,7 @@ struct DevTree {
   DBuf<int> far_off, far_src;         // CSR over nodes
   DBuf<uint16_t> far_dir;             // offset code (dx+3)+7(dy+3)+49(dz+3)
   DBuf<int> leaf_node;                // leaf ordinal -> node
+  DBuf<int> win_leaf;                 // leaf of particle 32 w (windows of 32 particles)
   DBuf<int> near_off, near_rng;       // CSR over leaves of [lf_a, lf_b) ranges (2 ints)
   DBuf<int> m2l_targets;              // nodes with non-empty far lists
   int n_m2l_targets = 0;

@@ -493,6 +493,179 @@ __global__ void k_l2p(int nleaves, const int *__restrict__ leaf_node, const int 
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 L2P (+ gradient) over windows of 32 consecutive particles (leaf
+// order), the order P a compile-time constant: the same evaluation as k_l2p,
+// with every lane busy whatever the leaves' sizes.  Warp w takes particles
+// 32 w .. 32 w + 31, which belong to leaves win_leaf[w] onwards (at most
+// 32 of them); each lane evaluates with its own leaf's coefficients, staged
+// four leaves at a time in shared memory: the local with the m-weight
+// (2 for m > 0) folded in and, for the gradient, the d/dz local and the
+// (d/dx - i d/dy) local's m' = m and m' = -m parts combined per (l, m) into
+// the two real vectors that multiply (Re S, Im S) for its real and
+// imaginary parts (S^{-m} = (-1)^m conj(S^m)).  Each term is formed, then
+// added to its sum once.  The solid harmonics run by degree (outer,
+// unrolled) and order (inner), so every table offset is a constant.
+// ---------------------------------------------------------------------------
+constexpr int kWinSlots = 4;     // leaves staged at a time per warp
+constexpr int kWinWarps = 4;     // warps per block
+
+template <int P, bool FIELD>
+__host__ __device__ constexpr int win_slot() {   // float2 per staged leaf
+  return (P + 1) * (P + 2) / 2 + (FIELD ? 3 * (P * (P + 1) / 2) : 0);
+}
+
+template <int P, bool FIELD>
+__global__ void __launch_bounds__(32 * kWinWarps)
+    k_l2p_win(int64_t n, int nleaves, const int *__restrict__ win_leaf,
+              const int *__restrict__ leaf_node, const int *__restrict__ begin,
+              const uint8_t *__restrict__ depth, const real4<float> *__restrict__ rel,
+              const float *__restrict__ rec_g, const float *__restrict__ gz_g,
+              const float *__restrict__ gm_g, double scale_e, const cplx<float> *__restrict__ loc,
+              double *__restrict__ acc_pot, double *__restrict__ acc_fld) {
+  constexpr int NL = (P + 1) * (P + 2) / 2, NM = P * (P + 1) / 2;
+  constexpr int SLOT = win_slot<P, FIELD>();
+  __shared__ __align__(8) float rec[2 * NL];
+  __shared__ uint8_t lmt[2 * NL];
+  __shared__ float2 coef[kWinWarps][kWinSlots][SLOT];
+  for (int i = threadIdx.x; i < 2 * NL; i += blockDim.x) rec[i] = rec_g[i];
+  for (int c = threadIdx.x; c < NL; c += blockDim.x) {
+    int l = 0;
+    while ((l + 1) * (l + 2) / 2 <= c) ++l;
+    lmt[2 * c] = (uint8_t)l;
+    lmt[2 * c + 1] = (uint8_t)(c - l * (l + 1) / 2);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t wid = (int64_t)blockIdx.x * kWinWarps + w;
+  const int64_t j0 = wid * 32;
+  if (j0 >= n) return;
+  // the window's leaves: lane k holds leaf win_leaf + k (node, first particle)
+  const int L0 = win_leaf[wid];
+  int nd_k = -1;
+  int64_t b_k = INT64_MAX;
+  if (L0 + lane < nleaves) {
+    nd_k = leaf_node[L0 + lane];
+    b_k = begin[nd_k];
+  }
+  // bit i: particle j0 + i starts a leaf after the window's first
+  const unsigned bit = (lane >= 1 && b_k > j0 && b_k < j0 + 32) ? 1u << (int)(b_k - j0) : 0u;
+  const unsigned M = __reduce_or_sync(kFull, bit);
+  const int nslots = __popc(M) + 1;
+  const int64_t j = j0 + lane;
+  const bool act = j < n;
+  const int slot = __popc(M & ((2u << lane) - 1u));
+  const int nd = __shfl_sync(kFull, nd_k, slot);
+  const float ih = inv_scale<float>(act ? depth[nd] : 0, scale_e);
+  const real4<float> r = act ? rel[j] : real4<float>{0.f, 0.f, 0.f, 0.f};
+  const float x = r.x * ih, y = r.y * ih, z = r.z * ih;
+  const float r2 = x * x + y * y + z * z;
+  float phi = 0.f, dz = 0.f, gre = 0.f, gim = 0.f;
+  for (int g0 = 0; g0 < nslots; g0 += kWinSlots) {
+    // stage leaves g0 .. g0 + 3 of the window
+    __syncwarp();
+    for (int sidx = 0; sidx < kWinSlots && g0 + sidx < nslots; ++sidx) {
+      const int node = __shfl_sync(kFull, nd_k, g0 + sidx);
+      const cplx<float> *Lg = loc + (size_t)node * NL;
+      float2 *cf = coef[w][sidx];
+      for (int c = lane; c < NL; c += 32) {
+        const cplx<float> v = Lg[c];
+        const float wm = lmt[2 * c + 1] ? 2.f : 1.f;
+        cf[c] = make_float2(wm * v.re, wm * v.im);
+      }
+      if (FIELD)
+        for (int c = lane; c < NM; c += 32) {
+          const int l = lmt[2 * c], m = lmt[2 * c + 1];
+          const float wm = m ? 2.f : 1.f;
+          // d/dz: L(l+1, m) gz
+          const cplx<float> a = Lg[(l + 1) * (l + 2) / 2 + m];
+          const float gz = gz_g[c];
+          cf[NL + c] = make_float2(wm * gz * a.re, wm * gz * a.im);
+          // (d/dx - i d/dy), m' = m: bp = L(l+1, m+1) gm[l^2 + l + m]
+          const cplx<float> vp = Lg[(l + 1) * (l + 2) / 2 + m + 1];
+          const float gp = gm_g[l * l + l + m];
+          const float bpr = gp * vp.re, bpi = gp * vp.im;
+          // m' = -m (m > 0): source order 1 - m, times (-1)^m for S^{-m}
+          float bnr = 0.f, bni = 0.f;
+          if (m > 0) {
+            const float gn = gm_g[l * l + l - m];
+            cplx<float> u;
+            if (m == 1) u = Lg[(l + 1) * (l + 2) / 2];
+            else {
+              const cplx<float> v = Lg[(l + 1) * (l + 2) / 2 + m - 1];
+              u = ((m - 1) & 1) ? cmake<float>(-v.re, v.im) : cmake<float>(v.re, -v.im);
+            }
+            const float sg = (m & 1) ? -gn : gn;
+            bnr = sg * u.re;
+            bni = sg * u.im;
+          }
+          // real part bp S + bn conj(S): (bpr + bnr) Re S + (bni - bpi) Im S;
+          // imaginary part: (bpi + bni) Re S + (bpr - bnr) Im S
+          cf[NL + NM + c] = make_float2(bpr + bnr, bni - bpi);
+          cf[NL + 2 * NM + c] = make_float2(bpi + bni, bpr - bnr);
+        }
+    }
+    __syncwarp();
+    if (act && slot >= g0 && slot < g0 + kWinSlots) {
+      const float2 *cf = coef[w][slot - g0];
+      // s1[m] = S_{l-1}^m, s2[m] = S_{l-2}^m
+      float s1r[P + 1], s1i[P + 1], s2r[P + 1], s2i[P + 1];
+#pragma unroll
+      for (int l = 0; l <= P; ++l) {
+        // the diagonal term first: S_l^l = a_l (x + i y) S_{l-1}^{l-1}
+        float Sr, Si;
+        if (l == 0) {
+          Sr = rec[0];
+          Si = 0.f;
+        } else {
+          const float a = rec[2 * (l * (l + 1) / 2 + l)];
+          Sr = a * (x * s1r[l - 1] - y * s1i[l - 1]);
+          Si = a * (x * s1i[l - 1] + y * s1r[l - 1]);
+        }
+        float dr[P + 1], di[P + 1];
+        dr[l] = Sr;
+        di[l] = Si;
+#pragma unroll
+        for (int m = 0; m < l; ++m) {
+          const float2 cc = *reinterpret_cast<const float2 *>(&rec[2 * (l * (l + 1) / 2 + m)]);
+          const float t0 = cc.x * z, t1 = cc.y * r2;
+          const float pr = m + 1 < l ? s2r[m] : 0.f, pi = m + 1 < l ? s2i[m] : 0.f;
+          dr[m] = t0 * s1r[m] - t1 * pr;
+          di[m] = t0 * s1i[m] - t1 * pi;
+        }
+#pragma unroll
+        for (int m = 0; m <= l; ++m) {
+          const int c = l * (l + 1) / 2 + m;
+          const float Sr_ = dr[m], Si_ = di[m];
+          const float2 Lv = cf[c];
+          phi += fmaf(Lv.x, Sr_, -Lv.y * Si_);
+          if (FIELD && l < P) {
+            const float2 a = cf[NL + c];
+            dz += fmaf(a.x, Sr_, -a.y * Si_);
+            const float2 gr = cf[NL + NM + c], gi = cf[NL + 2 * NM + c];
+            gre += fmaf(gr.x, Sr_, gr.y * Si_);
+            gim += fmaf(gi.x, Sr_, gi.y * Si_);
+          }
+          if (m < l) {
+            s2r[m] = s1r[m];
+            s2i[m] = s1i[m];
+          }
+          s1r[m] = Sr_;
+          s1i[m] = Si_;
+        }
+      }
+    }
+  }
+  if (act) {
+    acc_pot[j] += (double)phi;
+    if (FIELD) {
+      acc_fld[3 * j] += (double)(gre * ih);
+      acc_fld[3 * j + 1] += (double)(-gim * ih);
+      acc_fld[3 * j + 2] += (double)(dz * ih);
+    }
+  }
+}
+
 __global__ void k_scatter(int64_t n, const int *__restrict__ perm, const double *__restrict__ acc_pot,
                           const double *__restrict__ acc_fld, double *__restrict__ pot,
                           double *__restrict__ fld) {
@@ -731,7 +904,28 @@ void run_passes_t(AranGpuSolver3d *s, OpTables<T> &tb, DBuf<T> &multb, DBuf<T> &
     smem_opt_in(k_l2p<T, true>, sm);
     smem_opt_in(k_l2p<T, false>, sm);
     const int nb = ceil_div(t.nleaves, LPB);
-    if (sizeof(T) == 4 && field && (p == 8 || p == 12)) {
+    if (sizeof(T) == 4 && m2l_lane_order(p)) {
+      // windows of 32 particles, the order folded in at compile time
+      const int64_t nw = (t.n + 31) / 32;
+      const int nbw = (int)ceil_div(nw, (int64_t)kWinWarps);
+      auto run = [&](auto kern) {
+        if (nbw == 0) return;
+        kern<<<nbw, 32 * kWinWarps, 0, st>>>(
+            t.n, t.nleaves, t.win_leaf.ptr, t.leaf_node.ptr, t.begin.ptr, t.depth.ptr,
+            reinterpret_cast<const real4<float> *>(rel), reinterpret_cast<const float *>(tb.rec.ptr),
+            reinterpret_cast<const float *>(tb.gz.ptr), reinterpret_cast<const float *>(tb.gm.ptr),
+            s->scale_e, reinterpret_cast<const cplx<float> *>(loc), s->acc_pot.ptr, s->acc_fld.ptr);
+      };
+      if (field) {
+        if (p == 4) run(k_l2p_win<4, true>);
+        else if (p == 8) run(k_l2p_win<8, true>);
+        else run(k_l2p_win<12, true>);
+      } else {
+        if (p == 4) run(k_l2p_win<4, false>);
+        else if (p == 8) run(k_l2p_win<8, false>);
+        else run(k_l2p_win<12, false>);
+      }
+    } else if (sizeof(T) == 4 && field && (p == 8 || p == 12)) {
       // the bench orders with the order folded in at compile time
       auto kern = p == 8 ? k_l2p<T, true, 8> : k_l2p<T, true, 12>;
       smem_opt_in(kern, sm);

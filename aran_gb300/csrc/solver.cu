@@ -181,7 +181,8 @@ void aran_gpu_solver3d_destroy(AranGpuSolver3d *s) {
   t.key.release(); t.ijk.release(); t.depth.release(); t.begin.release(); t.end.release();
   t.child.release(); t.parent.release(); t.center.release(); t.col.release(); t.ncol.release();
   t.lf_begin.release(); t.lf_end.release(); t.far_off.release(); t.far_src.release();
-  t.far_dir.release(); t.leaf_node.release(); t.near_off.release(); t.near_rng.release();
+  t.far_dir.release(); t.leaf_node.release(); t.win_leaf.release(); t.near_off.release();
+  t.near_rng.release();
   t.m2l_targets.release();
   for (auto *tb : {&s->t64}) {
     tb->rec.release(); tb->p2mf.release(); tb->vt.release(); tb->vm.release(); tb->vl.release();

@@ -300,6 +300,12 @@ __global__ void k_mark_leaf_starts(int nn, const int *__restrict__ begin, const 
   if (child[i] < 0 && end[i] > begin[i]) flags[begin[i]] = 1;
 }
 
+// leaf ordinal of particle 32 w, the first of window w
+__global__ void k_win_leaf(int64_t nw, const int *__restrict__ incl, int *__restrict__ win_leaf) {
+  const int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (w < nw) win_leaf[w] = incl[32 * w] - 1;
+}
+
 __global__ void k_leaf_ranges(int nn, const int *__restrict__ begin, const int *__restrict__ end,
                               const int *__restrict__ child, const int *__restrict__ incl,
                               int *__restrict__ lf_begin, int *__restrict__ lf_end,
@@ -722,6 +728,14 @@ void build_lists(AranGpuSolver3d *s) {
   k_leaf_ranges<<<ceil_div(nn, TB), TB, 0, st>>>(nn, t.begin.ptr, t.end.ptr, t.child.ptr, incl,
                                                   t.lf_begin.ptr, t.lf_end.ptr, t.leaf_node.ptr);
   s->launches++;
+  {
+    const int64_t nw = (n + 31) / 32;
+    t.win_leaf.reserve(nw + 1);
+    if (nw > 0) {
+      k_win_leaf<<<ceil_div(nw, TB), TB, 0, st>>>(nw, incl, t.win_leaf.ptr);
+      s->launches++;
+    }
+  }
   // relative coordinates
   if (s->cfg.precision == ARAN_PRECISION_MIXED) {
     s->rel32.reserve(n);
