@@ -198,6 +198,7 @@ struct AranGpuSolver3d {
   aran::DBuf<int> scan_tmp;
   aran::DBuf<unsigned long long> stats_dev;
   aran::DBuf<int> err_dev;               // device error word (bounded waits)
+  int *h_small = nullptr;                // pinned host words for the solve's small readbacks
   int64_t stats[11] = {};
   double ms[16] = {};
   int64_t launches = 0;

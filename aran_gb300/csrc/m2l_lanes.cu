@@ -214,6 +214,12 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
 
   cplx<float> *my_stg = stg + (size_t)(w * kLanePar + pi_) * NMP;
   float *my_acc = accs + (size_t)w * NL * 32 + lane;   // coefficient c at my_acc[32 c]
+  // up to order 8 the target's local part stays in registers (at order 12
+  // the series already fill them, and it lives in shared memory)
+  constexpr bool RACC = P <= 8;
+  float racc[RACC ? NL : 1];
+#pragma unroll
+  for (int c = 0; c < (RACC ? NL : 1); ++c) racc[c] = 0.f;
   int next_i = 0, next_s = -1;
   auto find_next = [&](int from) {
     for (next_i = from; next_i < nact; ++next_i) {
@@ -394,8 +400,12 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
         for (int mp = 0; mp <= l; ++mp) {
           const float a = o[l * (l + 1) / 2 + mp];
           const float bp = __shfl_xor_sync(kFull, a, 1);
-          float *slot = my_acc + 32 * (l * (l + 1) / 2 + mp);
-          *slot += fmaf(a, cph[mp], bp * sph[mp]);
+          if (RACC) {
+            racc[RACC ? l * (l + 1) / 2 + mp : 0] += fmaf(a, cph[mp], bp * sph[mp]);
+          } else {
+            float *slot = my_acc + 32 * (l * (l + 1) / 2 + mp);
+            *slot += fmaf(a, cph[mp], bp * sph[mp]);
+          }
         }
     }
     __syncwarp();
@@ -420,10 +430,13 @@ __global__ void __launch_bounds__(32 * kLaneWarps, 1)
     // back from the mirror frame: S on the accumulated local
     const float ih = (float)((double)(1ull << depth[tgt]) / scale_e);   // 2^depth / scale
     float *lo = reinterpret_cast<float *>(loc) + (size_t)tgt * NL * 2 + h;
-    for (int l = 0, c = 0; l <= P; ++l)
-      for (int m = 0; m <= l; ++m, ++c) {
+#pragma unroll
+    for (int l = 0; l <= P; ++l)
+#pragma unroll
+      for (int m = 0; m <= l; ++m) {
+        const int c = l * (l + 1) / 2 + m;
         const bool neg = ((bz & (l + m)) ^ (bx & m) ^ (h & (bx ^ by))) & 1;
-        lo[2 * c] = my_acc[32 * c] * (neg ? -ih : ih);
+        lo[2 * c] = (RACC ? racc[RACC ? c : 0] : my_acc[32 * c]) * (neg ? -ih : ih);
       }
   }
 }

@@ -458,9 +458,10 @@ void build_p2p_work(AranGpuSolver3d *s) {
   ACHECK(cudaGetLastError());
   s->launches++;
   // chunk total and heavy-range count, as k_near listed them
-  int hb[2] = {0, 0};
+  int *hb = s->h_small + 8;   // pinned
+  hb[0] = hb[1] = 0;
   if (t.n_near_rng > 0) {
-    ACHECK(cudaMemcpyAsync(hb, t.big_rng.ptr, sizeof(hb), cudaMemcpyDeviceToHost, st));
+    ACHECK(cudaMemcpyAsync(hb, t.big_rng.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     ACHECK(cudaStreamSynchronize(st));
   }
   const int nbig = hb[0], nheavy = hb[1];

@@ -162,6 +162,7 @@ int aran_gpu_solver3d_create(const AranGpuConfig3d *cfg, AranGpuSolver3d **out) 
       build_tables_fp64(s);
     }
     s->err_dev.reserve(4);
+    ACHECK(cudaHostAlloc(&s->h_small, 16 * sizeof(int), cudaHostAllocDefault));
     ACHECK(cudaMemset(s->err_dev.ptr, 0, sizeof(int)));
   } catch (const CudaError &ce) {
     int r = from_cuda(ce);
@@ -177,6 +178,7 @@ void aran_gpu_solver3d_destroy(AranGpuSolver3d *s) {
   cudaSetDevice(s->device);
   if (s->s0) cudaStreamSynchronize(s->s0);
   if (s->s1) cudaStreamSynchronize(s->s1);
+  if (s->h_small) cudaFreeHost(s->h_small);
   DevTree &t = s->tree;
   t.key.release(); t.ijk.release(); t.depth.release(); t.begin.release(); t.end.release();
   t.child.release(); t.parent.release(); t.center.release(); t.col.release(); t.ncol.release();

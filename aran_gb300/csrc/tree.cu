@@ -601,7 +601,8 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
   int off = 0, cnt = nsys;
   DBuf<int> &flags = s->scan_tmp;
   int d = 0;
-  int hostbuf[3] = {0, 0, 0};
+  int *hostbuf = s->h_small;   // pinned: the level's readbacks go together
+  hostbuf[2] = 0;
   while (cnt > 0) {
     t.level_off.push_back(off + cnt);
     flags.reserve(2 * (size_t)cnt + 2);
@@ -718,9 +719,9 @@ void build_lists(AranGpuSolver3d *s) {
                                                        lflags.ptr);
   s->launches++;
   inclusive_scan(s, lflags.ptr, incl, n, st);
-  int nleaves = 0;
-  ACHECK(cudaMemcpyAsync(&nleaves, incl + n - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ACHECK(cudaMemcpyAsync(s->h_small + 3, incl + n - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
   ACHECK(cudaStreamSynchronize(st));
+  const int nleaves = s->h_small[3];
   t.nleaves = nleaves;
   t.lf_begin.reserve(nn);
   t.lf_end.reserve(nn);
@@ -766,15 +767,15 @@ void build_lists(AranGpuSolver3d *s) {
   s->launches++;
   ACHECK(cudaMemsetAsync(cntbuf.ptr + nleaves, 0, sizeof(int), st));
   exclusive_scan(s, cntbuf.ptr, t.near_off.ptr, nleaves + 1, st);
-  int nrng = 0;
-  ACHECK(cudaMemcpyAsync(&nrng, t.near_off.ptr + nleaves, sizeof(int), cudaMemcpyDeviceToHost, st));
-  int nsemi = 0;
+  s->h_small[5] = 0;
+  ACHECK(cudaMemcpyAsync(s->h_small + 4, t.near_off.ptr + nleaves, sizeof(int), cudaMemcpyDeviceToHost, st));
   if (T > 0) {
     ACHECK(cudaMemsetAsync(semi_cnt + nleaves, 0, sizeof(int), st));
     exclusive_scan(s, semi_cnt, t.semi_off.ptr, nleaves + 1, st);
-    ACHECK(cudaMemcpyAsync(&nsemi, t.semi_off.ptr + nleaves, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ACHECK(cudaMemcpyAsync(s->h_small + 5, t.semi_off.ptr + nleaves, sizeof(int), cudaMemcpyDeviceToHost, st));
   }
   ACHECK(cudaStreamSynchronize(st));
+  const int nrng = s->h_small[4], nsemi = s->h_small[5];
   t.n_near_rng = nrng;
   t.n_semi = nsemi;
   t.near_rng.reserve(2 * (size_t)nrng + 2);
@@ -800,9 +801,9 @@ void build_lists(AranGpuSolver3d *s) {
     s->launches++;
     ACHECK(cudaMemsetAsync(fl.ptr + nn, 0, sizeof(int), st));
     exclusive_scan(s, fl.ptr, fl.ptr + nn + 1, nn + 1, st);
-    int np = 0;
-    ACHECK(cudaMemcpyAsync(&np, fl.ptr + nn + 1 + nn, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ACHECK(cudaMemcpyAsync(s->h_small + 6, fl.ptr + nn + 1 + nn, sizeof(int), cudaMemcpyDeviceToHost, st));
     ACHECK(cudaStreamSynchronize(st));
+    const int np = s->h_small[6];
     t.n_parents = np;
     t.parents.reserve(np + 1);
     k_parent_scatter<<<ceil_div(nn, TB), TB, 0, st>>>(nn, fl.ptr, fl.ptr + nn + 1, t.parents.ptr);
