@@ -28,6 +28,7 @@ struct InputError {
 // bits of the solver's device error word
 constexpr int kErrTimeout = 1;     // a bounded mbarrier wait gave up
 constexpr int kErrNonFinite = 2;   // NaN/Inf coordinate or charge
+constexpr int kErrOutside = 4;     // a point outside its system's box (closed)
 
 // sets the thread's last error and returns the status code
 inline int fail(int code, const std::string &msg) {

@@ -47,6 +47,15 @@ __global__ void k_keys(int64_t n, const double *__restrict__ xyz, const double *
   const double *b = sys_box + 9 * lo;
   const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
   if (!(isfinite(x) && isfinite(y) && isfinite(z) && isfinite(q[i]))) atomicOr(err, kErrNonFinite);
+  // outside the closed box (beyond rounding): the key clamps it into a
+  // boundary cell, which the FP64 path evaluates like the oracle, but its
+  // distance from the cell overflows the scaled FP32 expansions
+  {
+    const double lim = (double)(1 << kKeyBits) + 1e-6;
+    const double tx = (x - b[0]) * b[6], ty = (y - b[1]) * b[7], tz = (z - b[2]) * b[8];
+    if (tx < -1e-6 || ty < -1e-6 || tz < -1e-6 || tx > lim || ty > lim || tz > lim)
+      atomicOr(err, kErrOutside);
+  }
   uint64_t qx = (uint64_t)quantise(x, b[0], b[6]);
   uint64_t qy = (uint64_t)quantise(y, b[1], b[7]);
   uint64_t qz = (uint64_t)quantise(z, b[2], b[8]);
@@ -617,6 +626,9 @@ void build_tree(AranGpuSolver3d *s, int64_t n, const double *d_xyz, const double
     if (d == 0) ACHECK(cudaMemcpyAsync(&hostbuf[2], s->err_dev.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
     ACHECK(cudaStreamSynchronize(st));
     if (hostbuf[2] & kErrNonFinite) throw InputError{"a particle coordinate or charge is NaN or infinite"};
+    if ((hostbuf[2] & kErrOutside) && c.precision == ARAN_PRECISION_MIXED)
+      throw InputError{"a particle lies outside the solver's box (mixed precision needs every point "
+                       "inside [lbound, ubound])"};
     int ninternal = hostbuf[0] + hostbuf[1];
     t.level_internal.push_back(ninternal);
     int child_off = off + cnt;

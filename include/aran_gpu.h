@@ -76,7 +76,11 @@ void aran_gpu_solver3d_destroy (AranGpuSolver3d *s);
  * doubles (AoS), q is n doubles; pot (n) and field (3n, AoS) receive the
  * potential sum_j q_j/|xi-xj| and field sum_j -q_j (xi-xj)/|xi-xj|^3 of
  * every particle (either may be NULL).  mem selects host or device pointers;
- * with host pointers the copies are part of the call.  Replaces
+ * with host pointers the copies are part of the call.  A point outside the
+ * closed box [lbound, ubound] is placed in the nearest boundary cell (FP64
+ * solves evaluate it there); a mixed-precision solve returns
+ * ARAN_ERR_INVALID for it instead, before any output is written, as are a
+ * NaN or infinite coordinate or charge.  Replaces
  * aran_solver3d_insert_point x n + aran_solver3d_solve
  * (aran/aransolver3d.c:972-978,1135-1202). */
 int aran_gpu_solver3d_solve (AranGpuSolver3d *s, int64_t n, const double *xyz,

@@ -55,6 +55,7 @@ def concat(sy):
 
 
 @pytest.mark.parametrize("order,precision,flavour", [(8, "fp64", "rotate"), (8, "mixed", "rotate"),
+                                                     (12, "mixed", "rotate"),
                                                      (16, "mixed", "rotate"),
                                                      (6, "mixed", "kkylin")])
 def test_forest_equals_alone(aran, order, precision, flavour):

@@ -150,6 +150,49 @@ def test_tensor_core_m2l(aran, oracle, case, monkeypatch):
     assert rel_l2(out["tc"][0], opot) < MIXED_TOL
 
 
+@pytest.mark.parametrize("p", [4, 8, 12])
+def test_potential_only_matches_field_solve(aran, oracle, p):
+    """At the orders with lane-parallel FP32 kernels the potential-only solve
+    runs its own variants (the windowed L2P without the gradient locals, the
+    near field without the field terms): its potential equals the full
+    solve's to FP32 rounding, and both stay within the mixed tolerance of
+    the oracle."""
+    x, q = W.plummer(30000, 40 + p)
+    lb, ub = (-1, -1, -1), (1, 1, 1)
+    with aran.Solver3d(lb, ub, maxbox=32, order=p, field=False, precision="mixed") as s:
+        pot_only, none = s.solve(x, q)
+    assert none is None
+    with aran.Solver3d(lb, ub, maxbox=32, order=p, field=True, precision="mixed") as s:
+        pot, _ = s.solve(x, q)
+    assert rel_l2(pot_only, pot) < 1e-7
+    opot, _ = oracle.solve(x, q, order=p, maxbox=32, field=False, lb=lb, ub=ub)
+    assert rel_l2(pot_only, opot) < MIXED_TOL
+
+
+def test_points_outside_the_box(aran, oracle):
+    """A point outside the solver's box: the key clamps it into a boundary
+    cell (the oracle's contract), so an FP64 solve still equals the oracle;
+    a mixed solve refuses the input (the point's distance from its cell would
+    overflow the scaled FP32 expansions) with ARAN_ERR_INVALID and writes no
+    output, and the solver stays usable.  Points on the upper bound are
+    inside."""
+    x, q = W.uniform(5000, 77)
+    x[0] = (1.5, 0.5, 0.5)
+    x[1] = (1.0, 1.0, 1.0)
+    with aran.Solver3d(maxbox=32, order=8, field=False, precision="fp64") as s:
+        pot, _ = s.solve(x, q)
+    opot, _ = oracle.solve(x, q, order=8, maxbox=32, field=False)
+    assert rel_l2(pot, opot) < FP64_TOL
+    with aran.Solver3d(maxbox=32, order=8, field=False, precision="mixed") as s:
+        with pytest.raises(aran.AranError) as ei:
+            s.solve(x, q)
+        assert ei.value.code == -1
+        x[0] = (0.5, 0.5, 0.5)
+        pot, _ = s.solve(x, q)
+    opot, _ = oracle.solve(x, q, order=8, maxbox=32, field=False)
+    assert rel_l2(pot, opot) < MIXED_TOL
+
+
 @pytest.mark.parametrize("p", [1, 2, 4, 6, 16, 20])
 def test_orders_fp64(aran, oracle, p):
     x, q = W.uniform(4000, 20 + p)
