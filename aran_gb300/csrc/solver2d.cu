@@ -73,9 +73,13 @@ __device__ __forceinline__ double shfl_sum(double v) {
 
 // ---------------------------------------------------------------- keys/sort
 // per system: lbx, lby, ubx, uby, scale x, scale y
+// a non-finite coordinate or charge sets kErrNonFinite in *err, a point
+// outside its system's closed box kErrOutside (its key is clamped into a
+// boundary cell)
 __global__ void k2_keys(int64_t n, int nsys, const int64_t *__restrict__ offs,
                         const double *__restrict__ sysbox, const double *__restrict__ xy,
-                        uint64_t *__restrict__ keys, int *__restrict__ idx) {
+                        const double *__restrict__ q, uint64_t *__restrict__ keys,
+                        int *__restrict__ idx, int *__restrict__ err) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   // last system s with offs[s] <= i
@@ -85,8 +89,15 @@ __global__ void k2_keys(int64_t n, int nsys, const int64_t *__restrict__ offs,
     if (offs[mid] <= i) lo = mid; else hi = mid;
   }
   const double *b = sysbox + 6 * lo;
-  uint64_t qx = (uint64_t)quantise(xy[2 * i], b[0], b[4]);
-  uint64_t qy = (uint64_t)quantise(xy[2 * i + 1], b[1], b[5]);
+  const double x = xy[2 * i], y = xy[2 * i + 1];
+  if (!(isfinite(x) && isfinite(y) && isfinite(q[i]))) atomicOr(err, kErrNonFinite);
+  {
+    const double lim = (double)(1 << kKeyBits) + 1e-6;
+    const double tx = (x - b[0]) * b[4], ty = (y - b[1]) * b[5];
+    if (tx < -1e-6 || ty < -1e-6 || tx > lim || ty > lim) atomicOr(err, kErrOutside);
+  }
+  uint64_t qx = (uint64_t)quantise(x, b[0], b[4]);
+  uint64_t qy = (uint64_t)quantise(y, b[1], b[5]);
   keys[i] = ((uint64_t)lo << kSysShift) | spread2(qx) | (spread2(qy) << 1);
   idx[i] = (int)i;
 }
@@ -868,6 +879,7 @@ struct AranGpuSolver2d {
   aran::DBuf<double> sysbox;
   aran::DBuf<uint64_t> keys_in, keys_out;
   aran::DBuf<int> idx_in, perm, incl, flags;
+  aran::DBuf<int> err2;   // input checks of the key pass
   aran::DBuf<uint8_t> cub_tmp;
   aran::DBuf<double> sx, sy, sq, io_xy, io_q, io_acc;
   // forest
@@ -983,9 +995,18 @@ void build_forest(AranGpuSolver2d *s, int nsys, const double *dxy, const double 
   s->keys_out.reserve(n);
   s->idx_in.reserve(n);
   s->perm.reserve(n);
-  k2_keys<<<ceil_div(n, TB), TB, 0, st>>>(n, nsys, s->offs.ptr, s->sysbox.ptr, dxy, s->keys_in.ptr,
-                                           s->idx_in.ptr);
+  s->err2.reserve(1);
+  ACHECK(cudaMemsetAsync(s->err2.ptr, 0, sizeof(int), st));
+  k2_keys<<<ceil_div(n, TB), TB, 0, st>>>(n, nsys, s->offs.ptr, s->sysbox.ptr, dxy, dq,
+                                           s->keys_in.ptr, s->idx_in.ptr, s->err2.ptr);
   s->launches++;
+  {
+    const int e = read_int(s->err2.ptr, st);
+    if (e & kErrNonFinite) throw InputError{"a particle coordinate or charge is NaN or infinite"};
+    if ((e & kErrOutside) && s->cfg.precision == ARAN_PRECISION_MIXED)
+      throw InputError{"a particle lies outside its system's box (mixed precision needs every "
+                       "point inside it)"};
+  }
   int sysbits = 1;
   while ((1ll << sysbits) < nsys) ++sysbits;
   size_t bytes = 0;
@@ -1317,6 +1338,7 @@ void aran_gpu_solver2d_destroy(AranGpuSolver2d *s) {
   s->keys_in.release();
   s->keys_out.release();
   s->idx_in.release();
+  s->err2.release();
   s->perm.release();
   s->incl.release();
   s->flags.release();
@@ -1474,6 +1496,11 @@ int solve2d_impl(AranGpuSolver2d *s, int nsys, const int64_t *offs, const double
     s->ms[11] = el(2 * Stage::D2H, 2 * Stage::D2H + 1);
   } catch (const CudaError &ce) {
     return from_cuda(ce);
+  } catch (const InputError &ie) {
+    // stopped after the key pass: nothing was written
+    cudaStreamSynchronize(s->s0);
+    cudaStreamSynchronize(s->s1);
+    return fail(ARAN_ERR_INVALID, ie.msg);
   }
   return ARAN_OK;
 }

@@ -336,7 +336,9 @@ void aran_gpu_solver2d_destroy (AranGpuSolver2d *s);
  * int64, offs[0] = 0, non-decreasing) in the box box[4s .. 4s+3] = (lbx,
  * lby, ubx, uby) (host).  xy is 2n doubles (AoS), q n doubles, acc receives
  * 2n doubles (re, im per particle).  mem selects host or device pointers for
- * xy, q and acc. */
+ * xy, q and acc.  ARAN_ERR_INVALID, before anything is written, for a NaN or
+ * infinite coordinate or charge, and in mixed precision for a point outside
+ * its system's closed box (FP64 places it in the nearest boundary cell). */
 int aran_gpu_solver2d_solve (AranGpuSolver2d *s, int nsys, const int64_t *offs,
                              const double *box, const double *xy, const double *q,
                              double *acc, int mem);

@@ -181,3 +181,32 @@ def test_mixed_forest_systems_and_boxes(aran):
         if b - a < 2:
             continue
         assert rel_l2(a32[a:b], a64[a:b]) < 2e-6, i
+
+
+def test_input_checks_2d(aran):
+    """The 2D key pass refuses a NaN coordinate (both precisions) and, in
+    mixed precision, a point outside its system's box, whose key is clamped
+    into a boundary cell (FP64 evaluates it there); a refused solve writes
+    nothing and leaves the solver usable."""
+    rng = np.random.default_rng(9)
+    xy = rng.uniform(-1, 1, (4000, 2))
+    q = rng.uniform(-1, 1, 4000)
+    offs = np.array([0, 4000], dtype=np.int64)
+    boxes = np.array([[-1.0, -1.0, 1.0, 1.0]])
+    for prec in ("fp64", "mixed"):
+        with aran.Solver2d(maxbox=32, order=12, precision=prec) as s:
+            ref = s.solve(xy, q, offs, boxes)
+            bad = xy.copy()
+            bad[5, 0] = np.nan
+            with pytest.raises(aran.AranError) as ei:
+                s.solve(bad, q, offs, boxes)
+            assert ei.value.code == -1
+            out = xy.copy()
+            out[7] = (1.5, 0.0)
+            if prec == "mixed":
+                with pytest.raises(aran.AranError) as ei:
+                    s.solve(out, q, offs, boxes)
+                assert ei.value.code == -1
+            else:
+                assert np.isfinite(s.solve(out, q, offs, boxes)).all()
+            assert rel_l2(s.solve(xy, q, offs, boxes), ref) < 1e-12
