@@ -838,14 +838,22 @@ def run_gpu(args):
     # written once (FP32 complex), x2 as counted for expansions
     real = 4 if args.precision == "mixed" else 8
     alg_bytes = info["nodes"] * (p * (p + 1) // 2 + (p + 1) * (p + 2) // 2) * 2 * real * 2
+    # the M2L kernel the library ran: ARAN_M2L_KERNEL (lanes, sibling, tc)
+    # where that kernel serves the order, else the default
+    kern_env = os.environ.get("ARAN_M2L_KERNEL", "")
+    if args.precision != "mixed" or p not in (4, 8, 12) or kern_env == "sibling":
+        m2l_kernel = "k_m2l_sibling (rotate M2L, all levels, one launch)"
+    elif kern_env == "tc" and p in (8, 12):
+        m2l_kernel = (f"k_m2l_tc<{p}> (rotate M2L as dense TF32 hi/lo products on tcgen05, "
+                      "all levels, one launch)")
+    else:
+        m2l_kernel = f"k_m2l_lanes<{p}> (rotate M2L, FP32 lane pairs, all levels, one launch)"
     traffic = args.m2l_traffic
-    if traffic is None and args.workload == "plummer4m" and p == 12 and args.precision == "mixed":
+    if (traffic is None and args.workload == "plummer4m" and p == 12
+            and m2l_kernel.startswith("k_m2l_lanes")):
         traffic = M2L_DRAM_BYTES_PLUMMER4M
     roof = {
-        "kernel": ("k_m2l_sibling (rotate M2L, all levels, one launch)"
-                   if os.environ.get("ARAN_M2L_KERNEL") == "sibling" or p not in (8, 12)
-                   or args.precision != "mixed" else
-                   f"k_m2l_lanes<{p}> (rotate M2L, FP32 lane pairs, all levels, one launch)"),
+        "kernel": m2l_kernel,
         "bound": "fp32",
         "achieved": round(achieved, 3), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
         "frac": round(achieved / fp32_peak, 4),
