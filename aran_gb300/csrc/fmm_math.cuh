@@ -142,17 +142,29 @@ FMM_HD uint32_t compact3(uint64_t v) {
   return (uint32_t)v;
 }
 
-FMM_HD int64_t quantise(double x, double lb, double scale) {
+// the point's position in finest cells, (x - lb) * scale, rounded as the
+// oracle rounds it
+FMM_HD double cell_pos(double x, double lb, double scale) {
 #ifdef __CUDA_ARCH__
-  double t = __dmul_rn(__dsub_rn(x, lb), scale);
+  return __dmul_rn(__dsub_rn(x, lb), scale);
 #else
-  double t = (x - lb) * scale;
+  return (x - lb) * scale;
 #endif
-  int64_t i = (int64_t)floor(t);
+}
+
+// the finest cell of position t (cell_pos), not clamped
+FMM_HD int64_t cell_index(double t) { return (int64_t)floor(t); }
+
+// a cell index clamped into the box
+FMM_HD int64_t cell_clamp(int64_t i) {
   if (i < 0) i = 0;
   if (i > (1 << kKeyBits) - 1) i = (1 << kKeyBits) - 1;
   return i;
 }
+
+// a point more than one finest cell outside the closed box (a point on the
+// upper bound, or within rounding of it, is inside)
+FMM_HD bool cell_outside(int64_t i) { return i < -1 || i > (1 << kKeyBits); }
 
 // centre of the node with integer coordinates c at depth d, by repeated
 // halving of the root box [lb, ub] (the oracle performs the same sequence).

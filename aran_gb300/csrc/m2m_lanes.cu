@@ -174,10 +174,12 @@ __global__ void __launch_bounds__(32 * kOctWarps, 1)
         }
       }
     }
-    // translation along z, order by order (real factors, both parts alike)
+    // translation along z, order by order (real factors, both parts alike;
+    // the factors are read four at a time in the order they are stored)
     float z[NC];
     {
-      const float *V = tab + D::VT;
+      const float4 *V4 = reinterpret_cast<const float4 *>(tab + D::VT);
+      float4 vq = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
       for (int m = 0; m < LD; ++m)
 #pragma unroll
@@ -185,8 +187,11 @@ __global__ void __launch_bounds__(32 * kOctWarps, 1)
           float acc = 0.f;
           const int n0 = DOWN ? l : m, n1 = DOWN ? LD - 1 : l;
 #pragma unroll
-          for (int n = n0; n <= n1; ++n)
-            acc = fmaf(V[oct_vidx(LD, DOWN, m, l, n)], y[oct_tri(n) + m], acc);
+          for (int n = n0; n <= n1; ++n) {
+            const int t = oct_vidx(LD, DOWN, m, l, n);
+            if ((t & 3) == 0) vq = V4[t >> 2];
+            acc = fmaf(sel4(vq, t & 3), y[oct_tri(n) + m], acc);
+          }
           z[oct_tri(l) + m] = acc;
         }
     }

@@ -91,13 +91,10 @@ __global__ void k2_keys(int64_t n, int nsys, const int64_t *__restrict__ offs,
   const double *b = sysbox + 6 * lo;
   const double x = xy[2 * i], y = xy[2 * i + 1];
   if (!(isfinite(x) && isfinite(y) && isfinite(q[i]))) atomicOr(err, kErrNonFinite);
-  {
-    const double lim = (double)(1 << kKeyBits) + 1e-6;
-    const double tx = (x - b[0]) * b[4], ty = (y - b[1]) * b[5];
-    if (tx < -1e-6 || ty < -1e-6 || tx > lim || ty > lim) atomicOr(err, kErrOutside);
-  }
-  uint64_t qx = (uint64_t)quantise(x, b[0], b[4]);
-  uint64_t qy = (uint64_t)quantise(y, b[1], b[5]);
+  const int64_t ix = cell_index(cell_pos(x, b[0], b[4])), iy = cell_index(cell_pos(y, b[1], b[5]));
+  if (cell_outside(ix) || cell_outside(iy)) atomicOr(err, kErrOutside);
+  uint64_t qx = (uint64_t)cell_clamp(ix);
+  uint64_t qy = (uint64_t)cell_clamp(iy);
   keys[i] = ((uint64_t)lo << kSysShift) | spread2(qx) | (spread2(qy) << 1);
   idx[i] = (int)i;
 }

@@ -47,18 +47,15 @@ __global__ void k_keys(int64_t n, const double *__restrict__ xyz, const double *
   const double *b = sys_box + 9 * lo;
   const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
   if (!(isfinite(x) && isfinite(y) && isfinite(z) && isfinite(q[i]))) atomicOr(err, kErrNonFinite);
-  // outside the closed box (beyond rounding): the key clamps it into a
-  // boundary cell, which the FP64 path evaluates like the oracle, but its
-  // distance from the cell overflows the scaled FP32 expansions
-  {
-    const double lim = (double)(1 << kKeyBits) + 1e-6;
-    const double tx = (x - b[0]) * b[6], ty = (y - b[1]) * b[7], tz = (z - b[2]) * b[8];
-    if (tx < -1e-6 || ty < -1e-6 || tz < -1e-6 || tx > lim || ty > lim || tz > lim)
-      atomicOr(err, kErrOutside);
-  }
-  uint64_t qx = (uint64_t)quantise(x, b[0], b[6]);
-  uint64_t qy = (uint64_t)quantise(y, b[1], b[7]);
-  uint64_t qz = (uint64_t)quantise(z, b[2], b[8]);
+  const int64_t ix = cell_index(cell_pos(x, b[0], b[6])), iy = cell_index(cell_pos(y, b[1], b[7])),
+                iz = cell_index(cell_pos(z, b[2], b[8]));
+  // outside the box: the key clamps it into a boundary cell, which the FP64
+  // path evaluates like the oracle, but its distance from the cell
+  // overflows the scaled FP32 expansions
+  if (cell_outside(ix) || cell_outside(iy) || cell_outside(iz)) atomicOr(err, kErrOutside);
+  uint64_t qx = (uint64_t)cell_clamp(ix);
+  uint64_t qy = (uint64_t)cell_clamp(iy);
+  uint64_t qz = (uint64_t)cell_clamp(iz);
   keys[i] = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
   idx[i] = (int)i;
 }
