@@ -77,10 +77,10 @@ void aran_gpu_solver3d_destroy (AranGpuSolver3d *s);
  * potential sum_j q_j/|xi-xj| and field sum_j -q_j (xi-xj)/|xi-xj|^3 of
  * every particle (either may be NULL).  mem selects host or device pointers;
  * with host pointers the copies are part of the call.  A point outside the
- * closed box [lbound, ubound] is placed in the nearest boundary cell (FP64
- * solves evaluate it there); a mixed-precision solve returns
- * ARAN_ERR_INVALID for it instead, before any output is written, as are a
- * NaN or infinite coordinate or charge.  Replaces
+ * box [lbound, ubound] is placed in the nearest boundary cell (FP64 solves
+ * evaluate it there); a mixed-precision solve returns ARAN_ERR_INVALID,
+ * before any output is written, for a point more than one finest cell
+ * (box / 2^21) outside it, as for a NaN or infinite coordinate or charge.  Replaces
  * aran_solver3d_insert_point x n + aran_solver3d_solve
  * (aran/aransolver3d.c:972-978,1135-1202). */
 int aran_gpu_solver3d_solve (AranGpuSolver3d *s, int64_t n, const double *xyz,
@@ -337,8 +337,9 @@ void aran_gpu_solver2d_destroy (AranGpuSolver2d *s);
  * lby, ubx, uby) (host).  xy is 2n doubles (AoS), q n doubles, acc receives
  * 2n doubles (re, im per particle).  mem selects host or device pointers for
  * xy, q and acc.  ARAN_ERR_INVALID, before anything is written, for a NaN or
- * infinite coordinate or charge, and in mixed precision for a point outside
- * its system's closed box (FP64 places it in the nearest boundary cell). */
+ * infinite coordinate or charge, and in mixed precision for a point more
+ * than one finest cell outside its system's box (FP64 places it in the
+ * nearest boundary cell). */
 int aran_gpu_solver2d_solve (AranGpuSolver2d *s, int nsys, const int64_t *offs,
                              const double *box, const double *xy, const double *q,
                              double *acc, int mem);
