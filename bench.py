@@ -126,6 +126,18 @@ def stage_rooflines(stage_ms: dict, stats: dict, info: dict, n: int, p: int, fp3
     return out
 
 
+def m2l_kernel_name(precision: str, p: int, choice: str) -> str:
+    """The M2L kernel a solve runs: choice is ARAN_M2L_KERNEL ("lanes",
+    "sibling", "tc" or empty); a kernel that does not serve the order or the
+    precision hands over to the next in tc, lanes, sibling."""
+    if precision != "mixed" or p not in (4, 8, 12) or choice == "sibling":
+        return "k_m2l_sibling (rotate M2L, all levels, one launch)"
+    if choice == "tc" and p in (8, 12):
+        return (f"k_m2l_tc<{p}> (rotate M2L as dense TF32 hi/lo products on tcgen05, "
+                "all levels, one launch)")
+    return f"k_m2l_lanes<{p}> (rotate M2L, FP32 lane pairs, all levels, one launch)"
+
+
 def m2l_flops(p: int) -> int:
     """Algorithmic flops of one rotate-flavour M2L as the GPU applies it:
     2 flops per multiply-add of
@@ -838,16 +850,8 @@ def run_gpu(args):
     # written once (FP32 complex), x2 as counted for expansions
     real = 4 if args.precision == "mixed" else 8
     alg_bytes = info["nodes"] * (p * (p + 1) // 2 + (p + 1) * (p + 2) // 2) * 2 * real * 2
-    # the M2L kernel the library ran: ARAN_M2L_KERNEL (lanes, sibling, tc)
-    # where that kernel serves the order, else the default
-    kern_env = os.environ.get("ARAN_M2L_KERNEL", "")
-    if args.precision != "mixed" or p not in (4, 8, 12) or kern_env == "sibling":
-        m2l_kernel = "k_m2l_sibling (rotate M2L, all levels, one launch)"
-    elif kern_env == "tc" and p in (8, 12):
-        m2l_kernel = (f"k_m2l_tc<{p}> (rotate M2L as dense TF32 hi/lo products on tcgen05, "
-                      "all levels, one launch)")
-    else:
-        m2l_kernel = f"k_m2l_lanes<{p}> (rotate M2L, FP32 lane pairs, all levels, one launch)"
+    # the M2L kernel the library ran
+    m2l_kernel = m2l_kernel_name(args.precision, p, os.environ.get("ARAN_M2L_KERNEL", ""))
     traffic = args.m2l_traffic
     if (traffic is None and args.workload == "plummer4m" and p == 12
             and m2l_kernel.startswith("k_m2l_lanes")):

@@ -78,3 +78,16 @@ def test_stage_rooflines_arithmetic():
     assert r["sort+tree+lists"]["measured_ms"] == 1.5
     total = sum(v["ideal_ms"] for k, v in r.items() if isinstance(v, dict))
     assert abs(r["sum_ideal_over_step"] - total / 10.0) < 1e-3
+
+
+def test_m2l_kernel_name():
+    """The roofline entry names the kernel the library runs for the order,
+    precision and ARAN_M2L_KERNEL choice (tc serves orders 8 and 12, the
+    lane kernel 4, 8 and 12 in mixed precision, the sibling kernel the
+    rest)."""
+    assert bench.m2l_kernel_name("mixed", 12, "").startswith("k_m2l_lanes<12>")
+    assert bench.m2l_kernel_name("mixed", 12, "tc").startswith("k_m2l_tc<12>")
+    assert bench.m2l_kernel_name("mixed", 4, "tc").startswith("k_m2l_lanes<4>")
+    assert bench.m2l_kernel_name("mixed", 8, "sibling").startswith("k_m2l_sibling")
+    assert bench.m2l_kernel_name("mixed", 16, "").startswith("k_m2l_sibling")
+    assert bench.m2l_kernel_name("fp64", 12, "lanes").startswith("k_m2l_sibling")
