@@ -91,3 +91,19 @@ def test_m2l_kernel_name():
     assert bench.m2l_kernel_name("mixed", 8, "sibling").startswith("k_m2l_sibling")
     assert bench.m2l_kernel_name("mixed", 16, "").startswith("k_m2l_sibling")
     assert bench.m2l_kernel_name("fp64", 12, "lanes").startswith("k_m2l_sibling")
+
+
+def test_workloads_inside_their_boxes():
+    """Mixed-precision solves refuse points outside the box, so every bench
+    workload and batch generator stays inside the box it is solved in."""
+    import numpy as np
+    from aran_gb300 import workloads as W
+    for name, (gen, _n, _p, _mb, lb, ub, _d) in bench.WORKLOADS.items():
+        x, _q = getattr(W, gen)(20000, 3)
+        assert (x >= np.array(lb)).all() and (x <= np.array(ub)).all(), name
+    x, _q = W.blobs(20000, 5)
+    assert (x >= 0.0).all() and (x <= 1.0).all()
+    xy, _q, _offs, boxes = W.batch2d(nsys=8)
+    assert (xy >= boxes[0, :2]).all() and (xy <= boxes[0, 2:]).all()
+    for x, _q, _p in W.batch3d(nsys=8, nhi=5e3):
+        assert (x >= 0.0).all() and (x <= 1.0).all()
